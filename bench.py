@@ -1,0 +1,346 @@
+"""Benchmark: |M|^2 evaluations per second of the g g > t t~ g g integrand
+(13 TeV, synthetic gluon PDF, pT > 60 GeV, |eta| < 2.5, Delta R > 0.4) inside
+VEGAS iterations on one GB300, plus the time to reach a 1e-3 relative
+integration error.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--events N] [--impl reference]
+
+A step is one fused VEGAS iteration over --events phase-space points (Philox
+uniforms -> grid map -> phase space -> cuts -> PDF -> |M|^2 -> sums ->
+refinement).  One JSON line is printed by rank 0.  --impl reference times the
+reference's CPU path (the CPU restatement of madflow's integrand, on all host
+cores) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "s to 1e-3 rel. error & |M|^2 evals/s, gg>tt~gg, flow+mixed vs plain VEGAS, 1 GB300"
+MT, WT, ALPHA_S = 173.0, 1.4915000200271606, 0.118
+SQRTS = 13000.0
+CUTS = dict(ptmin=60.0, etamax=2.5, drmin=0.4)
+# Algorithmic flops per phase-space point of the colour-ordered evaluation
+# (all helicities, no sharing across helicities; complex mul 6, add 2,
+# div/sqrt/log 1), counted by the oracle's counting scalar
+# (tests/test_flop_counts.py keeps these in step with it).
+ALG_FLOPS = {2: 23601.0, 3: 356161.0, 4: 5744961.0}
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max clock
+
+
+def workload(events):
+    return {
+        "workload": "g g > t t~ g g, sqrt(S)=13 TeV, synthetic gluon PDF x g=A x^-0.2 (1-x)^5 (100x50 bicubic), "
+        "Q=mt, pT>60, |eta|<2.5, dR(g,g)>0.4, 18-dim ramboflow, VEGAS 50 bins/dim",
+        "events_per_iteration": events,
+        "process": "gg_ttxgg (123 diagrams, 24 colour flows, 64 helicities)",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    from madflow_gb300 import _lib
+    from madflow_gb300.vegas import FusedIntegrand, VegasFlow
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    prec = _lib.MF_PREC_MIXED if args.precision == "mixed" else _lib.MF_PREC_FP64
+    integ = FusedIntegrand(4, kind=1, sqrts=SQRTS, mt=MT, wt=WT, alpha_s=ALPHA_S, precision=prec, **CUTS)
+    N = args.events
+    # replicas: each rank integrates its own Philox stream (stream id = rank)
+    vegas = VegasFlow(integ.n_dim, N, seed=args.seed, stream_id=rank, use_graph=True)
+    vegas.compile(integ)
+    f_out = torch.empty(N, dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
+    npass = torch.zeros((), dtype=torch.int64, device="cuda")
+
+    def step():
+        integ.iteration(vegas.grid, vegas.seed, vegas.stream_id, vegas.iteration, N, vegas.results, f_out=f_out)
+        _lib.call("mf_vegas_refine", vegas.grid.data_ptr(), vegas.results[2:].data_ptr(), vegas.n_dim, vegas.nbins,
+                  vegas.alpha, torch.cuda.current_stream().cuda_stream)
+        vegas.iteration += 1
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    # also time the dominant kernel alone: the fused iteration (events on the same stream)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record()
+            step()
+            ends[i].record()
+            npass += torch.count_nonzero(f_out)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    step_s = sum(ms) / 1000.0
+    if dist:
+        t = torch.tensor([step_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_s = float(t.item())
+        c = npass.clone()
+        dist.all_reduce(c)
+        npass = c
+    n_me = int(npass.item())
+    pass_frac = n_me / (N * args.steps * world)
+    me_per_s = n_me / step_s
+
+    # dominant kernel alone (fused iteration), timed with events on its stream
+    kt0, kt1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kms = []
+    for _ in range(2):
+        flush.zero_()
+        kt0.record()
+        integ.iteration(vegas.grid, vegas.seed, vegas.stream_id, vegas.iteration, N, vegas.results)
+        kt1.record()
+        torch.cuda.synchronize()
+        kms.append(kt0.elapsed_time(kt1))
+    k_s = min(kms) / 1000.0
+    achieved = ALG_FLOPS[4] * N * pass_frac / k_s / 1e12
+
+    # end to end: the integrand contract f(x) with host buffers, copies timed
+    e2e_n = min(N, args.e2e_events)
+    rng = np.random.default_rng(args.seed)
+    x_host = torch.from_numpy(rng.uniform(size=(e2e_n, integ.n_dim))).pin_memory()
+    f_host = torch.empty(e2e_n, dtype=torch.float64).pin_memory()
+    x_dev = torch.empty((e2e_n, integ.n_dim), dtype=torch.float64, device="cuda")
+    f_host_nz = 0
+    for _ in range(1):  # warm-up
+        x_dev.copy_(x_host, non_blocking=True)
+        f_host.copy_(integ(x_dev), non_blocking=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    reps = max(1, args.e2e_reps)
+    for _ in range(reps):
+        x_dev.copy_(x_host, non_blocking=True)
+        f_host.copy_(integ(x_dev), non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    f_host_nz = int((f_host != 0).sum())
+    e2e_s = e0.elapsed_time(e1) / 1000.0
+    e2e_rate = f_host_nz * reps / e2e_s
+
+    peaks = load_peaks()
+    out = {
+        "metric": METRIC,
+        "value": me_per_s,
+        "unit": "|M|^2 evals/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000.0 * step_s / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 (mixed: FP64 momenta, propagators, sums)" if prec == 1 else "f64",
+        "data": "synthetic (Philox4x32-10 uniforms, seed %d)" % args.seed,
+        "config": dict(workload(N), precision=args.precision, l2="flushed (256 MB write) before every step",
+                       parallelism="replicas" if world > 1 else "single GPU"),
+        "pass_fraction": pass_frac,
+        "phase_space_points_per_s": N * args.steps * world / step_s,
+        "wall_s": wall,
+        "gpu_launches": 5 * args.steps,
+        "e2e": {"value": e2e_rate, "unit": "|M|^2 evals/s", "h2d_bytes_per_step": int(x_host.numel() * 8),
+                "d2h_bytes_per_step": int(f_host.numel() * 8), "api": "FusedIntegrand(x) -> f, host buffers"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                     "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": None,
+                     "kernel": "iteration_kernel<4,float>",
+                     "peak_source": "nominal FP32 SIMT (152 SMs x 128 lanes x 2 x 2.07 GHz); "
+                                    "MEASURED_PEAKS.json holds no FP32 figure",
+                     "alg_flops_per_event": ALG_FLOPS[4], "kernel_ms": k_s * 1000.0},
+        "clocks": clk.summary(),
+    }
+    if args.time_to_target:
+        out["time_to_1e-3"] = time_to_target(args, integ, prec)
+    if args.cpu_baseline and rank == 0:
+        out["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+def time_to_target(args, integ, prec, target=1e-3):
+    """Wall-clock seconds of VEGAS iterations until the combined relative
+    error reaches the target (grid adapted from scratch)."""
+    import torch
+
+    from madflow_gb300.vegas import VegasFlow
+
+    v = VegasFlow(integ.n_dim, args.target_events, seed=args.seed + 1, use_graph=True)
+    v.compile(integ)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res, err = v.run_integration(args.max_iter, target_rel_error=target)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"seconds": dt, "iterations": len(v.last_run), "events_per_iteration": args.target_events,
+            "result_pb": res, "error_pb": err, "rel_error": err / abs(res) if res else None,
+            "reached": bool(res and err / abs(res) <= target), "method": "VEGAS",
+            "precision": "mixed" if prec == 1 else "fp64"}
+
+
+def cpu_baseline(args, sample=None):
+    """The CPU restatement of madflow's integrand (oracle, C++/OpenMP over all
+    host cores) on a bounded sample of the same workload."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    n = sample or args.cpu_events
+    plan = oracle.TTNG(4)
+    rng = np.random.default_rng(args.seed)
+    x = rng.uniform(size=(n, 18))
+    cfg = [1, 4, SQRTS, MT, WT, ALPHA_S, CUTS["ptmin"], CUTS["etamax"], CUTS["drmin"], 0]
+    oracle.integrand(cfg, x[: min(64, n)], plan)  # warm-up
+    t0 = time.perf_counter()
+    f = oracle.integrand(cfg, x, plan)
+    dt = time.perf_counter() - t0
+    n_me = int((f != 0).sum())
+    return {"value": n_me / dt, "unit": "|M|^2 evals/s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{n} phase-space points of the same workload ({n_me} pass the cuts), {dt:.1f} s",
+            "seconds": dt}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cb = cpu_baseline(args, args.cpu_events)
+    out = {
+        "metric": METRIC,
+        "value": cb["value"],
+        "unit": cb["unit"],
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000.0 * cb["seconds"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (uniform points, seed %d)" % args.seed,
+        "config": workload(args.events),
+        "impl": "reference",
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--events", type=int, default=2_000_000)
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--cpu-events", type=int, default=4000)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--time-to-target", action="store_true")
+    ap.add_argument("--target-events", type=int, default=1_000_000)
+    ap.add_argument("--max-iter", type=int, default=30)
+    ap.add_argument("--e2e-events", type=int, default=1_000_000)
+    ap.add_argument("--e2e-reps", type=int, default=2)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

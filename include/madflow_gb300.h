@@ -1,0 +1,177 @@
+/* madflow_gb300: C ABI of the GB300 (sm_103a) implementation of madflow's
+ * leading-order integrand and its VEGAS integrator.
+ *
+ * Conventions
+ *   - Every entry point returns an mf_status (0 = MF_OK); no C++ exception or
+ *     abort crosses the ABI.  mf_status_string() names a code.
+ *   - All array arguments are DEVICE pointers owned by the caller unless a
+ *     parameter says "host".  Layouts are structure-of-arrays (SoA): an array
+ *     documented as [a][b][N] holds element (i, j, event e) at
+ *     ((i*b + j)*N + e).
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *     Calls are asynchronous with respect to the host unless stated.
+ *   - Handles are not shared between host threads without external locking;
+ *     distinct handles may be used concurrently.
+ *
+ * Particle order of g g > t t~ + (k-2) g is MadGraph's: 0, 1 incoming gluons,
+ * 2 = t, 3 = t~, 4.. outgoing gluons.  Momenta are (E, px, py, pz), GeV.
+ */
+#ifndef MADFLOW_GB300_H
+#define MADFLOW_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  MF_OK = 0,
+  MF_ERR_ARG = 1,         /* invalid argument (null pointer, size, unsupported value) */
+  MF_ERR_CUDA = 2,        /* a CUDA call failed; see mf_last_cuda_error() */
+  MF_ERR_UNSUPPORTED = 3, /* process / precision not built */
+  MF_ERR_CAPACITY = 4,    /* request exceeds a documented maximum */
+  MF_ERR_NONFINITE = 5    /* non-finite weights were produced (counted and zeroed) */
+} mf_status;
+
+typedef enum { MF_PREC_FP64 = 0, MF_PREC_MIXED = 1 } mf_precision;
+typedef enum { MF_NEWTON_BATCH = 0, MF_NEWTON_PER_EVENT = 1 } mf_newton_rule;
+
+typedef struct mf_process mf_process;
+
+const char* mf_version(void);
+const char* mf_status_string(int status);
+const char* mf_last_cuda_error(void);
+
+/* ---- process handles ------------------------------------------------------
+ * Replaces the generated module madflow's PyOut exporter writes
+ * (madgraph_plugin/template_files/matrix_method_python.inc:56-138, the
+ * Matrix_<proc> class): n_gluons = total number of gluons k (2: g g > t t~,
+ * 3: ... g, 4: ... g g).  precision: MF_PREC_FP64 (all FP64) or MF_PREC_MIXED
+ * (FP32 wavefunctions/vertices/colour sum; FP64 momenta, propagator
+ * denominators and accumulation). */
+int mf_process_create(int n_gluons, int precision, mf_process** out);
+int mf_process_destroy(mf_process* proc);
+/* nexternal, ncomb (helicity combinations), ncolor (colour flows), ndiags;
+ * denominator = the helicity/colour average (matrix_method_python.inc:61-66). */
+int mf_process_info(const mf_process* proc, int* nexternal, int* ncomb, int* ncolor, int* ndiags,
+                    double* denominator);
+/* host out[ncomb][nexternal] (PyOut_exporter.py:288-298 helicity table) */
+int mf_process_helicities(const mf_process* proc, double* out);
+/* host out[ncolor][ncolor], the colour matrix (PyOut_exporter.py:301-324) */
+int mf_process_colour_matrix(const mf_process* proc, double* out);
+
+/* Matrix_<proc>.smatrix(all_ps, mdl_MT, mdl_WT, GC_10, GC_11[, GC_12])
+ * (matrix_method_python.inc:80-104; tests/mockup_debug_me.py:454-480).
+ *   ps        [nexternal][4][N] FP64 momenta
+ *   couplings [N or 1][3] complex as (re, im) pairs: GC_10, GC_11, GC_12;
+ *             coupling_stride = 1 for per-event couplings (running alpha_s),
+ *             0 for one shared set
+ *   out       [N] |M|^2 summed over helicities and colours, averaged
+ *   hel_out   optional [ncomb][N]: per-helicity values of Matrix_<proc>.matrix
+ *             (matrix_method_python.inc:106-138), NULL to skip */
+int mf_smatrix(const mf_process* proc, const double* ps, int64_t n_events, double mdl_MT, double mdl_WT,
+               const double* couplings, int64_t coupling_stride, double* out, double* hel_out, void* stream);
+
+/* ---- phase space (python_package/madflow/phasespace.py) -------------------
+ * rambo (phasespace.py:145-212): x [4*n][N] uniforms, sqrts [N] (or one value
+ * when sqrts_stride = 0), masses host [n] (NULL: massless); p [n][4][N], w [N].
+ * newton_rule MF_NEWTON_BATCH reproduces phasespace.py:84-103 (the loop stops
+ * for the whole batch when one event converges). */
+int mf_rambo(const double* x, int64_t n_events, int n_particles, const double* sqrts, int64_t sqrts_stride,
+             const double* masses, int newton_rule, double* p, double* w, void* stream);
+/* ramboflow (phasespace.py:257-319), nparticles >= 4: x [4*(n-2)+2][N];
+ * p [n][4][N], w [N], x1 [N], x2 [N]. */
+int mf_ramboflow(const double* x, int64_t n_events, int n_particles, double com_sqrts, const double* masses,
+                 int newton_rule, double* p, double* w, double* x1, double* x2, void* stream);
+/* _boost_to_lab (phasespace.py:322-356), in place on p [n][4][N] */
+int mf_boost_to_lab(double* p, int64_t n_events, int n_particles, const double* x1, const double* x2, void* stream);
+
+/* ---- external wavefunctions (python_package/madflow/wavefunctions_flow.py) -
+ * p [4][N]; out [6][2][N] (slot, re/im, event), i.e. the reference's (6, N)
+ * complex128 result.  sxxxxx returns 3 slots ([3][2][N]). */
+int mf_ixxxxx(const double* p, int64_t n, double fmass, double nhel, double nsf, double* out, void* stream);
+int mf_oxxxxx(const double* p, int64_t n, double fmass, double nhel, double nsf, double* out, void* stream);
+int mf_vxxxxx(const double* p, int64_t n, double vmass, double nhel, double nsv, double* out, void* stream);
+int mf_sxxxxx(const double* p, int64_t n, double nss, double* out, void* stream);
+
+/* ---- ALOHA routines (tests/mockup_debug_me.py:43-397) ---------------------
+ * wavefunctions [6][2][N]; coup host (re, im); amplitudes [2][N]. */
+int mf_FFV1_0(const double* F1, const double* F2, const double* V3, const double* coup, int64_t n, double* out,
+              void* stream);
+int mf_FFV1_1(const double* F2, const double* V3, const double* coup, double M1, double W1, int64_t n, double* out,
+              void* stream);
+int mf_FFV1_2(const double* F1, const double* V3, const double* coup, double M2, double W2, int64_t n, double* out,
+              void* stream);
+int mf_VVV1P0_1(const double* V2, const double* V3, const double* coup, double M1, double W1, int64_t n,
+                double* out, void* stream);
+
+/* ---- integrand and VEGAS ---------------------------------------------------
+ * Configuration of the integrand f(x, n_dim, weight) madflow hands to
+ * vegasflow (scripts/madflow_exec.py:422-470; utilities.py:82-86).
+ *   kind 0: g g > t t~ at fixed partonic sqrt(s): rambo over 8 uniforms,
+ *           flux 389379365.6/(2 s) pb (phasespace.py:316-317);
+ *   kind 1: hadronic: ramboflow (x1, x2 + rambo) at sqrt(S), synthetic gluon
+ *           PDF luminosity f(x1) f(x2) / (x1 x2) at Q^2 = q2 (utilities.py:42-53),
+ *           cuts on the outgoing gluons (pT > ptmin, |eta| < etamax,
+ *           Delta R > drmin in the lab frame; <= 0 disables). */
+typedef struct {
+  int kind;
+  double sqrts;
+  double mt, wt;
+  double alpha_s;      /* couplings GC_10 = -g, GC_11 = i g, GC_12 = i g^2, g = 2 sqrt(pi alpha_s) */
+  double ptmin, etamax, drmin;
+  double q2;
+  int newton_rule;
+} mf_integrand_config;
+
+/* Number of integration dimensions of a configuration (8 for kind 0,
+ * 4*(n-2)+2 for kind 1). */
+int mf_integrand_ndim(const mf_process* proc, const mf_integrand_config* cfg, int* ndim);
+
+/* f(x): x [ndim][N] points of the unit hypercube -> f [N] (pb), 0 for events
+ * failing the cuts (madflow_exec.py:466-468 scatters them back as zeros). */
+int mf_integrand(const mf_process* proc, const mf_integrand_config* cfg, const double* x, int64_t n_events,
+                 double* f, void* stream);
+
+/* One VEGAS iteration (Lepage, J. Comput. Phys. 27 (1978) 192), fused:
+ * Philox4x32-10 uniforms (seed, stream id, iteration) -> grid map -> integrand
+ * -> per-iteration sums.  grid [ndim][nbins+1] (device, the bin edges).
+ * results (device) [2 + ndim*nbins]: sum of w = jac*f/N, sum of w^2, and per
+ * bin sums of w^2 (the refinement weights).  f_out optional [N] (jac*f).
+ * u_out optional [ndim][N] float32 copy of the uniforms.
+ * The iteration index is read from the device int *iteration so a captured
+ * CUDA graph can be replayed for successive iterations. */
+int mf_vegas_iteration(const mf_process* proc, const mf_integrand_config* cfg, const double* grid, int nbins,
+                       uint64_t seed, uint32_t stream_id, const int* iteration, int64_t n_events, double* results,
+                       double* f_out, float* u_out, void* stream);
+
+/* VEGAS accumulation for an integrand evaluated by the caller: f [N], jac
+ * [N], bins [ndim][N] (from mf_vegas_sample); results (device)
+ * [2 + ndim*nbins] as in mf_vegas_iteration, with w = f*jac*inv_n.
+ * Deterministic (fixed-order reductions). */
+int mf_vegas_accumulate(const double* f, const double* jac, const int32_t* bins, int64_t n_events, int ndim,
+                        int nbins, double inv_n, double* results, void* stream);
+
+/* Grid refinement of one iteration (device): grid [ndim][nbins+1] updated in
+ * place from the per-bin weights hist [ndim][nbins] with damping alpha. */
+int mf_vegas_refine(double* grid, const double* hist, int ndim, int nbins, double alpha, void* stream);
+
+/* Stand-alone VEGAS map: u [ndim][N] -> x [ndim][N], jac [N], bins
+ * [ndim][N] int32 (bit-exact bin indices for identical uniforms). */
+int mf_vegas_sample(const double* grid, int ndim, int nbins, const double* u, int64_t n_events, double* x,
+                    double* jac, int32_t* bins, void* stream);
+
+/* Philox4x32-10 uniforms in (0,1): u [ndim][N] for events event0.. */
+int mf_philox_uniforms(uint64_t seed, uint32_t stream_id, uint32_t iteration, uint64_t event0, int64_t n_events,
+                       int ndim, double* u, void* stream);
+
+/* Synthetic gluon PDF x g(x) = A x^-0.2 (1-x)^5 (A from the momentum sum rule
+ * int x g dx = 1/2) on a 100 (log x) x 50 (log Q^2) table, bicubic lookup:
+ * x [N], out [N]. */
+int mf_pdf_xfx(const double* x, int64_t n, double q2, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,815 @@
+// C ABI of madflow_gb300 (declared in include/madflow_gb300.h): process
+// handles, phase space, wavefunctions, ALOHA routines, VEGAS and the fused
+// integrand/iteration drivers.  Per-process matrix-element kernels live in
+// mf_proc_k<K>.cu.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/madflow_gb300.h"
+#include "mf_launch.h"
+#include "mf_me.cuh"
+
+namespace {
+thread_local std::string g_cuda_err;
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return MF_OK;
+  g_cuda_err = cudaGetErrorString(e);
+  return MF_ERR_CUDA;
+}
+int last_launch() { return cuda_status(cudaPeekAtLastError()); }
+cudaStream_t S(void* s) { return (cudaStream_t)s; }
+int blocks_for(int64_t n, int threads = 256) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b > 65535LL * 64) b = 65535LL * 64;
+  return (int)(b < 1 ? 1 : b);
+}
+
+// ---- synthetic PDF table, one copy per device ------------------------------
+constexpr int kNX = 100, kNQ = 50;
+struct PdfHost {
+  std::vector<double> tab;
+  double lx0, dlx, lq0, dlq;
+};
+const PdfHost& pdf_host() {
+  static PdfHost P = [] {
+    PdfHost h;
+    double A = 0.5 / std::exp(std::lgamma(0.8) + std::lgamma(6.0) - std::lgamma(6.8));
+    h.lx0 = std::log(1e-6);
+    h.dlx = (0.0 - h.lx0) / (kNX - 1);
+    h.lq0 = std::log(1.0);
+    h.dlq = (std::log(1e10) - h.lq0) / (kNQ - 1);
+    h.tab.resize(kNX * kNQ);
+    for (int iq = 0; iq < kNQ; ++iq)
+      for (int ix = 0; ix < kNX; ++ix) {
+        double x = std::exp(h.lx0 + ix * h.dlx);
+        if (ix == kNX - 1) x = 1.0;
+        h.tab[iq * kNX + ix] = A * std::pow(x, -0.2) * std::pow(1.0 - x, 5.0);
+      }
+    return h;
+  }();
+  return P;
+}
+std::mutex g_pdf_mu;
+double* g_pdf_dev[64] = {nullptr};
+int pdf_device_table(PdfTable& T) {
+  int dev = 0;
+  int st = cuda_status(cudaGetDevice(&dev));
+  if (st) return st;
+  const PdfHost& H = pdf_host();
+  {
+    std::lock_guard<std::mutex> lk(g_pdf_mu);
+    if (!g_pdf_dev[dev]) {
+      double* d = nullptr;
+      st = cuda_status(cudaMalloc(&d, sizeof(double) * kNX * kNQ));
+      if (st) return st;
+      st = cuda_status(cudaMemcpy(d, H.tab.data(), sizeof(double) * kNX * kNQ, cudaMemcpyHostToDevice));
+      if (st) return st;
+      g_pdf_dev[dev] = d;
+    }
+  }
+  T.tab = g_pdf_dev[dev];
+  T.nx = kNX;
+  T.nq = kNQ;
+  T.lx0 = H.lx0;
+  T.dlx = H.dlx;
+  T.lq0 = H.lq0;
+  T.dlq = H.dlq;
+  return MF_OK;
+}
+
+struct Masses {
+  double m[MF_MAX_OUT];
+};
+
+__global__ void set_int_kernel(int* p, int v) { *p = v; }
+
+// ---- phase space kernels ----------------------------------------------------
+// pass 1 of the batch Newton rule for rambo / ramboflow
+__global__ void rambo_conv_kernel(const double* __restrict__ x, int64_t N, int n, const double* __restrict__ sqrts,
+                                  int64_t sstride, Masses M, int flow, double com_s, double shat_min, int* kmin) {
+  int local = 11;
+  MfConsts K = mf_consts(true);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double xe[4 * MF_MAX_OUT + 2];
+    int nd = flow ? 4 * n + 2 : 4 * n;
+    for (int d = 0; d < nd; ++d) xe[d] = x[(int64_t)d * N + e];
+    double roots;
+    const double* xr = xe;
+    if (flow) {
+      double shat, w, x1, x2;
+      get_x1x2(xe[0], xe[1], shat_min, com_s, shat, w, x1, x2);
+      roots = sqrt(shat);
+      xr = xe + 2;
+    } else {
+      roots = sqrts[e * sstride];
+    }
+    double p[MF_MAX_OUT][4];
+    rambo_massless(xr, n, roots, K.pi, p);
+    local = min(local, newton_conv_iter(n, M.m, p, roots, K.acc));
+  }
+  for (int o = 16; o > 0; o >>= 1) local = min(local, __shfl_xor_sync(0xffffffffu, local, o));
+  if ((threadIdx.x & 31) == 0) atomicMin(kmin, local);
+}
+
+// rambo (flow = 0, n outgoing particles in p[n][4][N]) or ramboflow (flow = 1,
+// p[n+2][4][N] with the two incoming partons first).
+__global__ void rambo_kernel(const double* __restrict__ x, int64_t N, int n, const double* __restrict__ sqrts,
+                             int64_t sstride, Masses M, int massive, int flow, double com_s, double shat_min,
+                             const int* __restrict__ kmin, int per_event, double* __restrict__ p,
+                             double* __restrict__ w, double* __restrict__ x1o, double* __restrict__ x2o) {
+  MfConsts K = mf_consts(true);
+  int iters = per_event ? 0 : min(*kmin, 10);
+  int npo = flow ? n + 2 : n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double xe[4 * MF_MAX_OUT + 2];
+    int nd = flow ? 4 * n + 2 : 4 * n;
+    for (int d = 0; d < nd; ++d) xe[d] = x[(int64_t)d * N + e];
+    double roots, shat = 0, wgt = 1.0, x1 = 1, x2 = 1;
+    const double* xr = xe;
+    if (flow) {
+      get_x1x2(xe[0], xe[1], shat_min, com_s, shat, wgt, x1, x2);
+      roots = sqrt(shat);
+      xr = xe + 2;
+    } else {
+      roots = sqrts[e * sstride];
+    }
+    double q[MF_MAX_OUT + 2][4];
+    double(*po)[4] = flow ? q + 2 : q;
+    double logw = rambo_massless(xr, n, roots, K.pi, po);
+    double wps;
+    if (massive) logw = rambo_massive(n, M.m, po, roots, logw, K.acc, iters);
+    wps = exp(logw) / pow(2.0 * K.pi, (double)(3 * n - 4));
+    if (flow) {
+      double ein = roots / 2.0;
+      q[0][0] = ein; q[0][1] = 0; q[0][2] = 0; q[0][3] = ein;
+      q[1][0] = ein; q[1][1] = 0; q[1][2] = 0; q[1][3] = -ein;
+      wgt = wgt * wps;
+      wgt = wgt * K.gev2pb;
+      wgt = wgt / (2.0 * shat);
+      x1o[e] = x1;
+      x2o[e] = x2;
+    } else {
+      wgt = wps;
+    }
+    w[e] = wgt;
+    for (int i = 0; i < npo; ++i)
+      for (int c = 0; c < 4; ++c) p[((int64_t)i * 4 + c) * N + e] = q[i][c];
+  }
+}
+
+__global__ void boost_kernel(double* __restrict__ p, int64_t N, int n, const double* __restrict__ x1,
+                             const double* __restrict__ x2) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x)
+    for (int i = 0; i < n; ++i) {
+      double q[4];
+      for (int c = 0; c < 4; ++c) q[c] = p[((int64_t)i * 4 + c) * N + e];
+      boost_lab(q, x1[e], x2[e]);
+      p[((int64_t)i * 4 + 0) * N + e] = q[0];
+      p[((int64_t)i * 4 + 3) * N + e] = q[3];
+    }
+}
+
+// ---- wavefunction / ALOHA kernels (reference slot layout [6][2][N]) --------
+__device__ __forceinline__ void load_p(const double* p, int64_t N, int64_t e, double* q) {
+  for (int c = 0; c < 4; ++c) q[c] = p[(int64_t)c * N + e];
+}
+__device__ __forceinline__ void store_slot(double* out, int64_t N, int64_t e, int s, cx<double> v) {
+  out[((int64_t)s * 2 + 0) * N + e] = v.re;
+  out[((int64_t)s * 2 + 1) * N + e] = v.im;
+}
+__device__ __forceinline__ cx<double> load_slot(const double* in, int64_t N, int64_t e, int s) {
+  return {in[((int64_t)s * 2 + 0) * N + e], in[((int64_t)s * 2 + 1) * N + e]};
+}
+__device__ __forceinline__ W4<double> load_w4(const double* in, int64_t N, int64_t e) {
+  W4<double> w;
+  for (int k = 0; k < 4; ++k) w.v[k] = load_slot(in, N, e, 2 + k);
+  return w;
+}
+__device__ __forceinline__ void slot_mom(const double* in, int64_t N, int64_t e, double* P) {
+  cx<double> s0 = load_slot(in, N, e, 0), s1 = load_slot(in, N, e, 1);
+  P[0] = s0.re; P[1] = s1.re; P[2] = s1.im; P[3] = s0.im;
+}
+
+__global__ void wf_kernel(int which, const double* __restrict__ p, int64_t N, double m, double nhel, double ns,
+                          double* __restrict__ out) {
+  const double sqh = mf_consts(true).sqh;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double q[4];
+    load_p(p, N, e, q);
+    W4<double> f;
+    double sg = ns;
+    if (which == 0) { f = ixxxxx<double>(q, m, nhel, ns); sg = -ns; }
+    else if (which == 1) f = oxxxxx<double>(q, m, nhel, ns);
+    else if (which == 2) f = vxxxxx<double>(q, m, nhel, ns, sqh);
+    if (which == 3) {
+      store_slot(out, N, e, 0, {q[0] * ns, q[3] * ns});
+      store_slot(out, N, e, 1, {q[1] * ns, q[2] * ns});
+      store_slot(out, N, e, 2, {1.0, 0.0});
+      continue;
+    }
+    store_slot(out, N, e, 0, {q[0] * sg, q[3] * sg});
+    store_slot(out, N, e, 1, {q[1] * sg, q[2] * sg});
+    for (int k = 0; k < 4; ++k) store_slot(out, N, e, 2 + k, f.v[k]);
+  }
+}
+
+// y += S(V)^T F
+__device__ __forceinline__ void svt_add(const W4<double>& V, const W4<double>& F, W4<double>& y) {
+  cx<double> p03 = V.v[0] + V.v[3], m03 = V.v[0] - V.v[3];
+  cx<double> p12 = V.v[1] + mul_i(V.v[2]), m12 = V.v[1] - mul_i(V.v[2]);
+  y.v[0] += m03 * F.v[2] - m12 * F.v[3];
+  y.v[1] += -(p12 * F.v[2]) + p03 * F.v[3];
+  y.v[2] += p03 * F.v[0] + m12 * F.v[1];
+  y.v[3] += p12 * F.v[0] + m03 * F.v[1];
+}
+
+// which: 0 FFV1_0, 1 FFV1_1, 2 FFV1_2, 3 VVV1P0_1
+__global__ void aloha_kernel(int which, const double* __restrict__ A, const double* __restrict__ B,
+                             const double* __restrict__ Cw, cx<double> coup, double M, double W, int64_t N,
+                             double* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    if (which == 0) {
+      cx<double> t = sandwich<double>(load_w4(A, N, e), load_w4(Cw, N, e), load_w4(B, N, e));
+      cx<double> a = coup * mul_mi(t);
+      out[e] = a.re;
+      out[N + e] = a.im;
+      continue;
+    }
+    double Pa[4], Pb[4], Q[4];
+    slot_mom(A, N, e, Pa);
+    slot_mom(B, N, e, Pb);
+    for (int c = 0; c < 4; ++c) Q[c] = Pa[c] + Pb[c];
+    double q2 = Q[0] * Q[0] - Q[1] * Q[1] - Q[2] * Q[2] - Q[3] * Q[3];
+    cx<double> cf = cdiv(mul_i(coup), cx<double>{q2 - M * M, M * W});
+    W4<double> r;
+    if (which == 1) {
+      W4<double> y = w4zero<double>();
+      sv_add<double>(load_w4(B, N, e), load_w4(A, N, e), y);
+      r = topprop<double>(Q, M, cf, y);
+    } else if (which == 2) {
+      W4<double> y = w4zero<double>(), z = w4zero<double>();
+      svt_add(load_w4(B, N, e), load_w4(A, N, e), y);
+      W4<double> mq;  // S(P)^T with P = -Q
+      for (int c = 0; c < 4; ++c) mq.v[c] = {-Q[c], 0.0};
+      svt_add(mq, y, z);
+      for (int c = 0; c < 4; ++c) r.v[c] = cf * (z.v[c] + M * y.v[c]);
+    } else {
+      W4<double> acc = w4zero<double>();
+      vvv_add<double>(load_w4(A, N, e), Pa, load_w4(B, N, e), Pb, acc);
+      for (int c = 0; c < 4; ++c) r.v[c] = cf * acc.v[c];
+    }
+    cx<double> a0 = load_slot(A, N, e, 0), b0 = load_slot(B, N, e, 0);
+    cx<double> a1 = load_slot(A, N, e, 1), b1 = load_slot(B, N, e, 1);
+    store_slot(out, N, e, 0, a0 + b0);
+    store_slot(out, N, e, 1, a1 + b1);
+    for (int c = 0; c < 4; ++c) store_slot(out, N, e, 2 + c, r.v[c]);
+  }
+}
+
+// ---- VEGAS ------------------------------------------------------------------
+__global__ void vegas_sample_kernel(const double* __restrict__ div, int ndim, int nb, const double* __restrict__ u,
+                                    int64_t N, double* __restrict__ x, double* __restrict__ jac,
+                                    int32_t* __restrict__ bins) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double j = 1.0;
+    for (int d = 0; d < ndim; ++d) {
+      double xn = u[(int64_t)d * N + e] * (double)nb;
+      int i = (int)xn;
+      if (i > nb - 1) i = nb - 1;
+      double frac = xn - (double)i;
+      double lo = div[d * (nb + 1) + i];
+      double w = div[d * (nb + 1) + i + 1] - lo;
+      x[(int64_t)d * N + e] = fma(w, frac, lo);
+      j *= w * (double)nb;
+      bins[(int64_t)d * N + e] = i;
+    }
+    jac[e] = j;
+  }
+}
+
+// Lepage refinement, one thread per dimension (smoothing with neighbours,
+// damping ((r-1)/ln r)^alpha, equal-share redistribution of the bin edges).
+__global__ void vegas_refine_kernel(double* __restrict__ div, const double* __restrict__ hist, int ndim, int nb,
+                                    double alpha) {
+  int dim = blockIdx.x * blockDim.x + threadIdx.x;
+  if (dim >= ndim) return;
+  constexpr int NBMAX = 256;
+  double d[NBMAX], r[NBMAX], nd[NBMAX + 1];
+  const double* h = hist + dim * nb;
+  double* g = div + dim * (nb + 1);
+  d[0] = (h[0] + h[1]) / 2.0;
+  for (int i = 1; i < nb - 1; ++i) d[i] = (h[i - 1] + h[i] + h[i + 1]) / 3.0;
+  d[nb - 1] = (h[nb - 2] + h[nb - 1]) / 2.0;
+  double tot = 0.0;
+  for (int i = 0; i < nb; ++i) tot += d[i];
+  if (!(tot > 0.0)) return;
+  double rsum = 0.0;
+  for (int i = 0; i < nb; ++i) {
+    double q = d[i] / tot;
+    r[i] = (q > 0.0) ? pow((q - 1.0) / log(q), alpha) : 0.0;
+    rsum += r[i];
+  }
+  if (!(rsum > 0.0)) return;
+  double per = rsum / (double)nb;
+  nd[0] = g[0];
+  nd[nb] = g[nb];
+  int i = 0;
+  double accum = 0.0;
+  for (int j = 1; j < nb; ++j) {
+    double target = per * (double)j;
+    while (i < nb && accum + r[i] < target) { accum += r[i]; ++i; }
+    if (i >= nb) { nd[j] = g[nb]; continue; }
+    double frac = (target - accum) / r[i];
+    nd[j] = g[i] + frac * (g[i + 1] - g[i]);
+  }
+  for (int j = 0; j <= nb; ++j) g[j] = nd[j];
+}
+
+// Fixed-order sum of the per-block partials: out[i] = sum_b partials[b][i].
+__global__ void reduce_partials_kernel(const double* __restrict__ partials, int nblocks, int width,
+                                       double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= width) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += partials[(int64_t)b * width + i];
+  out[i] = s;
+}
+
+// Deterministic VEGAS accumulation for integrands evaluated outside the fused
+// kernel: block b owns a contiguous slice of events; sums are tree-reduced in
+// a fixed order and each histogram dimension is summed by one thread in event
+// order.
+__global__ void vegas_accum_kernel(const double* __restrict__ f, const double* __restrict__ jac,
+                                   const int32_t* __restrict__ bins, int64_t N, int ndim, int nb, double inv_n,
+                                   double* __restrict__ partials) {
+  extern __shared__ double sh[];  // [ndim*nb] + [2*blockDim]
+  double* hist = sh;
+  double* red = sh + ndim * nb;
+  int width = 2 + ndim * nb;
+  int64_t per = (N + gridDim.x - 1) / gridDim.x;
+  int64_t e0 = (int64_t)blockIdx.x * per, e1 = min(N, e0 + per);
+  for (int i = threadIdx.x; i < ndim * nb; i += blockDim.x) hist[i] = 0.0;
+  double a = 0.0, b = 0.0;
+  for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    double w = f[e] * jac[e] * inv_n;
+    a += w;
+    b += w * w;
+  }
+  red[threadIdx.x] = a;
+  red[blockDim.x + threadIdx.x] = b;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      red[threadIdx.x] += red[threadIdx.x + s];
+      red[blockDim.x + threadIdx.x] += red[blockDim.x + threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  for (int d = threadIdx.x; d < ndim; d += blockDim.x)
+    for (int64_t e = e0; e < e1; ++e) {
+      double w = f[e] * jac[e] * inv_n;
+      hist[d * nb + bins[(int64_t)d * N + e]] += w * w;
+    }
+  __syncthreads();
+  double* out = partials + (int64_t)blockIdx.x * width;
+  if (threadIdx.x == 0) { out[0] = red[0]; out[1] = red[blockDim.x]; }
+  for (int i = threadIdx.x; i < ndim * nb; i += blockDim.x) out[2 + i] = hist[i];
+}
+
+__global__ void philox_kernel(uint64_t seed, uint32_t stream, uint32_t it, uint64_t e0, int64_t N, int ndim,
+                              double* __restrict__ u) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x)
+    for (int d = 0; d < ndim; d += 2) {
+      double a, b;
+      philox_pair(seed, stream, it, e0 + (uint64_t)e, d / 2, a, b);
+      u[(int64_t)d * N + e] = a;
+      if (d + 1 < ndim) u[(int64_t)(d + 1) * N + e] = b;
+    }
+}
+
+__global__ void pdf_kernel(PdfTable P, const double* __restrict__ x, int64_t N, double q2, double* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = pdf_xfx(P, x[e], q2);
+}
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct mf_process {
+  int k, prec;
+  int ncomb, nperm, ndiags;
+  double denominator;
+  std::vector<double> hel, colour;
+  int device;
+  // scratch owned by the handle (grown on demand)
+  int* d_kmin = nullptr;
+  double* d_partials = nullptr;
+  size_t partial_cap = 0;
+  int* d_zero_iter = nullptr;
+};
+
+static const int kDiagrams[6] = {0, 0, 3, 16, 123, 1240};
+
+extern "C" {
+
+const char* mf_version(void) { return "madflow_gb300 0.1 (sm_103a)"; }
+
+const char* mf_status_string(int s) {
+  switch (s) {
+    case MF_OK: return "ok";
+    case MF_ERR_ARG: return "invalid argument";
+    case MF_ERR_CUDA: return "CUDA error";
+    case MF_ERR_UNSUPPORTED: return "unsupported process or precision";
+    case MF_ERR_CAPACITY: return "request exceeds the supported maximum";
+    case MF_ERR_NONFINITE: return "non-finite weights produced";
+  }
+  return "unknown status";
+}
+
+const char* mf_last_cuda_error(void) { return g_cuda_err.c_str(); }
+
+int mf_process_create(int n_gluons, int precision, mf_process** out) {
+  if (!out) return MF_ERR_ARG;
+  *out = nullptr;
+  if (n_gluons < 2 || n_gluons > 4) return MF_ERR_UNSUPPORTED;
+  if (precision != MF_PREC_FP64 && precision != MF_PREC_MIXED) return MF_ERR_ARG;
+  auto* p = new mf_process();
+  p->k = n_gluons;
+  p->prec = precision;
+  const float* cn = nullptr;
+  const signed char* hh = nullptr;
+  double cden = 1.0;
+  mf_host_tables(n_gluons, &p->nperm, &p->ncomb, &p->denominator, &cden, &cn, &hh);
+  p->ndiags = kDiagrams[n_gluons];
+  p->colour.resize((size_t)p->nperm * p->nperm);
+  for (size_t i = 0; i < p->colour.size(); ++i) p->colour[i] = (double)cn[i] / cden;
+  int npart = n_gluons + 2;
+  p->hel.resize((size_t)p->ncomb * npart);
+  for (size_t i = 0; i < p->hel.size(); ++i) p->hel[i] = (double)hh[i];
+  p->device = -1;
+  *out = p;
+  return MF_OK;
+}
+
+int mf_process_destroy(mf_process* p) {
+  if (!p) return MF_ERR_ARG;
+  if (p->d_kmin) cudaFree(p->d_kmin);
+  if (p->d_partials) cudaFree(p->d_partials);
+  if (p->d_zero_iter) cudaFree(p->d_zero_iter);
+  delete p;
+  return MF_OK;
+}
+
+int mf_process_info(const mf_process* p, int* nexternal, int* ncomb, int* ncolor, int* ndiags, double* den) {
+  if (!p) return MF_ERR_ARG;
+  if (nexternal) *nexternal = p->k + 2;
+  if (ncomb) *ncomb = p->ncomb;
+  if (ncolor) *ncolor = p->nperm;
+  if (ndiags) *ndiags = p->ndiags;
+  if (den) *den = p->denominator;
+  return MF_OK;
+}
+
+int mf_process_helicities(const mf_process* p, double* out) {
+  if (!p || !out) return MF_ERR_ARG;
+  std::memcpy(out, p->hel.data(), sizeof(double) * p->hel.size());
+  return MF_OK;
+}
+
+int mf_process_colour_matrix(const mf_process* p, double* out) {
+  if (!p || !out) return MF_ERR_ARG;
+  std::memcpy(out, p->colour.data(), sizeof(double) * p->colour.size());
+  return MF_OK;
+}
+
+int mf_smatrix(const mf_process* p, const double* ps, int64_t N, double mt, double wt, const double* coup,
+               int64_t cstride, double* out, double* hel_out, void* stream) {
+  if (!p || (N > 0 && (!ps || !coup || !out)) || N < 0 || (cstride != 0 && cstride != 1)) return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  int st;
+  switch (p->k) {
+    case 2: st = mf_launch_smatrix_k2(p->prec, ps, N, mt, wt, coup, cstride, out, hel_out, S(stream)); break;
+    case 3: st = mf_launch_smatrix_k3(p->prec, ps, N, mt, wt, coup, cstride, out, hel_out, S(stream)); break;
+    case 4: st = mf_launch_smatrix_k4(p->prec, ps, N, mt, wt, coup, cstride, out, hel_out, S(stream)); break;
+    default: return MF_ERR_UNSUPPORTED;
+  }
+  return st ? last_launch() : MF_OK;
+}
+
+// ---- phase space --------------------------------------------------------------
+static int fill_masses(const double* masses, int n, Masses& M, bool& massive) {
+  massive = false;
+  for (int i = 0; i < MF_MAX_OUT; ++i) M.m[i] = 0.0;
+  if (!masses) return MF_OK;
+  for (int i = 0; i < n; ++i) {
+    // madflow holds the masses list as float_me(masses): float32-rounded
+    M.m[i] = (double)(float)masses[i];
+    if (masses[i] != 0.0) massive = true;
+  }
+  return MF_OK;
+}
+
+// scratch int for the Newton rule: a small per-thread cache keyed by device
+static int newton_scratch(int** out) {
+  static thread_local int* ptr[64] = {nullptr};
+  int dev = 0;
+  int st = cuda_status(cudaGetDevice(&dev));
+  if (st) return st;
+  if (!ptr[dev]) {
+    st = cuda_status(cudaMalloc(&ptr[dev], sizeof(int)));
+    if (st) return st;
+  }
+  *out = ptr[dev];
+  return MF_OK;
+}
+
+static int rambo_common(const double* x, int64_t N, int n, const double* sqrts, int64_t sstride,
+                        const double* masses, int rule, int flow, double com_sqrts, double* p, double* w, double* x1,
+                        double* x2, void* stream) {
+  if (N < 0 || n < 2 || n > MF_MAX_OUT || (N > 0 && (!x || !p || !w))) return MF_ERR_ARG;
+  if (!flow && N > 0 && !sqrts) return MF_ERR_ARG;
+  if (flow && N > 0 && (!x1 || !x2)) return MF_ERR_ARG;
+  if (rule != MF_NEWTON_BATCH && rule != MF_NEWTON_PER_EVENT) return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  Masses M;
+  bool massive;
+  fill_masses(masses, n, M, massive);
+  double msum = 0.0;
+  if (masses)
+    for (int i = 0; i < n; ++i) msum += masses[i];
+  double shat_min = msum * msum, com_s = com_sqrts * com_sqrts;
+  int* kmin = nullptr;
+  int st = newton_scratch(&kmin);
+  if (st) return st;
+  int per_event = rule == MF_NEWTON_PER_EVENT;
+  set_int_kernel<<<1, 1, 0, S(stream)>>>(kmin, 11);
+  if (massive && !per_event)
+    rambo_conv_kernel<<<blocks_for(N), 256, 0, S(stream)>>>(x, N, n, sqrts, sstride, M, flow, com_s, shat_min, kmin);
+  rambo_kernel<<<blocks_for(N), 256, 0, S(stream)>>>(x, N, n, sqrts, sstride, M, massive ? 1 : 0, flow, com_s,
+                                                      shat_min, kmin, per_event, p, w, x1, x2);
+  return last_launch();
+}
+
+int mf_rambo(const double* x, int64_t N, int n, const double* sqrts, int64_t sstride, const double* masses, int rule,
+             double* p, double* w, void* stream) {
+  return rambo_common(x, N, n, sqrts, sstride, masses, rule, 0, 0.0, p, w, nullptr, nullptr, stream);
+}
+
+int mf_ramboflow(const double* x, int64_t N, int npart, double com_sqrts, const double* masses, int rule, double* p,
+                 double* w, double* x1, double* x2, void* stream) {
+  if (npart < 4) return MF_ERR_UNSUPPORTED;
+  return rambo_common(x, N, npart - 2, nullptr, 0, masses, rule, 1, com_sqrts, p, w, x1, x2, stream);
+}
+
+int mf_boost_to_lab(double* p, int64_t N, int n, const double* x1, const double* x2, void* stream) {
+  if (N < 0 || (N > 0 && (!p || !x1 || !x2))) return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  boost_kernel<<<blocks_for(N), 256, 0, S(stream)>>>(p, N, n, x1, x2);
+  return last_launch();
+}
+
+// ---- wavefunctions / ALOHA ------------------------------------------------------
+static int wf_launch(int which, const double* p, int64_t N, double m, double nhel, double ns, double* out,
+                     void* stream) {
+  if (N < 0 || (N > 0 && (!p || !out))) return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  wf_kernel<<<blocks_for(N), 256, 0, S(stream)>>>(which, p, N, m, nhel, ns, out);
+  return last_launch();
+}
+int mf_ixxxxx(const double* p, int64_t n, double fm, double nhel, double nsf, double* out, void* s) {
+  return wf_launch(0, p, n, fm, nhel, nsf, out, s);
+}
+int mf_oxxxxx(const double* p, int64_t n, double fm, double nhel, double nsf, double* out, void* s) {
+  return wf_launch(1, p, n, fm, nhel, nsf, out, s);
+}
+int mf_vxxxxx(const double* p, int64_t n, double vm, double nhel, double nsv, double* out, void* s) {
+  return wf_launch(2, p, n, vm, nhel, nsv, out, s);
+}
+int mf_sxxxxx(const double* p, int64_t n, double nss, double* out, void* s) {
+  return wf_launch(3, p, n, 0.0, 0.0, nss, out, s);
+}
+static int aloha_launch(int which, const double* A, const double* B, const double* C, const double* coup, double M,
+                        double W, int64_t N, double* out, void* stream) {
+  if (N < 0 || !coup || (N > 0 && (!A || !B || !out || (which == 0 && !C)))) return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  aloha_kernel<<<blocks_for(N), 256, 0, S(stream)>>>(which, A, B, C, cx<double>{coup[0], coup[1]}, M, W, N, out);
+  return last_launch();
+}
+int mf_FFV1_0(const double* F1, const double* F2, const double* V3, const double* coup, int64_t n, double* out,
+              void* s) {
+  return aloha_launch(0, F1, F2, V3, coup, 0.0, 0.0, n, out, s);
+}
+int mf_FFV1_1(const double* F2, const double* V3, const double* coup, double M1, double W1, int64_t n, double* out,
+              void* s) {
+  return aloha_launch(1, F2, V3, nullptr, coup, M1, W1, n, out, s);
+}
+int mf_FFV1_2(const double* F1, const double* V3, const double* coup, double M2, double W2, int64_t n, double* out,
+              void* s) {
+  return aloha_launch(2, F1, V3, nullptr, coup, M2, W2, n, out, s);
+}
+int mf_VVV1P0_1(const double* V2, const double* V3, const double* coup, double M1, double W1, int64_t n, double* out,
+                void* s) {
+  return aloha_launch(3, V2, V3, nullptr, coup, M1, W1, n, out, s);
+}
+
+// ---- integrand / VEGAS ----------------------------------------------------------
+int mf_integrand_ndim(const mf_process* p, const mf_integrand_config* c, int* ndim) {
+  if (!p || !c || !ndim) return MF_ERR_ARG;
+  if (c->kind == 0) {
+    if (p->k != 2) return MF_ERR_UNSUPPORTED;
+    *ndim = 8;
+  } else if (c->kind == 1) {
+    *ndim = 4 * p->k + 2;
+  } else {
+    return MF_ERR_ARG;
+  }
+  return MF_OK;
+}
+
+static int ensure_partials(mf_process* p, size_t n) {
+  if (p->partial_cap >= n) return MF_OK;
+  if (p->d_partials) cudaFree(p->d_partials);
+  p->d_partials = nullptr;
+  p->partial_cap = 0;
+  int st = cuda_status(cudaMalloc(&p->d_partials, n * sizeof(double)));
+  if (st) return st;
+  p->partial_cap = n;
+  return MF_OK;
+}
+
+static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, IterArgs& A) {
+  std::memset(&A, 0, sizeof(A));
+  A.kind = c->kind;
+  A.sqrts = c->sqrts;
+  A.mt = c->mt;
+  A.wt = c->wt;
+  double g = 2.0 * std::sqrt(M_PI * c->alpha_s);
+  A.gc10 = {-g, 0.0};
+  A.gc11 = {0.0, g};
+  A.gc12 = {0.0, g * g};
+  for (int i = 0; i < MF_MAX_OUT; ++i) A.masses[i] = 0.0;
+  A.masses[0] = (double)(float)c->mt;
+  A.masses[1] = (double)(float)c->mt;
+  A.shat_min = (2.0 * c->mt) * (2.0 * c->mt);
+  A.ptmin = c->ptmin;
+  A.etamax = c->etamax;
+  A.drmin = c->drmin;
+  A.q2 = c->q2;
+  A.f32q = 1;
+  return pdf_device_table(A.pdf);
+}
+
+static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, double* results, void* stream) {
+  int st;
+  int grid;
+  switch (p->k) {
+    case 2: grid = mf_iteration_grid_k2(p->prec, A.ndim, A.nb, A.N); break;
+    case 3: grid = mf_iteration_grid_k3(p->prec, A.ndim, A.nb, A.N); break;
+    case 4: grid = mf_iteration_grid_k4(p->prec, A.ndim, A.nb, A.N); break;
+    default: return MF_ERR_UNSUPPORTED;
+  }
+  int width = 2 + A.ndim * A.nb;
+  st = ensure_partials(p, (size_t)grid * width);
+  if (st) return st;
+  A.partials = p->d_partials;
+  if (!p->d_kmin) {
+    st = cuda_status(cudaMalloc(&p->d_kmin, sizeof(int)));
+    if (st) return st;
+  }
+  A.newton_iters = p->d_kmin;
+  bool per_event = c->newton_rule == MF_NEWTON_PER_EVENT;
+  set_int_kernel<<<1, 1, 0, S(stream)>>>(p->d_kmin, per_event ? 0 : 11);
+  if (!per_event) {
+    switch (p->k) {
+      case 2: st = mf_launch_newton_k2(A, p->d_kmin, S(stream)); break;
+      case 3: st = mf_launch_newton_k3(A, p->d_kmin, S(stream)); break;
+      case 4: st = mf_launch_newton_k4(A, p->d_kmin, S(stream)); break;
+    }
+    if (st) return last_launch();
+  }
+  switch (p->k) {
+    case 2: st = mf_launch_iteration_k2(p->prec, A, grid, S(stream)); break;
+    case 3: st = mf_launch_iteration_k3(p->prec, A, grid, S(stream)); break;
+    case 4: st = mf_launch_iteration_k4(p->prec, A, grid, S(stream)); break;
+  }
+  if (st) return last_launch();
+  if (results) reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(A.partials, grid, width, results);
+  return last_launch();
+}
+
+int mf_integrand(const mf_process* pc, const mf_integrand_config* c, const double* x, int64_t N, double* f,
+                 void* stream) {
+  mf_process* p = const_cast<mf_process*>(pc);
+  int ndim = 0;
+  if (!p || !c || N < 0 || (N > 0 && (!x || !f))) return MF_ERR_ARG;
+  int st = mf_integrand_ndim(p, c, &ndim);
+  if (st) return st;
+  if (N == 0) return MF_OK;
+  IterArgs A;
+  st = fill_iter_args(p, c, A);
+  if (st) return st;
+  if (!p->d_zero_iter) {
+    st = cuda_status(cudaMalloc(&p->d_zero_iter, sizeof(int)));
+    if (st) return st;
+    st = cuda_status(cudaMemset(p->d_zero_iter, 0, sizeof(int)));
+    if (st) return st;
+  }
+  A.div = nullptr;
+  A.ndim = ndim;
+  A.nb = 1;
+  A.iteration = p->d_zero_iter;
+  A.N = N;
+  A.inv_n = 1.0;
+  A.x_in = x;
+  A.f_out = f;
+  return run_fused(p, A, c, nullptr, stream);
+}
+
+int mf_vegas_iteration(const mf_process* pc, const mf_integrand_config* c, const double* grid, int nb, uint64_t seed,
+                       uint32_t stream_id, const int* iteration, int64_t N, double* results, double* f_out,
+                       float* u_out, void* stream) {
+  mf_process* p = const_cast<mf_process*>(pc);
+  int ndim = 0;
+  if (!p || !c || !grid || !iteration || !results || N <= 0 || nb < 2 || nb > 255) return MF_ERR_ARG;
+  int st = mf_integrand_ndim(p, c, &ndim);
+  if (st) return st;
+  if (ndim > MF_MAX_DIM) return MF_ERR_CAPACITY;
+  IterArgs A;
+  st = fill_iter_args(p, c, A);
+  if (st) return st;
+  A.div = grid;
+  A.ndim = ndim;
+  A.nb = nb;
+  A.seed = seed;
+  A.stream = stream_id;
+  A.iteration = iteration;
+  A.N = N;
+  A.inv_n = 1.0 / (double)N;
+  A.f_out = f_out;
+  A.u_out = u_out;
+  return run_fused(p, A, c, results, stream);
+}
+
+int mf_vegas_accumulate(const double* f, const double* jac, const int32_t* bins, int64_t N, int ndim, int nb,
+                        double inv_n, double* results, void* stream) {
+  if (!f || !jac || !bins || !results || N <= 0 || ndim <= 0 || nb < 2 || ndim * nb > 8192) return MF_ERR_ARG;
+  static thread_local double* part[64] = {nullptr};
+  static thread_local size_t cap[64] = {0};
+  int dev = 0;
+  int st = cuda_status(cudaGetDevice(&dev));
+  if (st) return st;
+  int blocks = 256;
+  int width = 2 + ndim * nb;
+  size_t need = (size_t)blocks * width;
+  if (cap[dev] < need) {
+    if (part[dev]) cudaFree(part[dev]);
+    part[dev] = nullptr;
+    cap[dev] = 0;
+    st = cuda_status(cudaMalloc(&part[dev], need * sizeof(double)));
+    if (st) return st;
+    cap[dev] = need;
+  }
+  size_t shm = (size_t)(ndim * nb + 2 * 256) * sizeof(double);
+  cudaFuncSetAttribute(vegas_accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  vegas_accum_kernel<<<blocks, 256, shm, S(stream)>>>(f, jac, bins, N, ndim, nb, inv_n, part[dev]);
+  reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(part[dev], blocks, width, results);
+  return last_launch();
+}
+
+int mf_vegas_refine(double* grid, const double* hist, int ndim, int nb, double alpha, void* stream) {
+  if (!grid || !hist || ndim <= 0 || nb < 2 || nb > 256) return MF_ERR_ARG;
+  vegas_refine_kernel<<<(ndim + 31) / 32, 32, 0, S(stream)>>>(grid, hist, ndim, nb, alpha);
+  return last_launch();
+}
+
+int mf_vegas_sample(const double* grid, int ndim, int nb, const double* u, int64_t N, double* x, double* jac,
+                    int32_t* bins, void* stream) {
+  if (!grid || ndim <= 0 || nb < 1 || N < 0 || (N > 0 && (!u || !x || !jac || !bins))) return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  vegas_sample_kernel<<<blocks_for(N), 256, 0, S(stream)>>>(grid, ndim, nb, u, N, x, jac, bins);
+  return last_launch();
+}
+
+int mf_philox_uniforms(uint64_t seed, uint32_t stream_id, uint32_t it, uint64_t e0, int64_t N, int ndim, double* u,
+                       void* stream) {
+  if (N < 0 || ndim <= 0 || (N > 0 && !u)) return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  philox_kernel<<<blocks_for(N), 256, 0, S(stream)>>>(seed, stream_id, it, e0, N, ndim, u);
+  return last_launch();
+}
+
+int mf_pdf_xfx(const double* x, int64_t N, double q2, double* out, void* stream) {
+  if (N < 0 || (N > 0 && (!x || !out))) return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  PdfTable P;
+  int st = pdf_device_table(P);
+  if (st) return st;
+  pdf_kernel<<<blocks_for(N), 256, 0, S(stream)>>>(P, x, N, q2, out);
+  return last_launch();
+}
+
+}  // extern "C"

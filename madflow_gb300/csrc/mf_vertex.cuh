@@ -1,0 +1,126 @@
+// Vertex algebra of the colour-ordered recursion, restated from the ALOHA
+// routines madflow runs (tests/mockup_debug_me.py: FFV1_0 :43, FFV1_1 :67,
+// FFV1_2 :207, VVV1P0_1 :341) plus the four-gluon contact term, which has no
+// instance in the reference and follows the QCD Feynman rules.
+//
+// The momentum flow of a current is kept per subset of external legs (the
+// "slot" momentum Q: +p for outgoing, -p for incoming), so the propagator
+// factor of every subset is computed once per event, in FP64, instead of once
+// per current and helicity.  In the HELAS chiral basis the vertex bilinear is
+// F1^T S(V) F2 with S(a) = [[0, a+], [a-, 0]],
+//   a+ = [[a0+a3, a1+i a2], [a1-i a2, a0-a3]],
+//   a- = [[a0-a3, -(a1+i a2)], [-a1+i a2, a0+a3]].
+#pragma once
+#include "mf_common.cuh"
+
+template <class T> MF_D cx<T> mdot(const W4<T>& a, const W4<T>& b) {
+  return a.v[0] * b.v[0] - a.v[1] * b.v[1] - a.v[2] * b.v[2] - a.v[3] * b.v[3];
+}
+template <class T> MF_D cx<T> mdotq(const W4<T>& a, T q0, T q1, T q2, T q3) {
+  return cx<T>{q0 * a.v[0].re - q1 * a.v[1].re - q2 * a.v[2].re - q3 * a.v[3].re,
+               q0 * a.v[0].im - q1 * a.v[1].im - q2 * a.v[2].im - q3 * a.v[3].im};
+}
+
+// Three-gluon colour-ordered current (VVV1P0_1 Lorentz structure), without
+// the propagator/coupling factor: with P2 = Qa, P3 = Qb, P1 = -(Qa+Qb),
+//   acc += (a.b)(Qb-Qa) + a (b.(2Qa+Qb)) - b (a.(Qa+2Qb)).
+template <class T> MF_D void vvv_add(const W4<T>& a, const T* Qa, const W4<T>& b, const T* Qb, W4<T>& acc) {
+  cx<T> ab = mdot(a, b);
+  cx<T> ca = mdotq(b, T(2) * Qa[0] + Qb[0], T(2) * Qa[1] + Qb[1], T(2) * Qa[2] + Qb[2], T(2) * Qa[3] + Qb[3]);
+  cx<T> cb = mdotq(a, Qa[0] + T(2) * Qb[0], Qa[1] + T(2) * Qb[1], Qa[2] + T(2) * Qb[2], Qa[3] + T(2) * Qb[3]);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) acc.v[k] += (Qb[k] - Qa[k]) * ab + a.v[k] * ca - b.v[k] * cb;
+}
+// Four-gluon colour-ordered contact term for the order (a, b, d, off-shell):
+//   acc += 2 b (a.d) - a (b.d) - d (a.b)
+template <class T> MF_D void vvvv_add(const W4<T>& a, const W4<T>& b, const W4<T>& d, W4<T>& acc) {
+  cx<T> ad = mdot(a, d), bd = mdot(b, d), ab = mdot(a, b);
+  cx<T> ad2 = ad + ad;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) acc.v[k] += b.v[k] * ad2 - a.v[k] * bd - d.v[k] * ab;
+}
+template <class T> MF_D W4<T> combine(cx<T> c3, const W4<T>& a3, cx<T> c4, const W4<T>& a4) {
+  W4<T> r;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) r.v[k] = c3 * a3.v[k] + c4 * a4.v[k];
+  return r;
+}
+// y += S(V) F
+template <class T> MF_D void sv_add(const W4<T>& V, const W4<T>& F, W4<T>& y) {
+  cx<T> p03 = V.v[0] + V.v[3], m03 = V.v[0] - V.v[3];
+  cx<T> p12 = V.v[1] + mul_i(V.v[2]), m12 = V.v[1] - mul_i(V.v[2]);
+  y.v[0] += p03 * F.v[2] + p12 * F.v[3];
+  y.v[1] += m12 * F.v[2] + m03 * F.v[3];
+  y.v[2] += m03 * F.v[0] - p12 * F.v[1];
+  y.v[3] += -(m12 * F.v[0]) + p03 * F.v[1];
+}
+// Off-shell top current from y = sum S(V) F: cf * (S(Q) + M) y, with cf the
+// propagator/coupling factor i*GC_11/(Q^2 - M^2 + i M W) (FFV1_1, P1 = -Q).
+template <class T> MF_D W4<T> topprop(const T* Q, T M, cx<T> cf, const W4<T>& y) {
+  T p03 = Q[0] + Q[3], m03 = Q[0] - Q[3];
+  cx<T> p12 = {Q[1], Q[2]}, m12 = {Q[1], -Q[2]};
+  W4<T> z;
+  z.v[0] = p03 * y.v[2] + p12 * y.v[3] + M * y.v[0];
+  z.v[1] = m12 * y.v[2] + m03 * y.v[3] + M * y.v[1];
+  z.v[2] = m03 * y.v[0] - p12 * y.v[1] + M * y.v[2];
+  z.v[3] = -(m12 * y.v[0]) + p03 * y.v[1] + M * y.v[3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) z.v[k] = cf * z.v[k];
+  return z;
+}
+// F1^T S(V) F2 (the FFV1_0 bilinear without its coupling -i*GC_11)
+template <class T> MF_D cx<T> sandwich(const W4<T>& F1, const W4<T>& V, const W4<T>& F2) {
+  W4<T> y = w4zero<T>();
+  sv_add(V, F2, y);
+  return F1.v[0] * y.v[0] + F1.v[1] * y.v[1] + F1.v[2] * y.v[2] + F1.v[3] * y.v[3];
+}
+
+// Per-event data shared by all helicities of one event: slot momenta of every
+// subset of gluons (Qg) and of the top line (Qt = p_t + Qg), and the
+// propagator x coupling factors, evaluated in FP64 and stored in T.
+template <class T, int K> struct EvData {
+  T Qg[1 << K][4];
+  T Qt[1 << K][4];
+  cx<T> gv3[1 << K];   // GC_10 / Qg^2
+  cx<T> gv4[1 << K];   // -i GC_12 / Qg^2
+  cx<T> tden[1 << K];  // i GC_11 / (Qt^2 - M^2 + i M W)
+  T pext[K + 2][4];    // external momenta
+  T mt;
+};
+
+// Slot sign of gluon label j: incoming gluons (particles 0, 1) carry -p.
+template <int K> MF_D int gluon_particle(int j) { return j < 2 ? j : j + 2; }
+
+// Fill subset `s` of EvData from FP64 external momenta p[K+2][4].
+template <class T, int K>
+MF_D void evdata_subset(EvData<T, K>& ev, int s, const double (*p)[4], double mt, double wt, cx<double> gc10,
+                        cx<double> gc11, cx<double> gc12) {
+  double Q[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+    if (s >> j & 1) {
+      int part = gluon_particle<K>(j);
+      double sg = part < 2 ? -1.0 : 1.0;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) Q[c] += sg * p[part][c];
+    }
+  double Qt[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Qt[c] = p[2][c] + Q[c];
+  double q2 = Q[0] * Q[0] - Q[1] * Q[1] - Q[2] * Q[2] - Q[3] * Q[3];
+  double t2 = Qt[0] * Qt[0] - Qt[1] * Qt[1] - Qt[2] * Qt[2] - Qt[3] * Qt[3];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) { ev.Qg[s][c] = (T)Q[c]; ev.Qt[s][c] = (T)Qt[c]; }
+  int nbits = 0;
+  for (int j = 0; j < K; ++j) nbits += (s >> j) & 1;
+  if (nbits >= 2) {
+    double iq = 1.0 / q2;
+    ev.gv3[s] = ccast<T>(cx<double>{gc10.re * iq, gc10.im * iq});
+    ev.gv4[s] = ccast<T>(cx<double>{gc12.im * iq, -gc12.re * iq});
+  } else {
+    ev.gv3[s] = cx<T>{T(0), T(0)};
+    ev.gv4[s] = cx<T>{T(0), T(0)};
+  }
+  cx<double> den = {t2 - mt * mt, mt * wt};
+  ev.tden[s] = ccast<T>(cdiv(mul_i(gc11), den));
+}

@@ -1,0 +1,151 @@
+"""The generated per-process matrix-element modules of madflow, as classes
+backed by the CUDA kernels.
+
+madflow's PyOut exporter writes a ``Matrix_<proc>`` class per process
+(madgraph_plugin/template_files/matrix_method_python.inc:56-138) whose
+``smatrix(all_ps, <masses/widths>, <couplings>)`` returns |M|^2 summed over
+helicities and colours and averaged, and ``matrix(all_ps, hel, ...)`` one
+helicity.  The classes here keep that call for g g > t t~ + n gluons; the
+parameters follow the reference order, sorted masses/widths then sorted
+couplings (PyOut_exporter.py:244, 378-407): mdl_MT, mdl_WT, GC_10, GC_11,
+GC_12.  Couplings may be scalars or per-event complex tensors (running
+alpha_s).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .config import DTYPE, DTYPECOMPLEX, default_precision, device, stream_ptr, to_device
+
+
+class _Process:
+    """Owner of one mf_process handle."""
+
+    def __init__(self, n_gluons, precision):
+        h = ctypes.c_void_p()
+        _lib.call("mf_process_create", n_gluons, precision, ctypes.byref(h))
+        self.h = h
+        vals = [ctypes.c_int() for _ in range(4)]
+        den = ctypes.c_double()
+        _lib.call("mf_process_info", self.h, *[ctypes.byref(v) for v in vals], ctypes.byref(den))
+        self.nexternal, self.ncomb, self.ncolor, self.ndiags = (v.value for v in vals)
+        self.denominator = den.value
+        hel = (ctypes.c_double * (self.ncomb * self.nexternal))()
+        _lib.call("mf_process_helicities", self.h, hel)
+        self.helicities = np.array(hel[:], dtype=np.float64).reshape(self.ncomb, self.nexternal)
+        col = (ctypes.c_double * (self.ncolor * self.ncolor))()
+        _lib.call("mf_process_colour_matrix", self.h, col)
+        self.colour_matrix = np.array(col[:], dtype=np.float64).reshape(self.ncolor, self.ncolor)
+
+    def __del__(self):
+        try:
+            if self.h:
+                _lib.load().mf_process_destroy(self.h)
+        except Exception:
+            pass
+
+
+class MatrixTTNG:
+    """g g > t t~ + (n_gluons - 2) g."""
+
+    n_gluons = 2
+    process_string = "gg_ttx"
+    initial_states = [(21, 21)]
+    mirror_initial_states = False
+
+    def __init__(self, precision=None):
+        self.precision = default_precision() if precision is None else precision
+        self._proc = _Process(self.n_gluons, self.precision)
+        p = self._proc
+        self.nexternal = float(p.nexternal)
+        self.ndiags = float(p.ndiags)
+        self.ncomb = float(p.ncomb)
+        self.helicities = torch.tensor(p.helicities, dtype=DTYPE)
+        self.denominator = float(p.denominator)
+        self.colour_matrix = p.colour_matrix
+
+    def __str__(self):
+        return self.process_string
+
+    @property
+    def handle(self):
+        return self._proc.h
+
+    def _couplings(self, N, GC_10, GC_11, GC_12):
+        cs = []
+        per_event = False
+        for c in (GC_10, GC_11, GC_12):
+            if c is None:
+                c = 0j
+            if isinstance(c, torch.Tensor) and c.numel() > 1:
+                per_event = True
+            cs.append(c)
+        if per_event:
+            cols = []
+            for c in cs:
+                t = torch.as_tensor(c, dtype=DTYPECOMPLEX, device=device()).reshape(-1)
+                cols.append(t.expand(N) if t.numel() == 1 else t)
+            arr = torch.view_as_real(torch.stack(cols, dim=1)).reshape(N, 6).contiguous()
+            return arr, 1
+        flat = []
+        for c in cs:
+            c = complex(c.item() if isinstance(c, torch.Tensor) else c)
+            flat += [c.real, c.imag]
+        return torch.tensor(flat, dtype=DTYPE, device=device()), 0
+
+    def _run(self, all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12, with_hel):
+        ps = to_device(all_ps)
+        if ps.dim() != 3 or ps.shape[1] != self._proc.nexternal or ps.shape[2] != 4:
+            raise ValueError(f"all_ps must have shape (N, {self._proc.nexternal}, 4), got {tuple(ps.shape)}")
+        N = ps.shape[0]
+        soa = ps.permute(1, 2, 0).contiguous()
+        coup, stride = self._couplings(N, GC_10, GC_11, GC_12)
+        out = torch.empty(N, dtype=DTYPE, device=device())
+        hel = torch.empty((self._proc.ncomb, N), dtype=DTYPE, device=device()) if with_hel else None
+        _lib.call("mf_smatrix", self.handle, soa.data_ptr(), N, float(mdl_MT), float(mdl_WT), coup.data_ptr(), stride,
+                  out.data_ptr(), hel.data_ptr() if with_hel else None, stream_ptr())
+        return out, hel
+
+    def smatrix(self, all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12=None):
+        """|M|^2 averaged over initial and summed over final helicities and colours."""
+        return self._run(all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12, False)[0]
+
+    def smatrix_per_helicity(self, all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12=None):
+        """(smatrix, per-helicity matrix values (ncomb, N))."""
+        return self._run(all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12, True)
+
+    def matrix(self, all_ps, hel, mdl_MT, mdl_WT, GC_10, GC_11, GC_12=None):
+        """|M|^2 of one helicity combination, summed over colours."""
+        h = np.asarray(torch.as_tensor(hel).cpu(), dtype=np.float64).reshape(-1)
+        idx = np.where((self._proc.helicities == h).all(axis=1))[0]
+        if len(idx) != 1:
+            raise ValueError(f"helicity {h.tolist()} is not one of the process combinations")
+        _, per = self._run(all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12, True)
+        return per[int(idx[0])]
+
+
+class Matrix_1_gg_ttx(MatrixTTNG):
+    """g g > t t~ (3 diagrams, 2 colour flows, 16 helicities); the process of
+    madflow's frozen test module tests/mockup_debug_me.py:419-543."""
+
+    n_gluons = 2
+    process_string = "1_gg_ttx"
+
+
+class Matrix_1_gg_ttxg(MatrixTTNG):
+    """g g > t t~ g (16 diagrams, 6 colour flows, 32 helicities)."""
+
+    n_gluons = 3
+    process_string = "1_gg_ttxg"
+
+
+class Matrix_1_gg_ttxgg(MatrixTTNG):
+    """g g > t t~ g g (123 diagrams, 24 colour flows, 64 helicities)."""
+
+    n_gluons = 4
+    process_string = "1_gg_ttxgg"
+
+
+PROCESSES = {2: Matrix_1_gg_ttx, 3: Matrix_1_gg_ttxg, 4: Matrix_1_gg_ttxgg}

@@ -894,7 +894,8 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
   cfg.kind = (int)cfgv[0]; cfg.k = (int)cfgv[1]; cfg.sqrts = cfgv[2]; cfg.mt = cfgv[3]; cfg.wt = cfgv[4];
   cfg.alphas = cfgv[5]; cfg.ptmin = cfgv[6]; cfg.etamax = cfgv[7]; cfg.drmin = cfgv[8]; cfg.newton_rule = (int)cfgv[9];
   double gs = 2.0 * std::sqrt(M_PI * cfg.alphas);
-  double prm[12] = {cfg.mt, cfg.wt, -gs, 0.0, 0.0, gs, 0.0, gs * gs, 0.0, -1.0, 0.0, 0.0};
+  // MT, WT, GC_10 = -g, GC_11 = i g, GC_12 = i g^2, c3 = -i, c4 = -1
+  double prm[12] = {cfg.mt, cfg.wt, -gs, 0.0, 0.0, gs, 0.0, gs * gs, 0.0, -1.0, -1.0, 0.0};
   if (cfg.kind == 0) {
     // gg -> tt~ at fixed sqrt(s-hat)
     std::vector<double> pout((size_t)N * 8), w(N), sq(N, cfg.sqrts), p((size_t)N * 16), me(N);

@@ -180,9 +180,11 @@ def smatrix_ggttx(all_ps, mdl_MT, mdl_WT, GC_10, GC_11, per_helicity=False, f32q
 
 # Colour-ordered vertex factors of the tt~ + n g recursion (see mf_oracle.cpp):
 # c3 multiplies GC_10 in the ordered three-gluon current, c4 multiplies GC_12
-# in the ordered four-gluon current.
+# in the ordered four-gluon current.  c3 = -i reproduces the frozen gg -> tt~
+# module; c4 = -1 makes every colour-ordered amplitude gauge invariant and
+# matches the colour-dressed full Feynman rules (tests/test_physics_checks.py).
 C3 = -1j
-C4 = None  # set below once determined
+C4 = -1.0
 
 
 class TTNG:

@@ -1,0 +1,306 @@
+"""Parity of the CUDA library with the reference (golden vectors from madflow's
+own code) and with the CPU oracle, through the C ABI.  Tolerances: FP64 paths
+1e-12 relative (per-event |M|^2) or tighter; VEGAS bin indices and Philox bits
+exact; the mixed-precision |M|^2 path 1e-4 relative max."""
+import numpy as np
+import pytest
+
+from conftest import GC10, GC11, GC12, MT, WT, rel_err, scaled_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def test_rambo_golden(cuda, golden):
+    from madflow_gb300 import phasespace as ps
+
+    for n in range(2, 8):
+        p, w = ps.rambo(golden[f"rambo0_n{n}_x"], n, 7e3)
+        assert scaled_err(_np(p), golden[f"rambo0_n{n}_p"]) < 1e-14
+        assert rel_err(_np(w), golden[f"rambo0_n{n}_w"]) < 1e-13
+    p, w = ps.rambo(golden["rambo0_var_x"], 5, cuda.tensor(golden["rambo0_var_sqrts"]))
+    assert scaled_err(_np(p), golden["rambo0_var_p"]) < 1e-14
+    for name in ["tt", "ttg", "ttgg", "ttggg", "zh", "single"]:
+        meta = golden[f"rambom_{name}_meta"]
+        n, sq, m = int(meta[0]), float(meta[1]), list(meta[2:])
+        p, w = ps.rambo(golden[f"rambom_{name}_x"], n, sq, m)
+        assert scaled_err(_np(p), golden[f"rambom_{name}_p"]) < 1e-14, name
+        assert rel_err(_np(w), golden[f"rambom_{name}_w"]) < 1e-13, name
+
+
+def test_ramboflow_golden(cuda, golden):
+    from madflow_gb300 import phasespace as ps
+
+    for name in ["gg_ttx", "gg_ttxg", "gg_ttxgg", "gg_ttxggg", "massless5"]:
+        meta = golden[f"flow_{name}_meta"]
+        npar, sq, m = int(meta[0]), float(meta[1]), list(meta[2:])
+        m = None if not any(m) else m
+        p, w, x1, x2 = ps.ramboflow(golden[f"flow_{name}_x"], npar, sq, m)
+        assert scaled_err(_np(p), golden[f"flow_{name}_p"]) < 1e-14, name
+        assert rel_err(_np(w), golden[f"flow_{name}_w"]) < 1e-13, name
+        assert rel_err(_np(x1), golden[f"flow_{name}_x1"]) < 1e-15
+
+
+def test_phase_space_generator_golden(cuda, golden):
+    from madflow_gb300 import phasespace as ps
+
+    gen = ps.PhaseSpaceGenerator(5, 7e3, algorithm="ramboflow")
+    gen.register_cut("pt", particle=3, min_val=60, max_val=300.0)
+    p, w, x1, x2, idx = gen(golden["psgen_cut_x"])
+    np.testing.assert_array_equal(_np(idx).ravel(), golden["psgen_cut_idx"].ravel())
+    assert scaled_err(_np(p), golden["psgen_cut_p"]) < 1e-14
+    gen.clear_cuts()
+    full = gen(golden["psgen_cut_x"])[0]
+    assert full.shape[0] == golden["psgen_cut_x"].shape[0]
+    gen2 = ps.PhaseSpaceGenerator(4, 7e3, masses=[50.0, 125.0], com_output=False)
+    p, w, *_ = gen2(golden["psgen_lab_x"])
+    assert scaled_err(_np(p), golden["psgen_lab_p"]) < 1e-13
+    assert rel_err(_np(w), golden["psgen_lab_w"]) < 1e-13
+
+
+def test_empty_batch(cuda):
+    from madflow_gb300 import phasespace as ps
+    from madflow_gb300.matrix import Matrix_1_gg_ttxgg
+
+    p, w = ps.rambo(np.zeros((0, 8)), 2, 1000.0, [MT, MT])
+    assert p.shape == (0, 2, 4) and w.shape == (0,)
+    m = Matrix_1_gg_ttxgg()
+    assert m.smatrix(np.zeros((0, 6, 4)), MT, WT, GC10, GC11, GC12).shape == (0,)
+
+
+def test_wavefunctions_golden(cuda, golden):
+    from madflow_gb300 import wavefunctions as wf
+
+    pw = golden["wf_p"]
+    for mass in (0.0, 173.0):
+        for nhel in (-1.0, 1.0):
+            for ns in (-1.0, 1.0):
+                tag = f"m{int(mass)}_h{int(nhel)}_s{int(ns)}"
+                assert scaled_err(_np(wf.ixxxxx(pw, mass, nhel, ns)), golden[f"wf_ix_{tag}"]) < 1e-15, tag
+                assert scaled_err(_np(wf.oxxxxx(pw, mass, nhel, ns)), golden[f"wf_ox_{tag}"]) < 1e-15, tag
+    for mass in (0.0, 91.0):
+        for nhel in ((-1.0, 1.0, 4.0) if mass == 0.0 else (-1.0, 0.0, 1.0, 4.0)):
+            for nsv in (-1.0, 1.0):
+                tag = f"m{int(mass)}_h{int(nhel)}_s{int(nsv)}"
+                assert scaled_err(_np(wf.vxxxxx(pw, mass, nhel, nsv)), golden[f"wf_vx_{tag}"]) < 1e-15, tag
+
+
+def test_aloha_golden(cuda, golden):
+    from madflow_gb300 import aloha
+
+    fin, fout, v1, v2 = golden["aloha_fin"], golden["aloha_fout"], golden["aloha_v1"], golden["aloha_v2"]
+    assert scaled_err(_np(aloha.FFV1_0(fin, fout, v1, GC11)), golden["aloha_FFV1_0"]) < 1e-14
+    assert scaled_err(_np(aloha.FFV1_1(fout, v1, GC11, MT, WT)), golden["aloha_FFV1_1"]) < 1e-14
+    assert scaled_err(_np(aloha.FFV1_2(fin, v1, GC11, MT, WT)), golden["aloha_FFV1_2"]) < 1e-14
+    out = _np(aloha.VVV1P0_1(v1, v2, GC10, 0.0, 0.0))
+    ref = golden["aloha_VVV1P0_1"]
+    assert np.array_equal(np.isnan(out), np.isnan(ref))
+    assert scaled_err(np.nan_to_num(out), np.nan_to_num(ref)) < 1e-14
+
+
+def test_smatrix_ggttx_golden(cuda, golden):
+    from madflow_gb300.matrix import Matrix_1_gg_ttx
+
+    m = Matrix_1_gg_ttx(precision=0)
+    me = _np(m.smatrix(golden["me_ggttx_p"], MT, WT, GC10, GC11))
+    assert rel_err(me, golden["me_ggttx_smatrix"]) < 1e-12
+    for i, h in enumerate(golden["me_ggttx_helicities"]):
+        mh = _np(m.matrix(golden["me_ggttx_p"][:8], h, MT, WT, GC10, GC11))
+        assert scaled_err(mh, golden["me_ggttx_matrix_hel"][i]) < 1e-12
+    me2 = _np(m.smatrix(golden["flow_gg_ttx_p"], MT, WT, GC10, GC11))
+    assert rel_err(me2, golden["me_flow_ggttx_smatrix"]) < 1e-12
+
+
+@pytest.mark.parametrize("k", [2, 3, 4])
+def test_smatrix_vs_oracle(cuda, oracle, k):
+    from madflow_gb300.matrix import PROCESSES
+
+    rng = np.random.default_rng(30 + k)
+    N = 257  # not a multiple of the tile sizes
+    x = rng.uniform(size=(N, 4 * k + 2))
+    p, *_ = oracle.ramboflow(x, k + 2, 13000.0, [MT, MT] + [0.0] * (k - 2))
+    T = oracle.TTNG(k)
+    ref = T.smatrix(p, T.params(MT, WT, GC10, GC11, GC12))
+    fp64 = _np(PROCESSES[k](precision=0).smatrix(p, MT, WT, GC10, GC11, GC12))
+    assert rel_err(fp64, ref) < 1e-12
+    mixed = _np(PROCESSES[k](precision=1).smatrix(p, MT, WT, GC10, GC11, GC12))
+    assert rel_err(mixed, ref) < 1e-4
+
+
+def test_smatrix_per_event_couplings(cuda, oracle):
+    import torch
+
+    from madflow_gb300.matrix import Matrix_1_gg_ttxg
+
+    rng = np.random.default_rng(3)
+    x = rng.uniform(size=(64, 14))
+    p, *_ = oracle.ramboflow(x, 5, 13000.0, [MT, MT, 0.0])
+    alphas = rng.uniform(0.1, 0.13, size=64)
+    g = 2 * np.sqrt(np.pi * alphas)
+    m = Matrix_1_gg_ttxg(precision=0)
+    dev = torch.device("cuda")
+    me = _np(m.smatrix(p, MT, WT, torch.tensor(-g + 0j, device=dev), torch.tensor(1j * g, device=dev),
+                       torch.tensor(1j * g * g, device=dev)))
+    T = oracle.TTNG(3)
+    for e in (0, 17, 63):
+        ref = T.smatrix(p[e:e + 1], T.params(MT, WT, -g[e], 1j * g[e], 1j * g[e] ** 2))[0]
+        assert abs(me[e] / ref - 1) < 1e-12
+
+
+def test_philox_bits_and_vegas_bins(cuda, oracle):
+    import torch
+
+    from madflow_gb300 import _lib
+
+    N, ndim, nb = 1000, 18, 50
+    u = torch.empty((ndim, N), dtype=torch.float64, device="cuda")
+    _lib.call("mf_philox_uniforms", 4, 0, 3, 17, N, ndim, u.data_ptr(), None)
+    torch.cuda.synchronize()
+    uo = oracle.uniforms(4, 0, 3, 17, N, ndim)
+    np.testing.assert_array_equal(_np(u).T, uo)
+    rng = np.random.default_rng(0)
+    grid = np.sort(np.concatenate([np.zeros((ndim, 1)), rng.uniform(size=(ndim, nb - 1)), np.ones((ndim, 1))], 1), 1)
+    g = torch.tensor(grid, device="cuda")
+    x = torch.empty_like(u)
+    jac = torch.empty(N, dtype=torch.float64, device="cuda")
+    bins = torch.empty((ndim, N), dtype=torch.int32, device="cuda")
+    _lib.call("mf_vegas_sample", g.data_ptr(), ndim, nb, u.data_ptr(), N, x.data_ptr(), jac.data_ptr(),
+              bins.data_ptr(), None)
+    torch.cuda.synchronize()
+    xo, jo, bo = oracle.vegas_sample(grid, uo)
+    np.testing.assert_array_equal(_np(bins).T, bo)
+    np.testing.assert_array_equal(_np(x).T, xo)
+    assert rel_err(_np(jac), jo) < 1e-14
+
+
+def test_vegas_refine_and_accumulate(cuda, oracle):
+    import torch
+
+    from madflow_gb300 import _lib
+
+    rng = np.random.default_rng(1)
+    ndim, nb, N = 6, 50, 5000
+    grid = np.tile(np.linspace(0, 1, nb + 1), (ndim, 1))
+    bins = rng.integers(0, nb, size=(N, ndim)).astype(np.int32)
+    fw = rng.exponential(size=N)
+    jac = np.ones(N)
+    res = torch.empty(2 + ndim * nb, dtype=torch.float64, device="cuda")
+    _lib.call("mf_vegas_accumulate", torch.tensor(fw, device="cuda").data_ptr(),
+              torch.tensor(jac, device="cuda").data_ptr(), torch.tensor(bins.T.copy(), device="cuda").data_ptr(), N,
+              ndim, nb, 1.0, res.data_ptr(), None)
+    torch.cuda.synchronize()
+    sums, hist = oracle.vegas_accumulate(fw, bins, nb)
+    r = _np(res)
+    assert rel_err(r[:2], sums) < 1e-12
+    assert rel_err(r[2:].reshape(ndim, nb), hist) < 1e-12
+    g = torch.tensor(grid, device="cuda")
+    h = torch.tensor(hist, device="cuda")
+    _lib.call("mf_vegas_refine", g.data_ptr(), h.data_ptr(), ndim, nb, 1.5, None)
+    torch.cuda.synchronize()
+    go = oracle.vegas_refine(grid, hist, 1.5)
+    assert scaled_err(_np(g), go) < 1e-13
+    assert np.all(np.diff(_np(g), axis=1) > 0)
+
+
+def test_pdf(cuda, oracle):
+    from madflow_gb300.utilities import synthetic_pdf
+
+    x = np.exp(np.random.default_rng(2).uniform(np.log(1e-6), 0, size=500))
+    assert rel_err(_np(synthetic_pdf(x, MT * MT)), oracle.pdf_xfx(x, MT * MT)) < 1e-13
+
+
+def _cfg_vec(kind, k, sqrts, ptmin=0.0, etamax=0.0, drmin=0.0):
+    return [kind, k, sqrts, MT, WT, 0.118, ptmin, etamax, drmin, 0]
+
+
+@pytest.mark.parametrize("k,cuts", [(3, (30.0, 4.0, 0.0)), (4, (60.0, 2.5, 0.4))])
+def test_integrand_vs_oracle(cuda, oracle, k, cuts):
+    from madflow_gb300.vegas import FusedIntegrand
+
+    integ = FusedIntegrand(k, kind=1, sqrts=13000.0, ptmin=cuts[0], etamax=cuts[1], drmin=cuts[2], precision=0)
+    rng = np.random.default_rng(40 + k)
+    x = rng.uniform(size=(300, integ.n_dim))
+    f = _np(integ(x))
+    fo = oracle.integrand(_cfg_vec(1, k, 13000.0, *cuts), x, oracle.TTNG(k))
+    np.testing.assert_array_equal(f == 0, fo == 0)
+    nz = fo != 0
+    assert nz.sum() > 10
+    assert rel_err(f[nz], fo[nz]) < 1e-12
+
+
+def test_integrand_ggttx_fixed_sqrts(cuda, oracle):
+    from madflow_gb300.vegas import FusedIntegrand
+
+    integ = FusedIntegrand(2, kind=0, sqrts=1000.0, precision=0)
+    x = np.random.default_rng(5).uniform(size=(1000, 8))
+    assert rel_err(_np(integ(x)), oracle.integrand(_cfg_vec(0, 2, 1000.0), x)) < 1e-12
+
+
+def _oracle_iteration(oracle, cfg, plan, grid, seed, it, N, ndim, nb):
+    u = oracle.uniforms(seed, 0, it, 0, N, ndim)
+    x, jac, bins = oracle.vegas_sample(grid, u)
+    f = oracle.integrand(cfg, x, plan)
+    sums, hist = oracle.vegas_accumulate(f * jac / N, bins, nb)
+    return sums, hist
+
+
+def test_fused_iteration_vs_oracle(cuda, oracle):
+    import torch
+
+    from madflow_gb300.vegas import FusedIntegrand
+
+    k, N, nb = 3, 20000, 50
+    integ = FusedIntegrand(k, kind=1, sqrts=13000.0, ptmin=30.0, etamax=4.0, precision=0)
+    ndim = integ.n_dim
+    grid = torch.linspace(0, 1, nb + 1, dtype=torch.float64, device="cuda").repeat(ndim, 1).contiguous()
+    it = torch.tensor([2], dtype=torch.int32, device="cuda")
+    res = torch.empty(2 + ndim * nb, dtype=torch.float64, device="cuda")
+    integ.iteration(grid, 4, 0, it, N, res)
+    r1 = _np(res).copy()
+    integ.iteration(grid, 4, 0, it, N, res)
+    np.testing.assert_array_equal(_np(res), r1)  # bit-reproducible
+    sums, hist = _oracle_iteration(oracle, _cfg_vec(1, k, 13000.0, 30.0, 4.0), oracle.TTNG(k), _np(grid), 4, 2, N,
+                                   ndim, nb)
+    assert rel_err(r1[:2], sums) < 1e-10
+    assert scaled_err(r1[2:].reshape(ndim, nb), hist) < 1e-10
+
+
+def test_vegas_ggttx_integral_vs_oracle(cuda, oracle):
+    """Config-1 integral (g g > t t~ at sqrt(s) = 1 TeV): GPU VEGAS and the
+    oracle's VEGAS replay agree within the combined statistical error."""
+    from madflow_gb300.vegas import FusedIntegrand, VegasFlow
+
+    N, n_iter = 20000, 3
+    integ = FusedIntegrand(2, kind=0, sqrts=1000.0, precision=0)
+    v = VegasFlow(8, N, use_graph=False)
+    v.compile(integ)
+    res, err = v.run_integration(n_iter)
+    # oracle replay of the same iterations (same uniforms, same grid updates)
+    grid = np.tile(np.linspace(0, 1, 51), (8, 1))
+    wsum = wres = 0.0
+    for it in range(n_iter):
+        sums, hist = _oracle_iteration(oracle, _cfg_vec(0, 2, 1000.0), None, grid, 4, it, N, 8, 50)
+        var = (N * sums[1] - sums[0] ** 2) / (N - 1)
+        wsum += 1 / var
+        wres += sums[0] / var
+        grid = oracle.vegas_refine(grid, hist, 1.5)
+    ro, eo = wres / wsum, 1 / np.sqrt(wsum)
+    assert abs(res - ro) < 1e-9 * abs(ro)  # same samples: agreement far inside the error
+    assert abs(res - ro) < 3 * np.hypot(err, eo)
+    assert err / res < 0.01
+
+
+def test_cuda_graph_replay_matches(cuda):
+    from madflow_gb300.vegas import FusedIntegrand, VegasFlow
+
+    integ = FusedIntegrand(2, kind=0, sqrts=1000.0, precision=1)
+    a = VegasFlow(8, 30000, use_graph=False)
+    a.compile(integ)
+    ra = a.run_integration(4)
+    b = VegasFlow(8, 30000, use_graph=True)
+    b.compile(integ)
+    rb = b.run_integration(4)
+    assert ra == rb

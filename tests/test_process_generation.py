@@ -1,0 +1,88 @@
+"""The process generator (colour matrix, helicities, diagram counts) and the
+generated recursion, compiled as host code, against the oracle (CPU only)."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GC10, GC11, GC12, MT, ROOT, WT
+from madflow_gb300 import codegen
+
+
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
+def test_colour_matrix_exact_vs_numeric(oracle, k):
+    num, den = codegen.colour_matrix(k)
+    C = np.array(num, dtype=np.float64) / den
+    np.testing.assert_allclose(C, oracle.colour_matrix(k), atol=1e-12 * np.abs(C).max())
+    assert np.array_equal(C, C.T)
+
+
+def test_colour_matrix_ggttx_matches_reference():
+    # tests/mockup_debug_me.py:506-507: cf = [[16,-2],[-2,16]], denom = 3
+    num, den = codegen.colour_matrix(2)
+    assert den == 3 and num == [[16, -2], [-2, 16]]
+
+
+def test_diagram_counts():
+    for k, n in codegen.KNOWN_DIAGRAMS.items():
+        assert codegen.diagram_count(k) == n
+
+
+def test_helicities_match_reference_order(golden, oracle):
+    np.testing.assert_array_equal(np.array(codegen.helicities(2)), golden["me_ggttx_helicities"])
+    for k in (3, 4):
+        np.testing.assert_array_equal(np.array(codegen.helicities(k)), oracle.TTNG(k).helicities)
+
+
+def test_denominators():
+    assert codegen.denominator(2) == 256
+    assert codegen.denominator(4) == 512  # identical final-state gluons
+
+
+def test_colour_matrix_bf16_tf32_exact():
+    """The integer colour numerators are exact in TF32 (10-bit mantissa) for
+    24 flows: no split precision is needed for the matrix itself."""
+    num, _ = codegen.colour_matrix(4)
+    vals = np.unique(np.abs(np.array(num)))
+    assert np.all(vals < 2**11)
+
+
+HOST_SO = os.path.join(ROOT, "tests", "host", "_build", "libme_host.so")
+
+
+@pytest.fixture(scope="module")
+def host_lib():
+    src = os.path.join(ROOT, "tests", "host", "me_host.cu")
+    gen = os.path.join(ROOT, "madflow_gb300", "csrc", "generated")
+    codegen.write_generated(gen)
+    deps = [src] + [os.path.join(gen, f) for f in os.listdir(gen)] + [
+        os.path.join(ROOT, "madflow_gb300", "csrc", f) for f in ("mf_vertex.cuh", "mf_helas.cuh", "mf_common.cuh")]
+    if not os.path.exists(HOST_SO) or any(os.path.getmtime(d) > os.path.getmtime(HOST_SO) for d in deps):
+        os.makedirs(os.path.dirname(HOST_SO), exist_ok=True)
+        subprocess.run(["nvcc", "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-x", "cu", src, "-o", HOST_SO],
+                       check=True, capture_output=True)
+    return ctypes.CDLL(HOST_SO)
+
+
+def _dp(a):
+    return np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+@pytest.mark.parametrize("k", [2, 3, 4])
+def test_generated_recursion_vs_oracle(host_lib, oracle, k):
+    """FP64 generated code within 1e-12 of the oracle; FP32 (mixed) within 5e-5."""
+    T = oracle.TTNG(k)
+    prm = T.params(MT, WT, GC10, GC11, GC12)
+    rng = np.random.default_rng(11 + k)
+    x = rng.uniform(size=(16, 4 * k + 2))
+    p, *_ = oracle.ramboflow(x, k + 2, 13000.0, [MT, MT] + [0.0] * (k - 2))
+    coup = np.array([GC10.real, 0.0, 0.0, GC11.imag, 0.0, GC12.imag])
+    me0 = T.smatrix(p, prm)
+    for prec, tol in ((0, 1e-12), (1, 5e-5)):
+        out = np.zeros(len(p))
+        pc = np.ascontiguousarray(p)
+        host_lib.me_host_smatrix(k, prec, _dp(pc), ctypes.c_int64(len(p)), _dp(coup), ctypes.c_double(MT),
+                                 ctypes.c_double(WT), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        assert np.max(np.abs(out / me0 - 1)) < tol, (k, prec)
