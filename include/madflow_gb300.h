@@ -171,6 +171,23 @@ int mf_philox_uniforms(uint64_t seed, uint32_t stream_id, uint32_t iteration, ui
  * x [N], out [N]. */
 int mf_pdf_xfx(const double* x, int64_t n, double q2, double* out, void* stream);
 
+/* ---- normalizing-flow importance sampler ---------------------------------
+ * No counterpart in the reference (an addition of this implementation, used as
+ * a VEGAS alternative).  Piecewise-quadratic coupling transform of one layer
+ * (Mueller et al., ACM TOG 38 (2019) 145): x, y, u [N][nb] float32 values in
+ * [0,1] of the nb transformed dimensions; params [N][nb][2K+1] float32 raw
+ * bin widths (K) and vertex heights (K+1) from the conditioner network;
+ * logdet [N] = sum over the nb dimensions of log pdf.  2 <= K <= 64.
+ * mf_pq_forward: y = CDF(x); mf_pq_inverse: x = CDF^-1(u) (sampling);
+ * mf_pq_backward: gradients of mf_pq_forward given dL/dy (gy, may be NULL)
+ * and dL/dlogdet (glogdet, may be NULL) -> gx [N][nb], gparams like params. */
+int mf_pq_forward(const float* x, const float* params, int64_t n, int nb, int K, float* y, float* logdet,
+                  void* stream);
+int mf_pq_inverse(const float* u, const float* params, int64_t n, int nb, int K, float* x, float* logdet,
+                  void* stream);
+int mf_pq_backward(const float* x, const float* params, const float* gy, const float* glogdet, int64_t n, int nb,
+                   int K, float* gx, float* gparams, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -80,13 +80,9 @@ _SIGS = {
     "mf_vegas_sample": (c_int, [c_dp, c_int, c_int, c_dp, c_int64, c_dp, c_dp, c_dp, c_void_p]),
     "mf_philox_uniforms": (c_int, [c_uint64, c_uint32, c_uint32, c_uint64, c_int64, c_int, c_dp, c_void_p]),
     "mf_pdf_xfx": (c_int, [c_dp, c_int64, c_double, c_dp, c_void_p]),
-    "mf_flow_create": (c_int, [c_int, c_int, c_int, c_int, ctypes.POINTER(c_void_p)]),
-    "mf_flow_destroy": (c_int, [c_void_p]),
-    "mf_flow_num_params": (c_int, [c_void_p, ctypes.POINTER(c_int64)]),
-    "mf_flow_forward": (c_int, [c_void_p, c_dp, c_dp, c_int64, c_dp, c_dp, c_dp, c_void_p]),
-    "mf_flow_inverse": (c_int, [c_void_p, c_dp, c_dp, c_int64, c_dp, c_dp, c_void_p]),
-    "mf_flow_backward": (c_int, [c_void_p, c_dp, c_dp, c_int64, c_dp, c_dp, c_dp, c_void_p]),
-    "mf_flow_workspace_size": (c_int, [c_void_p, c_int64, ctypes.POINTER(c_int64)]),
+    "mf_pq_forward": (c_int, [c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
+    "mf_pq_inverse": (c_int, [c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
+    "mf_pq_backward": (c_int, [c_dp, c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
 }
 
 

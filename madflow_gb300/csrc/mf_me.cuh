@@ -279,7 +279,8 @@ __global__ void __launch_bounds__(32 * MF_WARPS) iteration_kernel(IterArgs A) {
   for (int i = threadIdx.x; i < MF_WARPS * nh; i += blockDim.x) hist[i] = 0.0;
   __syncthreads();
   const int it = *A.iteration;
-  const int niter_newton = *A.newton_iters;
+  // the batch rule runs at most 10 iterations (11 = no event converged)
+  const int niter_newton = min(*A.newton_iters, 10);
   const double sc = me_scale<K>(A.gc11);
   double s1 = 0.0, s2 = 0.0;
   double* wh = hist + warp * nh;

@@ -184,5 +184,5 @@ MF_HD double pdf_xfx(const PdfTable& P, double x, double q2) {
       s += wv * keys_w(fu - b) * P.tab[qi * P.nx + xi];
     }
   }
-  return s;
+  return s > 0.0 ? s : 0.0;  // the cubic can overshoot below zero next to x = 1
 }

@@ -1,0 +1,204 @@
+"""Normalizing-flow importance sampler over the unit hypercube, an alternative
+proposal to the VEGAS grid (no counterpart in the reference).
+
+Architecture (Mueller et al., "Neural Importance Sampling", ACM TOG 38 (2019)
+145): ``n_layers`` piecewise-quadratic coupling layers; each transforms half
+of the dimensions with bins (K widths, K+1 vertex heights) predicted by an MLP
+of ``n_hidden`` hidden layers of ``hidden`` units from the other half.
+
+Compute split: the conditioner MLPs are plain GEMMs, run in BF16 with FP32
+accumulation (cuBLAS via torch autocast), weights kept in FP32; the coupling
+transform, its inverse (sampling), log-Jacobian and backward pass are the
+hand-written CUDA kernels of ``mf_flow.cu`` behind the C ABI.
+
+Training minimises the variance of the weights f/q with the score-function
+gradient  d Var/d theta = -E_q[(f/q)^2 d log q/d theta]  on batches drawn from
+the flow itself; the integral estimate mean(f/q) stays unbiased for any
+trained state, and each integration iteration uses one frozen state.
+"""
+import math
+import time
+
+import torch
+
+from . import _lib
+from .config import device, stream_ptr
+
+
+class _PQ(torch.autograd.Function):
+    """y = CDF(x), logdet = sum log pdf(x) for one coupling layer (CUDA)."""
+
+    @staticmethod
+    def forward(ctx, x_b, params, K):
+        x_b = x_b.contiguous()
+        params = params.contiguous()
+        n, nb = x_b.shape
+        y = torch.empty_like(x_b)
+        ld = torch.empty(n, dtype=torch.float32, device=x_b.device)
+        _lib.call("mf_pq_forward", x_b.data_ptr(), params.data_ptr(), n, nb, K, y.data_ptr(), ld.data_ptr(),
+                  stream_ptr())
+        ctx.save_for_backward(x_b, params)
+        ctx.K = K
+        return y, ld
+
+    @staticmethod
+    def backward(ctx, gy, gld):
+        x_b, params = ctx.saved_tensors
+        n, nb = x_b.shape
+        gy = gy.contiguous() if gy is not None else None
+        gld = gld.contiguous() if gld is not None else None
+        gx = torch.empty_like(x_b)
+        gp = torch.empty_like(params)
+        _lib.call("mf_pq_backward", x_b.data_ptr(), params.data_ptr(), gy.data_ptr() if gy is not None else None,
+                  gld.data_ptr() if gld is not None else None, n, nb, ctx.K, gx.data_ptr(), gp.data_ptr(),
+                  stream_ptr())
+        return gx, gp, None
+
+
+def pq_forward(x_b, params, K):
+    return _PQ.apply(x_b, params, K)
+
+
+def pq_inverse(u_b, params, K):
+    u_b = u_b.contiguous()
+    params = params.contiguous()
+    n, nb = u_b.shape
+    x = torch.empty_like(u_b)
+    ld = torch.empty(n, dtype=torch.float32, device=u_b.device)
+    _lib.call("mf_pq_inverse", u_b.data_ptr(), params.data_ptr(), n, nb, K, x.data_ptr(), ld.data_ptr(), stream_ptr())
+    return x, ld
+
+
+def _masks(dim, n_layers, seed):
+    """Balanced random partitions; layers 2j and 2j+1 are complementary so
+    every dimension is transformed n_layers/2 times."""
+    g = torch.Generator().manual_seed(seed)
+    masks = []
+    for j in range((n_layers + 1) // 2):
+        perm = torch.randperm(dim, generator=g)
+        m = torch.zeros(dim, dtype=torch.bool)
+        m[perm[: dim // 2]] = True
+        masks += [m, ~m]
+    return masks[:n_layers]
+
+
+class NormalizingFlow(torch.nn.Module):
+    def __init__(self, dim, n_layers=6, bins=16, hidden=64, n_hidden=2, seed=0, bf16=True):
+        super().__init__()
+        self.dim, self.K, self.bf16 = dim, bins, bf16
+        self.masks = _masks(dim, n_layers, seed)
+        self.nets = torch.nn.ModuleList()
+        torch.manual_seed(seed)
+        for m in self.masks:
+            nb, na = int(m.sum()), int((~m).sum())
+            layers = [torch.nn.Linear(na, hidden), torch.nn.ReLU()]
+            for _ in range(n_hidden - 1):
+                layers += [torch.nn.Linear(hidden, hidden), torch.nn.ReLU()]
+            last = torch.nn.Linear(hidden, nb * (2 * bins + 1))
+            torch.nn.init.zeros_(last.weight)  # start at the identity map
+            torch.nn.init.zeros_(last.bias)
+            layers.append(last)
+            self.nets.append(torch.nn.Sequential(*layers))
+        self.to(device())
+        self._idx = [(torch.nonzero(m).flatten().to(device()), torch.nonzero(~m).flatten().to(device()))
+                     for m in self.masks]
+
+    def _params(self, l, x_a):
+        with torch.autocast("cuda", dtype=torch.bfloat16, enabled=self.bf16):
+            out = self.nets[l](2.0 * x_a - 1.0)
+        nb = int(self.masks[l].sum())
+        return out.float().reshape(-1, nb, 2 * self.K + 1)
+
+    @torch.no_grad()
+    def sample(self, n, seed=1234, iteration=0, stream_id=7):
+        """n points (float64 (n, dim)) and their log density (float64 (n,))."""
+        u = torch.empty((self.dim, n), dtype=torch.float64, device=device())
+        _lib.call("mf_philox_uniforms", int(seed), int(stream_id), int(iteration), 0, n, self.dim, u.data_ptr(),
+                  stream_ptr())
+        z = u.T.float().contiguous()
+        logq = torch.zeros(n, dtype=torch.float32, device=device())
+        for l in range(len(self.masks)):
+            ib, ia = self._idx[l]
+            params = self._params(l, z[:, ia])
+            xb, ld = pq_inverse(z[:, ib], params, self.K)
+            z[:, ib] = xb
+            logq += ld
+        return z.double(), logq.double()
+
+    def log_prob(self, x):
+        """log q(x) with gradients w.r.t. the network weights."""
+        z = x.float()
+        logq = torch.zeros(x.shape[0], dtype=torch.float32, device=x.device)
+        for l in reversed(range(len(self.masks))):
+            ib, ia = self._idx[l]
+            params = self._params(l, z[:, ia])
+            yb, ld = pq_forward(z[:, ib], params, self.K)
+            z = z.index_copy(1, ib, yb)
+            logq = logq + ld
+        return logq
+
+
+def _clamp_open(x, eps=1e-7):
+    return x.clamp(eps, 1.0 - eps)
+
+
+def train_flow(flow, integrand, n_batches=20, batch_size=1_000_000, minibatch=100_000, lr=2e-3, seed=99,
+               log=None):
+    """Variance-loss training on weights f/q of batches drawn from the flow."""
+    opt = torch.optim.Adam(flow.parameters(), lr=lr)
+    hist = []
+    for b in range(n_batches):
+        x, logq = flow.sample(batch_size, seed=seed, iteration=b)
+        x = _clamp_open(x)
+        f = integrand(x)
+        w = f * torch.exp(-logq)
+        mean_w = w.mean()
+        scale = (mean_w * mean_w).clamp_min(1e-300)
+        for s in range(0, batch_size, minibatch):
+            xm = x[s: s + minibatch]
+            wm = w[s: s + minibatch]
+            lq = flow.log_prob(xm)
+            loss = -((wm * wm / scale).float() * lq).mean()
+            opt.zero_grad(set_to_none=True)
+            loss.backward()
+            opt.step()
+        rel = float(w.std() / w.mean()) if float(mean_w) != 0 else float("nan")
+        hist.append(rel)
+        if log:
+            log(f"flow batch {b}: mean {float(mean_w):.5g}, std/mean {rel:.4f}")
+    return hist
+
+
+class FlowIntegrator:
+    """Importance-sampling integration with a (frozen) flow proposal."""
+
+    def __init__(self, flow, integrand, n_events, seed=4321):
+        self.flow, self.integrand, self.n_events, self.seed = flow, integrand, int(n_events), seed
+        self.history = []
+
+    def run_event(self, it):
+        x, logq = self.flow.sample(self.n_events, seed=self.seed, iteration=it)
+        x = _clamp_open(x)
+        w = self.integrand(x) * torch.exp(-logq)
+        n = w.numel()
+        res = float(w.mean())
+        var = float(w.var()) / n
+        self.last_eff = float(w.mean() / w.max()) if float(w.max()) > 0 else 0.0
+        return res, math.sqrt(max(var, 0.0))
+
+    def run_integration(self, n_iter, target_rel_error=None):
+        wsum = wres = 0.0
+        self.last_run = []
+        for it in range(int(n_iter)):
+            t0 = time.perf_counter()
+            res, sig = self.run_event(len(self.history))
+            self.history.append((res, sig))
+            self.last_run.append((res, sig, time.perf_counter() - t0))
+            if sig > 0:
+                wsum += 1.0 / (sig * sig)
+                wres += res / (sig * sig)
+            if target_rel_error is not None and wsum > 0:
+                cur = wres / wsum
+                if cur != 0 and (1.0 / math.sqrt(wsum)) / abs(cur) <= target_rel_error:
+                    break
+        return (wres / wsum, 1.0 / math.sqrt(wsum)) if wsum > 0 else (0.0, 0.0)

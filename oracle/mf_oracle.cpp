@@ -773,7 +773,7 @@ extern "C" void orc_pdf_xfx(const double* x, int64_t N, double q2, double* out) 
         s += wv * keys_w(fu - b) * tab[qi * kNX + xi];
       }
     }
-    out[e] = s;
+    out[e] = s > 0.0 ? s : 0.0;
   }
 }
 
