@@ -238,117 +238,6 @@ def _canonical(seq):
     return rev, (-1) ** (len(seq) + 1)
 
 
-def _jname(seq):
-    return "J_" + "".join(str(g) for g in seq)
-
-
-def emit_amplitudes(k):
-    """CUDA source of ``ttng<k>_amps<T>``: all colour-ordered partial
-    amplitudes of one event for one helicity."""
-    L = []
-    w = L.append
-    w(f"// Generated by madflow_gb300.codegen for {process_name(k)}: {math.factorial(k)} colour orderings.")
-    w("template <class T>")
-    w(f"MF_D void ttng{k}_amps(const EvData<T, {k}>& ev, const W4<T>* g, const W4<T>& wt,")
-    w("                                             const W4<T>& wtb, cx<T>* A) {")
-    # J table: lengths 2..k-1, canonical representatives
-    made = set()
-    for length in range(2, k):
-        for seq in itertools.permutations(range(k), length):
-            rep, sgn = _canonical(seq)
-            if rep in made:
-                continue
-            made.add(rep)
-            s = _mask(rep)
-            w(f"  W4<T> {_jname(rep)};")
-            w("  {")
-            w("    W4<T> a3 = w4zero<T>(), a4 = w4zero<T>();")
-            for i in range(1, length):
-                left, right = rep[:i], rep[i:]
-                w(f"    vvv_add<T>({_jref(left)}, ev.Qg[{_mask(left)}], {_jref(right)}, ev.Qg[{_mask(right)}], a3);")
-            for i in range(1, length):
-                for j in range(i + 1, length):
-                    w(f"    vvvv_add<T>({_jref(rep[:i])}, {_jref(rep[i:j])}, {_jref(rep[j:])}, a4);")
-            w(f"    {_jname(rep)} = combine<T>(ev.gv3[{s}], a3, ev.gv4[{s}], a4);")
-            w("  }")
-    w("  #pragma unroll")
-    w(f"  for (int i = 0; i < {math.factorial(k)}; ++i) A[i] = cx<T>{{T(0), T(0)}};")
-    # full-length gluon currents contracted with the bare quark line: A(sigma) += amp * wtb^T S(J(sigma)) wt
-    perms = permutations(k)
-    pidx = {p: i for i, p in enumerate(perms)}
-    done = set()
-    full = _mask(range(k))
-    for sig in perms:
-        rep, sgn = _canonical(sig)
-        if rep in done:
-            continue
-        done.add(rep)
-        w("  {")
-        w("    W4<T> a3 = w4zero<T>(), a4 = w4zero<T>();")
-        for i in range(1, k):
-            left, right = rep[:i], rep[i:]
-            w(f"    vvv_add<T>({_jref(left)}, ev.Qg[{_mask(left)}], {_jref(right)}, ev.Qg[{_mask(right)}], a3);")
-        for i in range(1, k):
-            for j in range(i + 1, k):
-                w(f"    vvvv_add<T>({_jref(rep[:i])}, {_jref(rep[i:j])}, {_jref(rep[j:])}, a4);")
-        w(f"    W4<T> Jf = combine<T>(ev.gv3[{full}], a3, ev.gv4[{full}], a4);")
-        w("    cx<T> t = sandwich<T>(wtb, Jf, wt);")
-        rev = tuple(reversed(rep))
-        w(f"    A[{pidx[rep]}] += t;")
-        if rev != rep:
-            rsgn = (-1) ** (k + 1)
-            w(f"    A[{pidx[rev]}] {'+=' if rsgn > 0 else '-='} t;")
-        w("  }")
-    # DFS over prefixes of the top-quark line
-    def dfs(prefix, depth_names):
-        # prefix: tuple of gluons attached so far (len >= 1); emit O(prefix)
-        m = len(prefix)
-        oname = "O_" + "".join(str(g) for g in prefix)
-        w("  " * m + "{")
-        ind = "  " * (m + 1)
-        w(f"{ind}W4<T> y = w4zero<T>();")
-        names = depth_names + [oname]
-        for i in range(m):
-            a_name = names[i]  # O(prefix[:i]) (i = 0 -> wt)
-            b = prefix[i:]
-            w(f"{ind}sv_add<T>({_jref(b)}, {a_name}, y);")
-        w(f"{ind}W4<T> {oname} = topprop<T>(ev.Qt[{_mask(prefix)}], ev.mt, ev.tden[{_mask(prefix)}], y);")
-        if m == k - 1:
-            last = [g for g in range(k) if g not in prefix][0]
-            sig = prefix + (last,)
-            w(f"{ind}{{")
-            w(f"{ind}  cx<T> acc = cx<T>{{T(0), T(0)}};")
-            for i in range(1, k):
-                o_name = names[i] if i < len(names) else oname
-                if i == m:
-                    o_name = oname
-                else:
-                    o_name = names[i]
-                b = sig[i:]
-                w(f"{ind}  acc += sandwich<T>(wtb, {_jref(b)}, {o_name});")
-            w(f"{ind}  A[{pidx[sig]}] += acc;")
-            w(f"{ind}}}")
-        else:
-            for g in range(k):
-                if g not in prefix:
-                    dfs(prefix + (g,), names)
-        w("  " * m + "}")
-
-    for g in range(k):
-        dfs((g,), ["wt"])
-    w("}")
-    return "\n".join(L)
-
-
-def _jref(seq):
-    """Expression for J(seq): external for length 1, table entry (with the
-    reflection sign) otherwise."""
-    if len(seq) == 1:
-        return f"g[{seq[0]}]"
-    rep, sgn = _canonical(tuple(seq))
-    return _jname(rep) if sgn > 0 else f"neg<T>({_jname(rep)})"
-
-
 def emit_process_header(k):
     """Header with the process constants and the amplitude recursion."""
     num, den = colour_matrix(k)
@@ -383,8 +272,128 @@ def emit_process_header(k):
         L.append("  {" + ", ".join(str(int(v)) for v in h) + "},")
     L.append("};")
     L.append("}  // namespace")
-    L.append(emit_amplitudes(k))
+    L.append(emit_recycled_tables(k))
     return "\n".join(L) + "\n"
+
+
+def _code(seq, base):
+    c = 0
+    for j, g in enumerate(seq):
+        c += (g + 1) * base**j
+    return c
+
+
+def _arr(name, ctype, vals):
+    vals = list(vals) or [0]
+    body = ", ".join(str(int(v)) for v in vals)
+    return f"__device__ const {ctype} {name}[{len(vals)}] = {{{body}}};\nstatic const {ctype} {name}_h[{len(vals)}] = {{{body}}};"
+
+
+def emit_recycled_tables(k):
+    """Tables of the helicity-recycling evaluation (mf_me_rec.cuh).
+
+    Ordered gluon sequences are coded as sum_j (g_j + 1) (k+1)^j.  A helicity
+    pattern of a sequence packs the helicity bit of its j-th gluon at bit j,
+    so the patterns of the parts of a split are shifts and masks of the whole.
+    """
+    base = k + 1
+    # canonical gluon-current nodes, lengths 2..k-1
+    jn = []
+    for L in range(2, k):
+        for seq in itertools.permutations(range(k), L):
+            rep, _ = _canonical(seq)
+            if rep == seq:
+                jn.append(seq)
+    jid = {s: i for i, s in enumerate(jn)}
+    NJ = len(jn)
+    jn_off, off = [], 0
+    for s in jn:
+        jn_off.append(off)
+        off += 1 << len(s)
+    J_TOTAL = off
+    jlen_first = [0] * (k + 2)
+    for L in range(k + 2):
+        jlen_first[L] = sum(1 for s in jn if len(s) < L)
+    # references of every ordered sequence of length 1..k-1 (and k for full)
+    ncode = base**k
+    seq_ref = [-1] * ncode
+    seq_mask = [0] * (base**k)
+    for L in range(1, k + 1):
+        for seq in itertools.permutations(range(k), L):
+            c = _code(seq, base)
+            seq_mask[c] = _mask(seq)
+            if L == 1:
+                seq_ref[c] = ((NJ + seq[0]) << 2)
+            elif L < k:
+                rep, sgn = _canonical(seq)
+                rev = 1 if rep != seq else 0
+                seq_ref[c] = (jid[rep] << 2) | (rev << 1) | (1 if sgn < 0 else 0)
+    # full-length canonical orderings
+    perms = permutations(k)
+    fn = []
+    for s in perms:
+        rep, _ = _canonical(s)
+        if rep == s:
+            fn.append(s)
+    fid = {s: i for i, s in enumerate(fn)}
+    perm_full = []
+    for s in perms:
+        rep, sgn = _canonical(s)
+        rev = 1 if rep != s else 0
+        perm_full.append((fid[rep] << 2) | (rev << 1) | (1 if sgn < 0 else 0))
+    # top-line prefix nodes, lengths 1..k-1 (all orders)
+    on = [seq for L in range(1, k) for seq in itertools.permutations(range(k), L)]
+    on_off, off = [], 0
+    opos = [-1] * ncode
+    for i, s in enumerate(on):
+        on_off.append(off)
+        opos[_code(s, base)] = i
+        off += 2 << len(s)
+    O_TOTAL = off
+    olen_first = [0] * (k + 2)
+    for L in range(k + 2):
+        olen_first[L] = sum(1 for s in on if len(s) < L)
+    # t~-side rows for every reference id (externals and J nodes)
+    r_len = [len(s) for s in jn] + [1] * k
+    r_off, off = [], 0
+    for L in r_len:
+        r_off.append(off)
+        off += 2 << L
+    R_TOTAL = off
+    L = []
+    w = L.append
+    w(f"namespace rec{k} {{")
+    w(f"constexpr int NJ = {NJ}, J_TOTAL = {J_TOTAL}, NF = {len(fn)}, NO = {len(on)}, O_TOTAL = {O_TOTAL};")
+    w(f"constexpr int NR = {NJ + k}, R_TOTAL = {R_TOTAL}, BASE = {base}, NCODE = {ncode};")
+    w(_arr("jn_code", "int", [_code(s, base) for s in jn]))
+    w(_arr("jn_off", "int", jn_off))
+    w(_arr("jlen_first", "int", jlen_first))
+    w(_arr("seq_ref", "int", seq_ref))
+    w(_arr("seq_mask", "int", seq_mask))
+    w(_arr("fn_code", "int", [_code(s, base) for s in fn]))
+    w(_arr("perm_code", "int", [_code(s, base) for s in perms]))
+    w(_arr("perm_full", "int", perm_full))
+    w(_arr("on_code", "int", [_code(s, base) for s in on]))
+    w(_arr("on_off", "int", on_off))
+    w(_arr("olen_first", "int", olen_first))
+    w(_arr("opos", "int", opos))
+    w(_arr("r_len", "int", r_len))
+    w(_arr("r_off", "int", r_off))
+    # MadGraph helicity index of a (gluon bits, top bit, antitop bit) config
+    hels = helicities(k)
+    hidx = {tuple(int(v) for v in h): i for i, h in enumerate(hels)}
+    cfg_to_mg = []
+    for c in range(1 << (k + 2)):
+        hg, ht, htb = c & ((1 << k) - 1), (c >> k) & 1, (c >> (k + 1)) & 1
+        h = [0] * (k + 2)
+        for q in range(k):
+            h[GLUON_PARTICLE[q]] = 1 if (hg >> q) & 1 else -1
+        h[2] = 1 if ht else -1
+        h[3] = 1 if htb else -1
+        cfg_to_mg.append(hidx[tuple(h)])
+    w(_arr("cfg_to_mg", "int", cfg_to_mg))
+    w("}  // namespace")
+    return "\n".join(L)
 
 
 def write_generated(outdir, ks=(2, 3, 4)):

@@ -405,11 +405,17 @@ struct mf_process {
   double denominator;
   std::vector<double> hel, colour;
   int device;
-  // scratch owned by the handle (grown on demand)
+  // scratch owned by the handle (grown on demand): the Newton counter, the
+  // block partials and the per-event pipeline buffers of an iteration
   int* d_kmin = nullptr;
   double* d_partials = nullptr;
   size_t partial_cap = 0;
   int* d_zero_iter = nullptr;
+  double* d_ps = nullptr;   // [K+2][4][cap]
+  double* d_pref = nullptr; // [cap]
+  double* d_me = nullptr;   // [cap]
+  unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
+  int64_t event_cap = 0;
 };
 
 static const int kDiagrams[6] = {0, 0, 3, 16, 123, 1240};
@@ -460,6 +466,10 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_kmin) cudaFree(p->d_kmin);
   if (p->d_partials) cudaFree(p->d_partials);
   if (p->d_zero_iter) cudaFree(p->d_zero_iter);
+  if (p->d_ps) cudaFree(p->d_ps);
+  if (p->d_pref) cudaFree(p->d_pref);
+  if (p->d_me) cudaFree(p->d_me);
+  if (p->d_bins) cudaFree(p->d_bins);
   delete p;
   return MF_OK;
 }
@@ -490,13 +500,8 @@ int mf_smatrix(const mf_process* p, const double* ps, int64_t N, double mt, doub
                int64_t cstride, double* out, double* hel_out, void* stream) {
   if (!p || (N > 0 && (!ps || !coup || !out)) || N < 0 || (cstride != 0 && cstride != 1)) return MF_ERR_ARG;
   if (N == 0) return MF_OK;
-  int st;
-  switch (p->k) {
-    case 2: st = mf_launch_smatrix_k2(p->prec, ps, N, mt, wt, coup, cstride, out, hel_out, S(stream)); break;
-    case 3: st = mf_launch_smatrix_k3(p->prec, ps, N, mt, wt, coup, cstride, out, hel_out, S(stream)); break;
-    case 4: st = mf_launch_smatrix_k4(p->prec, ps, N, mt, wt, coup, cstride, out, hel_out, S(stream)); break;
-    default: return MF_ERR_UNSUPPORTED;
-  }
+  int st = mf_launch_me(p->k, p->prec, ps, N, mt, wt, coup, cstride, nullptr, out, hel_out, S(stream));
+  if (st == 3) return MF_ERR_UNSUPPORTED;
   return st ? last_launch() : MF_OK;
 }
 
@@ -663,19 +668,50 @@ static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, Ite
   return pdf_device_table(A.pdf);
 }
 
-static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, double* results, void* stream) {
-  int st;
-  int grid;
-  switch (p->k) {
-    case 2: grid = mf_iteration_grid_k2(p->prec, A.ndim, A.nb, A.N); break;
-    case 3: grid = mf_iteration_grid_k3(p->prec, A.ndim, A.nb, A.N); break;
-    case 4: grid = mf_iteration_grid_k4(p->prec, A.ndim, A.nb, A.N); break;
-    default: return MF_ERR_UNSUPPORTED;
+static int ensure_events(mf_process* p, int64_t N) {
+  if (p->event_cap >= N) return MF_OK;
+  cudaFree(p->d_ps);
+  cudaFree(p->d_pref);
+  cudaFree(p->d_me);
+  cudaFree(p->d_bins);
+  p->d_ps = p->d_pref = p->d_me = nullptr;
+  p->d_bins = nullptr;
+  p->event_cap = 0;
+  int st = cuda_status(cudaMalloc(&p->d_ps, sizeof(double) * (size_t)(p->k + 2) * 4 * N));
+  if (!st) st = cuda_status(cudaMalloc(&p->d_pref, sizeof(double) * (size_t)N));
+  if (!st) st = cuda_status(cudaMalloc(&p->d_me, sizeof(double) * (size_t)N));
+  if (!st) st = cuda_status(cudaMalloc(&p->d_bins, (size_t)MF_MAX_DIM * N));
+  if (st) return st;
+  p->event_cap = N;
+  return MF_OK;
+}
+
+__global__ void set_couplings_kernel(double* c, cx<double> a, cx<double> b, cx<double> d) {
+  c[0] = a.re; c[1] = a.im; c[2] = b.re; c[3] = b.im; c[4] = d.re; c[5] = d.im;
+}
+
+// One pass of the pipeline over A.N events: Newton first pass, phase space,
+// |M|^2, accumulation.  results (optional) [2 + ndim*nb]; f_out (optional) [N].
+static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, double* results, double* f_out,
+                     void* stream) {
+  int st = ensure_events(p, A.N);
+  if (st) return st;
+  A.ps = p->d_ps;
+  A.pref = p->d_pref;
+  A.me = p->d_me;
+  A.bins = A.x_in ? nullptr : p->d_bins;
+  int accum_grid = 8 * 152;
+  {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    accum_grid = 8 * (sms > 0 ? sms : 152);
+    if (accum_grid > A.N) accum_grid = (int)A.N;
   }
   int width = 2 + A.ndim * A.nb;
-  st = ensure_partials(p, (size_t)grid * width);
+  st = ensure_partials(p, (size_t)accum_grid * width + 6);
   if (st) return st;
-  A.partials = p->d_partials;
+  double* d_coup = p->d_partials + (size_t)accum_grid * width;
   if (!p->d_kmin) {
     st = cuda_status(cudaMalloc(&p->d_kmin, sizeof(int)));
     if (st) return st;
@@ -683,21 +719,17 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   A.newton_iters = p->d_kmin;
   bool per_event = c->newton_rule == MF_NEWTON_PER_EVENT;
   set_int_kernel<<<1, 1, 0, S(stream)>>>(p->d_kmin, per_event ? 0 : 11);
-  if (!per_event) {
-    switch (p->k) {
-      case 2: st = mf_launch_newton_k2(A, p->d_kmin, S(stream)); break;
-      case 3: st = mf_launch_newton_k3(A, p->d_kmin, S(stream)); break;
-      case 4: st = mf_launch_newton_k4(A, p->d_kmin, S(stream)); break;
-    }
-    if (st) return last_launch();
-  }
-  switch (p->k) {
-    case 2: st = mf_launch_iteration_k2(p->prec, A, grid, S(stream)); break;
-    case 3: st = mf_launch_iteration_k3(p->prec, A, grid, S(stream)); break;
-    case 4: st = mf_launch_iteration_k4(p->prec, A, grid, S(stream)); break;
-  }
-  if (st) return last_launch();
-  if (results) reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(A.partials, grid, width, results);
+  set_couplings_kernel<<<1, 1, 0, S(stream)>>>(d_coup, A.gc10, A.gc11, A.gc12);
+  if (!per_event && mf_launch_newton(p->k, A, p->d_kmin, S(stream))) return last_launch();
+  if (mf_launch_ps(p->k, A, S(stream))) return last_launch();
+  if (mf_launch_me(p->k, p->prec, A.ps, A.N, A.mt, A.wt, d_coup, 0, A.pref, A.me, nullptr, S(stream)))
+    return last_launch();
+  size_t shm = (size_t)(A.ndim * A.nb + 2 * 256) * sizeof(double);
+  cudaFuncSetAttribute(accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  accum_kernel<<<accum_grid, 256, shm, S(stream)>>>(A.pref, A.me, A.bins, A.N, A.ndim, A.nb, A.inv_n, f_out,
+                                                     results ? p->d_partials : nullptr);
+  if (results)
+    reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(p->d_partials, accum_grid, width, results);
   return last_launch();
 }
 
@@ -725,8 +757,7 @@ int mf_integrand(const mf_process* pc, const mf_integrand_config* c, const doubl
   A.N = N;
   A.inv_n = 1.0;
   A.x_in = x;
-  A.f_out = f;
-  return run_fused(p, A, c, nullptr, stream);
+  return run_fused(p, A, c, nullptr, f, stream);
 }
 
 int mf_vegas_iteration(const mf_process* pc, const mf_integrand_config* c, const double* grid, int nb, uint64_t seed,
@@ -749,9 +780,8 @@ int mf_vegas_iteration(const mf_process* pc, const mf_integrand_config* c, const
   A.iteration = iteration;
   A.N = N;
   A.inv_n = 1.0 / (double)N;
-  A.f_out = f_out;
   A.u_out = u_out;
-  return run_fused(p, A, c, results, stream);
+  return run_fused(p, A, c, results, f_out, stream);
 }
 
 int mf_vegas_accumulate(const double* f, const double* jac, const int32_t* bins, int64_t N, int ndim, int nb,

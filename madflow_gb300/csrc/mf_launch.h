@@ -4,13 +4,12 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 struct IterArgs;
-#define MF_DECLARE_PROCESS(KK)                                                                                \
-  void mf_host_tables_k##KK(int* nperm, int* ncomb, double* den, double* cden, const float** cn,               \
-                            const signed char** hh);                                                          \
-  int mf_launch_smatrix_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup, \
-                              int64_t cstride, double* out, double* hel_out, cudaStream_t st);               \
-  int mf_iteration_grid_k##KK(int prec, int ndim, int nb, int64_t N);                                         \
-  int mf_launch_iteration_k##KK(int prec, const IterArgs& A, int grid, cudaStream_t st);                      \
+#define MF_DECLARE_PROCESS(KK)                                                                              \
+  void mf_host_tables_k##KK(int* nperm, int* ncomb, double* den, double* cden, const float** cn,             \
+                            const signed char** hh);                                                        \
+  int mf_launch_me_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,    \
+                         int64_t cstride, const double* skip, double* out, double* hel_out, cudaStream_t st); \
+  int mf_launch_ps_k##KK(const IterArgs& A, cudaStream_t st);                                               \
   int mf_launch_newton_k##KK(const IterArgs& A, int* kmin, cudaStream_t st);
 MF_DECLARE_PROCESS(2)
 MF_DECLARE_PROCESS(3)
@@ -23,4 +22,29 @@ inline void mf_host_tables(int k, int* nperm, int* ncomb, double* den, double* c
     case 3: mf_host_tables_k3(nperm, ncomb, den, cden, cn, hh); break;
     default: mf_host_tables_k4(nperm, ncomb, den, cden, cn, hh); break;
   }
+}
+inline int mf_launch_me(int k, int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,
+                        int64_t cstride, const double* skip, double* out, double* hel_out, cudaStream_t st) {
+  switch (k) {
+    case 2: return mf_launch_me_k2(prec, ps, N, mt, wt, coup, cstride, skip, out, hel_out, st);
+    case 3: return mf_launch_me_k3(prec, ps, N, mt, wt, coup, cstride, skip, out, hel_out, st);
+    case 4: return mf_launch_me_k4(prec, ps, N, mt, wt, coup, cstride, skip, out, hel_out, st);
+  }
+  return 3;
+}
+inline int mf_launch_ps(int k, const IterArgs& A, cudaStream_t st) {
+  switch (k) {
+    case 2: return mf_launch_ps_k2(A, st);
+    case 3: return mf_launch_ps_k3(A, st);
+    case 4: return mf_launch_ps_k4(A, st);
+  }
+  return 3;
+}
+inline int mf_launch_newton(int k, const IterArgs& A, int* kmin, cudaStream_t st) {
+  switch (k) {
+    case 2: return mf_launch_newton_k2(A, kmin, st);
+    case 3: return mf_launch_newton_k3(A, kmin, st);
+    case 4: return mf_launch_newton_k4(A, kmin, st);
+  }
+  return 3;
 }

@@ -86,3 +86,18 @@ def test_generated_recursion_vs_oracle(host_lib, oracle, k):
         host_lib.me_host_smatrix(k, prec, _dp(pc), ctypes.c_int64(len(p)), _dp(coup), ctypes.c_double(MT),
                                  ctypes.c_double(WT), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
         assert np.max(np.abs(out / me0 - 1)) < tol, (k, prec)
+
+
+@pytest.mark.parametrize("k", [2, 3, 4])
+def test_generated_per_helicity_vs_oracle(host_lib, oracle, k):
+    """Per-helicity values (Matrix_<proc>.matrix) in MadGraph's helicity order."""
+    T = oracle.TTNG(k)
+    prm = T.params(MT, WT, GC10, GC11, GC12)
+    x = np.random.default_rng(70 + k).uniform(size=(1, 4 * k + 2))
+    p, *_ = oracle.ramboflow(x, k + 2, 13000.0, [MT, MT] + [0.0] * (k - 2))
+    _, ref = T.smatrix(p, prm, per_helicity=True)
+    coup = np.array([GC10.real, 0.0, 0.0, GC11.imag, 0.0, GC12.imag])
+    out = np.zeros(T.ncomb)
+    host_lib.me_host_helicities(k, _dp(np.ascontiguousarray(p[0])), _dp(coup), ctypes.c_double(MT),
+                                ctypes.c_double(WT), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    np.testing.assert_allclose(out, ref[:, 0], rtol=1e-11, atol=1e-14 * np.abs(ref).max())
