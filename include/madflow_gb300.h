@@ -153,6 +153,21 @@ int mf_vegas_iteration(const mf_process* proc, const mf_integrand_config* cfg, c
 int mf_vegas_accumulate(const double* f, const double* jac, const int32_t* bins, int64_t n_events, int ndim,
                         int nbins, double inv_n, double* results, void* stream);
 
+/* mf_vegas_accumulate without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc, for instance
+ * code that runs inside a region where allocation is forbidden (a timed or
+ * captured section) or whose device memory belongs to a pool manager.  Same
+ * arguments, kernels and results as mf_vegas_accumulate; the block partials
+ * live in a fixed array inside the library (4.2 MB on every GPU that loads
+ * it, held until the process exits).  Limit: ndim * nbins <= 2048, else
+ * MF_ERR_CAPACITY.  The first call on each device resolves the array's device
+ * address (cudaGetSymbolAddress) with that device current: make that first
+ * call before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU (concurrent streams, or several host threads) race:
+ * serialise them. */
+int mf_vegas_accumulate_noalloc(const double* f, const double* jac, const int32_t* bins, int64_t n_events, int ndim,
+                                int nbins, double inv_n, double* results, void* stream);
+
 /* Grid refinement of one iteration (device): grid [ndim][nbins+1] updated in
  * place from the per-bin weights hist [ndim][nbins] with damping alpha. */
 int mf_vegas_refine(double* grid, const double* hist, int ndim, int nbins, double alpha, void* stream);

@@ -76,6 +76,7 @@ _SIGS = {
     "mf_vegas_iteration": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int, c_uint64, c_uint32, c_dp,
                                    c_int64, c_dp, c_dp, c_dp, c_void_p]),
     "mf_vegas_accumulate": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
+    "mf_vegas_accumulate_noalloc": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
     "mf_vegas_refine": (c_int, [c_dp, c_dp, c_int, c_int, c_double, c_void_p]),
     "mf_vegas_sample": (c_int, [c_dp, c_int, c_int, c_dp, c_int64, c_dp, c_dp, c_dp, c_void_p]),
     "mf_philox_uniforms": (c_int, [c_uint64, c_uint32, c_uint32, c_uint64, c_int64, c_int, c_dp, c_void_p]),

@@ -810,6 +810,62 @@ int mf_vegas_accumulate(const double* f, const double* jac, const int32_t* bins,
   return last_launch();
 }
 
+}  // extern "C"
+
+// ---- VEGAS accumulation without allocation ----------------------------------
+// For callers that must not allocate device memory (allocation is banned
+// inside their timed or captured region, or their memory is owned by a pool
+// manager), the block partials of the accumulation live in this file-scope
+// array instead of a cudaMalloc'd buffer.  Every GPU that loads the library
+// holds it (MF_NOALLOC_BLOCKS x (2 + MF_NOALLOC_MAX_BINS) doubles, 4.2 MB)
+// until the process exits.
+constexpr int MF_NOALLOC_BLOCKS = 256;  // same block count as mf_vegas_accumulate
+constexpr int MF_NOALLOC_MAX_BINS = 2048;
+static __device__ __align__(256) double g_noalloc_partials[MF_NOALLOC_BLOCKS * (2 + MF_NOALLOC_MAX_BINS)];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[64] = {nullptr};
+// Device address of the array for the current device.  Host code cannot use
+// the symbol itself: on the host, g_noalloc_partials names a host-side
+// stand-in, so it is resolved once per device with that device current.
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  int st = cuda_status(cudaGetDevice(&dev));
+  if (st) return st;
+  if (dev < 0 || dev >= 64) return MF_ERR_CAPACITY;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    st = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_partials));
+    if (st) return st;
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return MF_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int mf_vegas_accumulate_noalloc(const double* f, const double* jac, const int32_t* bins, int64_t N, int ndim, int nb,
+                                double inv_n, double* results, void* stream) {
+  if (!f || !jac || !bins || !results || N <= 0 || ndim <= 0 || nb < 2) return MF_ERR_ARG;
+  if ((int64_t)ndim * nb > MF_NOALLOC_MAX_BINS) return MF_ERR_CAPACITY;
+  double* part = nullptr;
+  int st = noalloc_scratch(&part);
+  if (st) return st;
+  const int blocks = MF_NOALLOC_BLOCKS;
+  const int width = 2 + ndim * nb;
+  // every block writes all `width` entries of its row, so the partials left
+  // by an earlier call never need clearing
+  size_t shm = (size_t)(ndim * nb + 2 * 256) * sizeof(double);
+  cudaFuncSetAttribute(vegas_accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  vegas_accum_kernel<<<blocks, 256, shm, S(stream)>>>(f, jac, bins, N, ndim, nb, inv_n, part);
+  reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(part, blocks, width, results);
+  return last_launch();
+}
+
 int mf_vegas_refine(double* grid, const double* hist, int ndim, int nb, double alpha, void* stream) {
   if (!grid || !hist || ndim <= 0 || nb < 2 || nb > 256) return MF_ERR_ARG;
   vegas_refine_kernel<<<(ndim + 31) / 32, 32, 0, S(stream)>>>(grid, hist, ndim, nb, alpha);
