@@ -272,7 +272,7 @@ def emit_process_header(k):
         L.append("  {" + ", ".join(str(int(v)) for v in h) + "},")
     L.append("};")
     L.append("}  // namespace")
-    L.append(emit_recycled_tables(k))
+    L.append(emit_program(k))
     return "\n".join(L) + "\n"
 
 
@@ -289,97 +289,133 @@ def _arr(name, ctype, vals):
     return f"__device__ const {ctype} {name}[{len(vals)}] = {{{body}}};\nstatic const {ctype} {name}_h[{len(vals)}] = {{{body}}};"
 
 
-def emit_recycled_tables(k):
-    """Tables of the helicity-recycling evaluation (mf_me_rec.cuh).
+def _bitrev(h, n):
+    r = 0
+    for j in range(n):
+        r |= ((h >> j) & 1) << (n - 1 - j)
+    return r
 
-    Ordered gluon sequences are coded as sum_j (g_j + 1) (k+1)^j.  A helicity
-    pattern of a sequence packs the helicity bit of its j-th gluon at bit j,
-    so the patterns of the parts of a split are shifts and masks of the whole.
+
+def emit_program(k):
+    """The helicity-recycling evaluation of mf_me_rec.cuh as a flat program.
+
+    Storage (shared memory of one event):
+      J  every ordered gluon sequence s of length 1..k-1, 2^|s| helicity
+         patterns (length 1: the external gluons);
+      O  every ordered prefix a (gluons next to the top) of length 1..k-1,
+         2 x 2^|a| (top helicity, pattern);
+      R  every ordered suffix b of length 1..k-1, 2 x 2^|b| (t~ helicity,
+         pattern): the row wtb^T S(J(b));
+      T0 every ordering sigma, 2^k x 4: wtb^T S(J(sigma)) wt.
+    A helicity pattern of a sequence packs the helicity bit of its j-th gluon
+    at bit j, so the patterns of the parts of a split are shifts and masks.
+    Only one of each pair (s, reverse s) is computed; the other is written
+    with J(reverse s; bitrev(h)) = (-1)^(|s|+1) J(s; h).
+
+    Stage L (1 <= L <= k-1) holds the gluon currents of length L+1, the top
+    currents of length L, the t~ rows of length L and, at L = k-1, the bare
+    full-length contractions T0; every item depends on earlier stages only.
     """
-    base = k + 1
-    # canonical gluon-current nodes, lengths 2..k-1
-    jn = []
-    for L in range(2, k):
-        for seq in itertools.permutations(range(k), L):
-            rep, _ = _canonical(seq)
-            if rep == seq:
-                jn.append(seq)
-    jid = {s: i for i, s in enumerate(jn)}
-    NJ = len(jn)
-    jn_off, off = [], 0
-    for s in jn:
-        jn_off.append(off)
+    seqs = [s for L in range(1, k) for s in itertools.permutations(range(k), L)]
+    jo, off = {}, 0
+    for s in seqs:
+        jo[s] = off
         off += 1 << len(s)
     J_TOTAL = off
-    jlen_first = [0] * (k + 2)
-    for L in range(k + 2):
-        jlen_first[L] = sum(1 for s in jn if len(s) < L)
-    # references of every ordered sequence of length 1..k-1 (and k for full)
-    ncode = base**k
-    seq_ref = [-1] * ncode
-    seq_mask = [0] * (base**k)
-    for L in range(1, k + 1):
-        for seq in itertools.permutations(range(k), L):
-            c = _code(seq, base)
-            seq_mask[c] = _mask(seq)
-            if L == 1:
-                seq_ref[c] = ((NJ + seq[0]) << 2)
-            elif L < k:
-                rep, sgn = _canonical(seq)
-                rev = 1 if rep != seq else 0
-                seq_ref[c] = (jid[rep] << 2) | (rev << 1) | (1 if sgn < 0 else 0)
-    # full-length canonical orderings
-    perms = permutations(k)
-    fn = []
-    for s in perms:
-        rep, _ = _canonical(s)
-        if rep == s:
-            fn.append(s)
-    fid = {s: i for i, s in enumerate(fn)}
-    perm_full = []
-    for s in perms:
-        rep, sgn = _canonical(s)
-        rev = 1 if rep != s else 0
-        perm_full.append((fid[rep] << 2) | (rev << 1) | (1 if sgn < 0 else 0))
-    # top-line prefix nodes, lengths 1..k-1 (all orders)
-    on = [seq for L in range(1, k) for seq in itertools.permutations(range(k), L)]
-    on_off, off = [], 0
-    opos = [-1] * ncode
-    for i, s in enumerate(on):
-        on_off.append(off)
-        opos[_code(s, base)] = i
+    oo, off = {}, 0
+    for s in seqs:
+        oo[s] = off
         off += 2 << len(s)
     O_TOTAL = off
-    olen_first = [0] * (k + 2)
-    for L in range(k + 2):
-        olen_first[L] = sum(1 for s in on if len(s) < L)
-    # t~-side rows for every reference id (externals and J nodes)
-    r_len = [len(s) for s in jn] + [1] * k
-    r_off, off = [], 0
-    for L in r_len:
-        r_off.append(off)
-        off += 2 << L
+    ro, off = {}, 0
+    for s in seqs:
+        ro[s] = off
+        off += 2 << len(s)
     R_TOTAL = off
-    L = []
-    w = L.append
-    w(f"namespace rec{k} {{")
-    w(f"constexpr int NJ = {NJ}, J_TOTAL = {J_TOTAL}, NF = {len(fn)}, NO = {len(on)}, O_TOTAL = {O_TOTAL};")
-    w(f"constexpr int NR = {NJ + k}, R_TOTAL = {R_TOTAL}, BASE = {base}, NCODE = {ncode};")
-    w(_arr("jn_code", "int", [_code(s, base) for s in jn]))
-    w(_arr("jn_off", "int", jn_off))
-    w(_arr("jlen_first", "int", jlen_first))
-    w(_arr("seq_ref", "int", seq_ref))
-    w(_arr("seq_mask", "int", seq_mask))
-    w(_arr("fn_code", "int", [_code(s, base) for s in fn]))
-    w(_arr("perm_code", "int", [_code(s, base) for s in perms]))
-    w(_arr("perm_full", "int", perm_full))
-    w(_arr("on_code", "int", [_code(s, base) for s in on]))
-    w(_arr("on_off", "int", on_off))
-    w(_arr("olen_first", "int", olen_first))
-    w(_arr("opos", "int", opos))
-    w(_arr("r_len", "int", r_len))
-    w(_arr("r_off", "int", r_off))
-    # MadGraph helicity index of a (gluon bits, top bit, antitop bit) config
+    perms = permutations(k)
+    pidx = {p: i for i, p in enumerate(perms)}
+
+    prog = []  # flat int records
+    parts = []  # per stage: list of (type, L, n_nodes, first_record, record_size)
+
+    def cur_record(s, out_off, out_rev, sign):
+        L = len(s)
+        rec = [out_off, out_rev, sign, _mask(s)]
+        for i in range(1, L):
+            a, b = s[:i], s[i:]
+            rec += [jo[a], jo[b], _mask(a), _mask(b)]
+        for i in range(1, L):
+            for j in range(i + 1, L):
+                rec += [jo[s[:i]], jo[s[i:j]], jo[s[j:]]]
+        return rec
+
+    TYPE_J, TYPE_T0, TYPE_O, TYPE_R = 0, 1, 2, 3
+    for stage in range(1, k):
+        plist = []
+        # gluon currents of length stage+1 (canonical representatives only)
+        L = stage + 1
+        if L <= k - 1:
+            recs = []
+            for s in itertools.permutations(range(k), L):
+                rep, _ = _canonical(s)
+                if rep != s:
+                    continue
+                rev = tuple(reversed(s))
+                recs.append(cur_record(s, jo[s], jo[rev], (-1) ** (L + 1)))
+            plist.append((TYPE_J, L, len(recs), len(prog), len(recs[0])))
+            for r in recs:
+                prog += r
+        # top-line currents with `stage` gluons
+        L = stage
+        recs = []
+        for a in itertools.permutations(range(k), L):
+            rec = [oo[a], _mask(a)]
+            for i in range(L):
+                prev = -1 if i == 0 else oo[a[:i]]
+                rec += [prev, jo[a[i:]]]
+            recs.append(rec)
+        plist.append((TYPE_O, L, len(recs), len(prog), len(recs[0])))
+        for r in recs:
+            prog += r
+        # t~ rows of every sequence of length `stage`
+        recs = [[ro[b], jo[b]] for b in itertools.permutations(range(k), L)]
+        plist.append((TYPE_R, L, len(recs), len(prog), 2))
+        for r in recs:
+            prog += r
+        if stage == k - 1:
+            recs = []
+            for s in perms:
+                rep, _ = _canonical(s)
+                if rep != s:
+                    continue
+                rev = tuple(reversed(s))
+                recs.append(cur_record(s, pidx[s], pidx[rev], (-1) ** (k + 1)))
+            plist.append((TYPE_T0, k, len(recs), len(prog), len(recs[0])))
+            # T0 items write their value straight into the amplitude of the
+            # helicity combination: hunpack[sigma][pattern] = gluon helicity bits
+            for r in recs:
+                prog += r
+        parts.append(plist)
+    # amplitude records: per ordering, for the splits i = 1..k-1: (O offset, R offset)
+    arec = []
+    for s in perms:
+        for i in range(1, k):
+            arec += [oo[s[:i]], ro[s[i:]]]
+    hpack = []
+    hunpack = []
+    for s in perms:
+        for hg in range(1 << k):
+            hpack.append(sum(((hg >> g) & 1) << j for j, g in enumerate(s)))
+        for hp in range(1 << k):
+            hunpack.append(sum(((hp >> j) & 1) << g for j, g in enumerate(s)))
+    # flatten the stage/part descriptors
+    pdesc = []
+    stage_first = []
+    for plist in parts:
+        stage_first.append(len(pdesc) // 5)
+        for p in plist:
+            pdesc += list(p)
+    stage_first.append(len(pdesc) // 5)
     hels = helicities(k)
     hidx = {tuple(int(v) for v in h): i for i, h in enumerate(hels)}
     cfg_to_mg = []
@@ -391,6 +427,18 @@ def emit_recycled_tables(k):
         h[2] = 1 if ht else -1
         h[3] = 1 if htb else -1
         cfg_to_mg.append(hidx[tuple(h)])
+    L = []
+    w = L.append
+    w(f"namespace rec{k} {{")
+    w(f"constexpr int J_TOTAL = {J_TOTAL}, O_TOTAL = {O_TOTAL}, R_TOTAL = {R_TOTAL};")
+    w(f"constexpr int NSTAGE = {k - 1}, NPART = {len(pdesc) // 5};")
+    w(_arr("prog", "int", prog))
+    w(_arr("pdesc", "int", pdesc))
+    w(_arr("stage_first", "int", stage_first))
+    w(_arr("arec", "int", arec))
+    w(_arr("hpack", "unsigned char", hpack))
+    w(_arr("hunpack", "unsigned char", hunpack))
+    w(_arr("jo_ext", "int", [jo[(q,)] for q in range(k)]))
     w(_arr("cfg_to_mg", "int", cfg_to_mg))
     w("}  // namespace")
     return "\n".join(L)

@@ -3,6 +3,7 @@
 // madflow carries with float32 rounding.
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #define MF_HD __host__ __device__ __forceinline__
@@ -32,7 +33,7 @@ template <class T, class S> MF_HD cx<T> ccast(cx<S> a) { return {(T)a.re, (T)a.i
 
 // Slots 2-5 of a HELAS wavefunction (the momentum flow of slots 0-1 is kept
 // per subset of external legs instead).
-template <class T> struct W4 {
+template <class T> struct alignas(16) W4 {
   cx<T> v[4];
 };
 template <class T> MF_HD W4<T> w4zero() {

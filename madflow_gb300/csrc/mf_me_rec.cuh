@@ -1,22 +1,22 @@
 // Helicity-recycling evaluation of g g > t t~ + (K-2) g: one thread block per
-// event, currents shared between the helicity combinations that agree on the
-// legs they depend on.
+// event, every current computed once for the helicity combinations that
+// agree on the legs it depends on.
 //
-//   gluon currents J(s; h_s)            per canonical ordered gluon sequence s
-//                                       and helicities of the gluons of s;
-//   bare full-length contractions T0    wtb^T S(J(sigma; h_g)) wt, per
-//                                       canonical sigma, h_g, h_t, h_tbar;
-//   top-line currents O(a; h_t, h_a)    per ordered prefix a (the gluons
-//                                       attached next to the top);
-//   t~-side rows RW(b; h_tb, h_b)       wtb^T S(J(b)), per gluon sequence b;
-//   partial amplitudes A(sigma; h) = T0 + sum_{sigma = a|b} RW(b) . O(a);
-//   colour sum sum_{ab} C_ab Re(A_a A_b^*).
+//   J(s; h_s)        gluon current of every ordered gluon sequence s (length
+//                    1..K-1; length 1 = the external gluons)
+//   O(a; h_t, h_a)   top-line current with the ordered prefix a attached
+//   R(b; h_tb, h_b)  the t~-side row wtb^T S(J(b))
+//   A(sigma; h) = wtb^T S(J(sigma)) wt + sum_{sigma = a|b} R(b) . O(a)
+//   |M|^2 = sum_h sum_{sigma,tau} C_{sigma tau} Re(A(sigma; h) A(tau; h)^*)
 //
-// Every stage is a loop over independent work items spread over the threads
-// of the block (tid, nt); stages are separated by __syncthreads().  The
-// stage functions are host-callable so the CPU test suite can run them one
-// thread at a time against the oracle.  Tables come from the generated
-// header of the process (namespace rec<K>, see codegen.emit_recycled_tables).
+// The generator (codegen.emit_program) lays the evaluation out as a flat
+// program: stage L computes the gluon currents of length L+1, the top
+// currents and t~ rows of length L, and at L = K-1 the full-length
+// contractions, which it writes straight into the amplitudes.  Each stage is
+// a set of independent items spread over the block's threads (tid, nt), read
+// from precomputed operand records; stages are separated by __syncthreads().
+// The stage functions are host-callable so the CPU test suite can run them
+// one thread at a time against the oracle.
 #pragma once
 #include "mf_helas.cuh"
 #include "mf_phasespace.cuh"
@@ -30,111 +30,70 @@ template <int K> struct RecTraits;
 #define MF_TBL(NS, NAME, I) (NS::NAME##_h[(I)])
 #endif
 
-#define MF_DEFINE_REC(KK)                                                                             \
-  template <> struct RecTraits<KK> {                                                                  \
-    static constexpr int K = KK, NJ = rec##KK::NJ, J_TOTAL = rec##KK::J_TOTAL, NF = rec##KK::NF;      \
-    static constexpr int NO = rec##KK::NO, O_TOTAL = rec##KK::O_TOTAL, NR = rec##KK::NR;              \
-    static constexpr int R_TOTAL = rec##KK::R_TOTAL, BASE = rec##KK::BASE;                            \
-    static constexpr int NPERM = ttng##KK::NPERM, NCOMB = ttng##KK::NCOMB;                            \
-    static constexpr double DENOMINATOR = ttng##KK::DENOMINATOR, COLOUR_DEN = ttng##KK::COLOUR_DEN;   \
-    MF_D static int jn_code(int i) { return MF_TBL(rec##KK, jn_code, i); }                            \
-    MF_D static int jn_off(int i) { return MF_TBL(rec##KK, jn_off, i); }                              \
-    MF_D static int jlen_first(int i) { return MF_TBL(rec##KK, jlen_first, i); }                      \
-    MF_D static int seq_ref(int i) { return MF_TBL(rec##KK, seq_ref, i); }                            \
-    MF_D static int seq_mask(int i) { return MF_TBL(rec##KK, seq_mask, i); }                          \
-    MF_D static int fn_code(int i) { return MF_TBL(rec##KK, fn_code, i); }                            \
-    MF_D static int perm_code(int i) { return MF_TBL(rec##KK, perm_code, i); }                        \
-    MF_D static int perm_full(int i) { return MF_TBL(rec##KK, perm_full, i); }                        \
-    MF_D static int on_code(int i) { return MF_TBL(rec##KK, on_code, i); }                            \
-    MF_D static int on_off(int i) { return MF_TBL(rec##KK, on_off, i); }                              \
-    MF_D static int olen_first(int i) { return MF_TBL(rec##KK, olen_first, i); }                      \
-    MF_D static int opos(int i) { return MF_TBL(rec##KK, opos, i); }                                  \
-    MF_D static int r_len(int i) { return MF_TBL(rec##KK, r_len, i); }                                \
-    MF_D static int r_off(int i) { return MF_TBL(rec##KK, r_off, i); }                                \
-    MF_D static int cfg_to_mg(int i) { return MF_TBL(rec##KK, cfg_to_mg, i); }                        \
-    MF_D static float colour(int i) { return MF_TBL(ttng##KK, colour_num, i); }                       \
+#define MF_DEFINE_REC(KK)                                                                                 \
+  template <> struct RecTraits<KK> {                                                                      \
+    static constexpr int K = KK, J_TOTAL = rec##KK::J_TOTAL, O_TOTAL = rec##KK::O_TOTAL;                  \
+    static constexpr int R_TOTAL = rec##KK::R_TOTAL, NSTAGE = rec##KK::NSTAGE;                            \
+    static constexpr int NPERM = ttng##KK::NPERM, NCOMB = ttng##KK::NCOMB;                                \
+    static constexpr double DENOMINATOR = ttng##KK::DENOMINATOR, COLOUR_DEN = ttng##KK::COLOUR_DEN;       \
+    MF_D static int prog(int i) { return MF_TBL(rec##KK, prog, i); }                                      \
+    MF_D static int pdesc(int i) { return MF_TBL(rec##KK, pdesc, i); }                                    \
+    MF_D static int stage_first(int i) { return MF_TBL(rec##KK, stage_first, i); }                        \
+    MF_D static int arec(int i) { return MF_TBL(rec##KK, arec, i); }                                      \
+    MF_D static int hpack(int i) { return MF_TBL(rec##KK, hpack, i); }                                    \
+    MF_D static int hunpack(int i) { return MF_TBL(rec##KK, hunpack, i); }                                \
+    MF_D static int jo_ext(int i) { return MF_TBL(rec##KK, jo_ext, i); }                                  \
+    MF_D static int cfg_to_mg(int i) { return MF_TBL(rec##KK, cfg_to_mg, i); }                            \
+    MF_D static float colour(int i) { return MF_TBL(ttng##KK, colour_num, i); }                           \
   };
 
-// Workspace of one event (shared memory).
+// Currents in shared memory as 16-byte planes: plane p holds bytes
+// [16p, 16p+16) of every element, so threads touching consecutive elements
+// read consecutive 16-byte words (no bank conflicts).
+template <class T, int N> struct W4Planes {
+  static constexpr int NPL = (int)(sizeof(W4<T>) / 16);
+  int4 pl[NPL][N > 0 ? N : 1];
+  // memcpy keeps the 16-byte moves free of aliasing assumptions
+  MF_D W4<T> get(int i) const {
+    int4 t[NPL];
+#pragma unroll
+    for (int p = 0; p < NPL; ++p) t[p] = pl[p][i];
+    W4<T> w;
+    memcpy(&w, t, sizeof(w));
+    return w;
+  }
+  MF_D void put(int i, const W4<T>& w) {
+    int4 t[NPL];
+    memcpy(t, &w, sizeof(w));
+#pragma unroll
+    for (int p = 0; p < NPL; ++p) pl[p][i] = t[p];
+  }
+};
+
 template <class T, int K> struct RecWS {
   using R = RecTraits<K>;
-  W4<T> G[K][2];
+  W4Planes<T, R::J_TOTAL> J;
+  W4Planes<T, R::O_TOTAL> O;
+  W4Planes<T, R::R_TOTAL> RW;
   W4<T> WT[2], WTB[2];
-  W4<T> J[R::J_TOTAL > 0 ? R::J_TOTAL : 1];
-  cx<T> T0[R::NF][1 << K][4];
-  W4<T> O[R::O_TOTAL];
-  W4<T> RW[R::R_TOTAL];
   cx<T> A[1 << (K + 2)][R::NPERM];
 };
 
-template <int B> MF_D int pow_base(int e) {
-  int p = 1;
-  for (int i = 0; i < e; ++i) p *= B;
-  return p;
-}
-// code of the ordered sub-sequence s[i:j]
-template <int B> MF_D int sub_code(int code, int i, int j) { return (code / pow_base<B>(i)) % pow_base<B>(j - i); }
 MF_D int bit_reverse(int hp, int len) {
   int r = 0;
   for (int j = 0; j < len; ++j) r |= ((hp >> j) & 1) << (len - 1 - j);
   return r;
 }
-// helicity pattern of the sequence `code` (length len) from gluon helicity bits hg
-template <int B> MF_D int pack_hel(int hg, int code, int len) {
-  int hp = 0;
-  for (int j = 0; j < len; ++j) {
-    int g = (code % B) - 1;
-    code /= B;
-    hp |= ((hg >> g) & 1) << j;
-  }
-  return hp;
-}
 
-template <class T, int K> MF_D W4<T> rec_cur(const RecWS<T, K>& ws, int ref, int len, int hp) {
-  using R = RecTraits<K>;
-  int id = ref >> 2;
-  W4<T> w;
-  if (id >= R::NJ) {
-    w = ws.G[id - R::NJ][hp & 1];
-  } else {
-    int h = (ref & 2) ? bit_reverse(hp, len) : hp;
-    w = ws.J[R::jn_off(id) + h];
-  }
-  return (ref & 1) ? neg(w) : w;
-}
-
-// colour-ordered gluon current of the ordered sequence `code` (length L)
-template <class T, int K>
-MF_D W4<T> rec_gluon_current(const RecWS<T, K>& ws, const EvData<T, K>& ev, int code, int L, int hp) {
-  using R = RecTraits<K>;
-  constexpr int B = R::BASE;
-  W4<T> a3 = w4zero<T>(), a4 = w4zero<T>();
-  for (int i = 1; i < L; ++i) {
-    int cl = sub_code<B>(code, 0, i), cr = sub_code<B>(code, i, L);
-    W4<T> a = rec_cur<T, K>(ws, R::seq_ref(cl), i, hp & ((1 << i) - 1));
-    W4<T> b = rec_cur<T, K>(ws, R::seq_ref(cr), L - i, hp >> i);
-    vvv_add<T>(a, ev.Qg[R::seq_mask(cl)], b, ev.Qg[R::seq_mask(cr)], a3);
-  }
-  for (int i = 1; i < L; ++i)
-    for (int j = i + 1; j < L; ++j) {
-      int c1 = sub_code<B>(code, 0, i), c2 = sub_code<B>(code, i, j), c3 = sub_code<B>(code, j, L);
-      W4<T> a = rec_cur<T, K>(ws, R::seq_ref(c1), i, hp & ((1 << i) - 1));
-      W4<T> b = rec_cur<T, K>(ws, R::seq_ref(c2), j - i, (hp >> i) & ((1 << (j - i)) - 1));
-      W4<T> d = rec_cur<T, K>(ws, R::seq_ref(c3), L - j, hp >> j);
-      vvvv_add<T>(a, b, d, a4);
-    }
-  int m = R::seq_mask(code);
-  return combine<T>(ev.gv3[m], a3, ev.gv4[m], a4);
-}
-
-// stage 0: external wavefunctions (gluons for both helicities, t, t~)
+// stage 0: external wavefunctions (the gluons go to their length-1 J slots)
 template <class T, int K> MF_D void rec_st_ext(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid, int nt) {
+  using R = RecTraits<K>;
   const T sqh = (T)0.70710676908493042;  // madflow's float32-rounded sqrt(1/2)
   for (int i = tid; i < 2 * K + 4; i += nt) {
     if (i < 2 * K) {
       int q = i >> 1, b = i & 1;
       int part = gluon_particle<K>(q);
-      ws.G[q][b] = vxxxxx<T>(ev.pext[part], T(0), b ? T(1) : T(-1), part < 2 ? T(-1) : T(1), sqh);
+      ws.J.put(R::jo_ext(q) + b, vxxxxx<T>(ev.pext[part], T(0), b ? T(1) : T(-1), part < 2 ? T(-1) : T(1), sqh));
     } else if (i < 2 * K + 2) {
       int b = i - 2 * K;
       ws.WT[b] = oxxxxx<T>(ev.pext[2], ev.mt, b ? T(1) : T(-1), T(1));
@@ -145,17 +104,29 @@ template <class T, int K> MF_D void rec_st_ext(RecWS<T, K>& ws, const EvData<T, 
   }
 }
 
-// stage J(L): gluon currents of length L (2 <= L <= K-1)
-template <class T, int K> MF_D void rec_st_J(RecWS<T, K>& ws, const EvData<T, K>& ev, int L, int tid, int nt) {
+// colour-ordered gluon current from a record (see codegen.emit_program)
+template <class T, int K>
+MF_D W4<T> rec_current(const RecWS<T, K>& ws, const EvData<T, K>& ev, int r, int L, int hp) {
   using R = RecTraits<K>;
-  int first = R::jlen_first(L), cnt = R::jlen_first(L + 1) - first;
-  for (int it = tid; it < (cnt << L); it += nt) {
-    int node = first + (it >> L), hp = it & ((1 << L) - 1);
-    ws.J[R::jn_off(node) + hp] = rec_gluon_current<T, K>(ws, ev, R::jn_code(node), L, hp);
+  W4<T> a3 = w4zero<T>(), a4 = w4zero<T>();
+  int q = r + 4;
+  for (int i = 1; i < L; ++i, q += 4) {
+    W4<T> a = ws.J.get(R::prog(q) + (hp & ((1 << i) - 1)));
+    W4<T> b = ws.J.get(R::prog(q + 1) + (hp >> i));
+    vvv_add<T>(a, ev.Qg[R::prog(q + 2)], b, ev.Qg[R::prog(q + 3)], a3);
   }
+  for (int i = 1; i < L; ++i)
+    for (int j = i + 1; j < L; ++j, q += 3) {
+      W4<T> a = ws.J.get(R::prog(q) + (hp & ((1 << i) - 1)));
+      W4<T> b = ws.J.get(R::prog(q + 1) + ((hp >> i) & ((1 << (j - i)) - 1)));
+      W4<T> d = ws.J.get(R::prog(q + 2) + (hp >> j));
+      vvvv_add<T>(a, b, d, a4);
+    }
+  int m = R::prog(r + 3);
+  return combine<T>(ev.gv3[m], a3, ev.gv4[m], a4);
 }
 
-// row vector r = F1^T S(V): F1^T S(V) F2 = r . F2
+// row vector r = F1^T S(V), so that F1^T S(V) F2 = r . F2
 template <class T> MF_D W4<T> sandwich_row(const W4<T>& F1, const W4<T>& V) {
   cx<T> p03 = V.v[0] + V.v[3], m03 = V.v[0] - V.v[3];
   cx<T> p12 = V.v[1] + mul_i(V.v[2]), m12 = V.v[1] - mul_i(V.v[2]);
@@ -170,83 +141,77 @@ template <class T> MF_D cx<T> dot4(const W4<T>& a, const W4<T>& b) {
   return a.v[0] * b.v[0] + a.v[1] * b.v[1] + a.v[2] * b.v[2] + a.v[3] * b.v[3];
 }
 
-// stage T0 + RW + O(1): all depend only on the gluon currents and externals
-template <class T, int K> MF_D void rec_st_mid(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid, int nt) {
+// one stage (1..K-1) of the program
+template <class T, int K>
+MF_D void rec_stage(RecWS<T, K>& ws, const EvData<T, K>& ev, int stage, int tid, int nt) {
   using R = RecTraits<K>;
-  const int n_t0 = R::NF << K;
-  const int n_o1 = R::olen_first(2) * 4;  // K prefixes of length 1, x 2 (h_t) x 2 (h)
-  const int total = n_t0 + R::R_TOTAL + n_o1;
+  const int p0 = R::stage_first(stage - 1), p1 = R::stage_first(stage);
+  int total = 0;
+  for (int p = p0; p < p1; ++p) {
+    int L = R::pdesc(5 * p + 1);
+    int per = (R::pdesc(5 * p) == 0 || R::pdesc(5 * p) == 1) ? (1 << L) : (2 << L);
+    total += R::pdesc(5 * p + 2) * per;
+  }
   for (int it = tid; it < total; it += nt) {
-    if (it < n_t0) {
-      int f = it >> K, hp = it & ((1 << K) - 1);
-      W4<T> Jf = rec_gluon_current<T, K>(ws, ev, R::fn_code(f), K, hp);
-      for (int q = 0; q < 4; ++q) ws.T0[f][hp][q] = dot4(sandwich_row(ws.WTB[q >> 1], Jf), ws.WT[q & 1]);
-    } else if (it < n_t0 + R::R_TOTAL) {
-      int idx = it - n_t0;
-      int r = 0;
-      while (r + 1 < R::NR && R::r_off(r + 1) <= idx) ++r;
-      int L = R::r_len(r), rem = idx - R::r_off(r);
-      int htb = rem >> L, hp = rem & ((1 << L) - 1);
-      const W4<T>& J = (r >= R::NJ) ? ws.G[r - R::NJ][hp] : ws.J[R::jn_off(r) + hp];
-      ws.RW[idx] = sandwich_row(ws.WTB[htb], J);
-    } else {
-      int idx = it - n_t0 - R::R_TOTAL;
-      int node = idx >> 2, ht = (idx >> 1) & 1, hp = idx & 1;
-      int code = R::on_code(node);
-      W4<T> y = w4zero<T>();
-      sv_add<T>(rec_cur<T, K>(ws, R::seq_ref(code), 1, hp), ws.WT[ht], y);
-      int m = R::seq_mask(code);
-      ws.O[R::on_off(node) + (ht << 1) + hp] = topprop<T>(ev.Qt[m], ev.mt, ev.tden[m], y);
+    int p = p0, local = it;
+    int type, L, per;
+    for (;;) {
+      type = R::pdesc(5 * p);
+      L = R::pdesc(5 * p + 1);
+      per = (type <= 1) ? (1 << L) : (2 << L);
+      int cnt = R::pdesc(5 * p + 2) * per;
+      if (local < cnt) break;
+      local -= cnt;
+      ++p;
     }
-  }
-}
-
-// stage O(L), 2 <= L <= K-1: top-line currents with L gluons attached
-template <class T, int K> MF_D void rec_st_O(RecWS<T, K>& ws, const EvData<T, K>& ev, int L, int tid, int nt) {
-  using R = RecTraits<K>;
-  constexpr int B = R::BASE;
-  int first = R::olen_first(L), cnt = R::olen_first(L + 1) - first;
-  for (int it = tid; it < (cnt << (L + 1)); it += nt) {
-    int node = first + (it >> (L + 1)), rem = it & ((2 << L) - 1);
-    int ht = rem >> L, hp = rem & ((1 << L) - 1);
-    int code = R::on_code(node);
-    W4<T> y = w4zero<T>();
-    for (int i = 0; i < L; ++i) {
-      int cb = sub_code<B>(code, i, L);
-      W4<T> Jb = rec_cur<T, K>(ws, R::seq_ref(cb), L - i, hp >> i);
-      if (i == 0) {
-        sv_add<T>(Jb, ws.WT[ht], y);
-      } else {
-        int ca = sub_code<B>(code, 0, i);
-        sv_add<T>(Jb, ws.O[R::on_off(R::opos(ca)) + (ht << i) + (hp & ((1 << i) - 1))], y);
+    const int node = local / per, sub = local % per;
+    const int r = R::pdesc(5 * p + 3) + node * R::pdesc(5 * p + 4);
+    if (type == 0) {  // gluon current, written for s and reverse(s)
+      W4<T> v = rec_current<T, K>(ws, ev, r, L, sub);
+      ws.J.put(R::prog(r) + sub, v);
+      ws.J.put(R::prog(r + 1) + bit_reverse(sub, L), R::prog(r + 2) < 0 ? neg(v) : v);
+    } else if (type == 1) {  // full length: bare contractions into the amplitudes
+      W4<T> Jf = rec_current<T, K>(ws, ev, r, K, sub);
+      const int s = R::prog(r), srev = R::prog(r + 1), sg = R::prog(r + 2);
+      const int hg = R::hunpack(s * (1 << K) + sub);
+      for (int q = 0; q < 4; ++q) {
+        cx<T> t = dot4(sandwich_row(ws.WTB[q >> 1], Jf), ws.WT[q & 1]);
+        int c = hg | ((q & 1) << K) | ((q >> 1) << (K + 1));
+        ws.A[c][s] = t;
+        ws.A[c][srev] = sg < 0 ? -t : t;
       }
+    } else if (type == 2) {  // top-line current
+      const int ht = sub >> L, hp = sub & ((1 << L) - 1);
+      W4<T> y = w4zero<T>();
+      for (int i = 0; i < L; ++i) {
+        int prev = R::prog(r + 2 + 2 * i), jsuf = R::prog(r + 3 + 2 * i);
+        W4<T> Jb = ws.J.get(jsuf + (hp >> i));
+        if (prev < 0) sv_add<T>(Jb, ws.WT[ht], y);
+        else sv_add<T>(Jb, ws.O.get(prev + (ht << i) + (hp & ((1 << i) - 1))), y);
+      }
+      int m = R::prog(r + 1);
+      ws.O.put(R::prog(r) + sub, topprop<T>(ev.Qt[m], ev.mt, ev.tden[m], y));
+    } else {  // t~ row
+      const int htb = sub >> L, hp = sub & ((1 << L) - 1);
+      ws.RW.put(R::prog(r) + sub, sandwich_row(ws.WTB[htb], ws.J.get(R::prog(r + 1) + hp)));
     }
-    int m = R::seq_mask(code);
-    ws.O[R::on_off(node) + (ht << L) + hp] = topprop<T>(ev.Qt[m], ev.mt, ev.tden[m], y);
   }
 }
 
-// stage A: partial amplitudes of every (helicity combination, ordering)
+// stage A: add the top-line terms to every (helicity combination, ordering)
 template <class T, int K> MF_D void rec_st_A(RecWS<T, K>& ws, int tid, int nt) {
   using R = RecTraits<K>;
-  constexpr int B = R::BASE;
   constexpr int NC = 1 << (K + 2);
   for (int it = tid; it < NC * R::NPERM; it += nt) {
     int c = it / R::NPERM, s = it % R::NPERM;
     int hg = c & ((1 << K) - 1), ht = (c >> K) & 1, htb = (c >> (K + 1)) & 1;
-    int code = R::perm_code(s), pf = R::perm_full(s);
-    int hfull = pack_hel<B>(hg, code, K);
-    int hcan = (pf & 2) ? bit_reverse(hfull, K) : hfull;
-    cx<T> a = ws.T0[pf >> 2][hcan][ht | (htb << 1)];
-    if (pf & 1) a = -a;
+    int hfull = R::hpack(s * (1 << K) + hg);
+    cx<T> a = ws.A[c][s];
     for (int i = 1; i < K; ++i) {
-      int ca = sub_code<B>(code, 0, i), cb = sub_code<B>(code, i, K);
-      const W4<T>& O = ws.O[R::on_off(R::opos(ca)) + (ht << i) + (hfull & ((1 << i) - 1))];
-      int ref = R::seq_ref(cb), id = ref >> 2, Lb = K - i;
-      int hb = hfull >> i;
-      if (ref & 2) hb = bit_reverse(hb, Lb);
-      cx<T> t = dot4(ws.RW[R::r_off(id) + (htb << Lb) + hb], O);
-      a = (ref & 1) ? a - t : a + t;
+      int oo = R::arec(s * 2 * (K - 1) + 2 * (i - 1)), ro = R::arec(s * 2 * (K - 1) + 2 * (i - 1) + 1);
+      W4<T> O = ws.O.get(oo + (ht << i) + (hfull & ((1 << i) - 1)));
+      W4<T> Rw = ws.RW.get(ro + (htb << (K - i)) + (hfull >> i));
+      a += dot4(Rw, O);
     }
     ws.A[c][s] = a;
   }
@@ -269,19 +234,32 @@ template <class T, int K> MF_D double rec_st_colour(const RecWS<T, K>& ws, const
   return acc;
 }
 
-// colour sum of one helicity combination c (for per-helicity outputs)
+// colour sum of one helicity combination c (per-helicity outputs)
 template <class T, int K> MF_D double rec_colour_one(const RecWS<T, K>& ws, const T* cm, int c) {
   using R = RecTraits<K>;
   constexpr int NP = R::NPERM;
   double acc = 0.0;
+  const cx<T>* A = ws.A[c];
   for (int a = 0; a < NP; ++a) {
-    const cx<T>* A = ws.A[c];
     cx<T> z = {T(0), T(0)};
     for (int b = a + 1; b < NP; ++b) z += cm[a * NP + b] * A[b];
     acc += (double)(cm[a * NP + a] * (A[a].re * A[a].re + A[a].im * A[a].im) + T(2) * (A[a].re * z.re + A[a].im * z.im));
   }
   return acc;
 }
+
+// the whole evaluation of one event by nt "threads" run one at a time (host tests)
+template <class T, int K> struct RecHostRun {
+  static double run(RecWS<T, K>& ws, const EvData<T, K>& ev, const T* cm, int nt) {
+    for (int t = 0; t < nt; ++t) rec_st_ext<T, K>(ws, ev, t, nt);
+    for (int st = 1; st < K; ++st)
+      for (int t = 0; t < nt; ++t) rec_stage<T, K>(ws, ev, st, t, nt);
+    for (int t = 0; t < nt; ++t) rec_st_A<T, K>(ws, t, nt);
+    double tot = 0.0;
+    for (int t = 0; t < nt; ++t) tot += rec_st_colour<T, K>(ws, cm, t, nt);
+    return tot;
+  }
+};
 
 constexpr int MF_REC_NT = 128;  // threads per event block
 
@@ -296,7 +274,7 @@ template <class T, int K> struct RecSmem {
 #ifdef __CUDACC__
 // Block-per-event |M|^2: ps [K+2][4][N]; couplings [N or 1][3] complex;
 // skip (optional) [N]: events with skip[e] == 0 get out[e] = 0 without work;
-// out [N]; hel_out (optional) [ncomb][N] MadGraph helicity order.
+// out [N]; hel_out (optional) [ncomb][N] in MadGraph helicity order.
 template <int K, class T>
 __global__ void __launch_bounds__(MF_REC_NT) me_rec_kernel(const double* __restrict__ ps, int64_t N, double mt,
                                                           double wt, const double* __restrict__ coup,
@@ -324,14 +302,8 @@ __global__ void __launch_bounds__(MF_REC_NT) me_rec_kernel(const double* __restr
     __syncthreads();
     rec_st_ext<T, K>(S.ws, S.ev, tid, nt);
     __syncthreads();
-    for (int L = 2; L < K; ++L) {
-      rec_st_J<T, K>(S.ws, S.ev, L, tid, nt);
-      __syncthreads();
-    }
-    rec_st_mid<T, K>(S.ws, S.ev, tid, nt);
-    __syncthreads();
-    for (int L = 2; L < K; ++L) {
-      rec_st_O<T, K>(S.ws, S.ev, L, tid, nt);
+    for (int st = 1; st < K; ++st) {
+      rec_stage<T, K>(S.ws, S.ev, st, tid, nt);
       __syncthreads();
     }
     rec_st_A<T, K>(S.ws, tid, nt);

@@ -113,14 +113,16 @@ MF_D void evdata_subset(EvData<T, K>& ev, int s, const double (*p)[4], double mt
   for (int c = 0; c < 4; ++c) { ev.Qg[s][c] = (T)Q[c]; ev.Qt[s][c] = (T)Qt[c]; }
   int nbits = 0;
   for (int j = 0; j < K; ++j) nbits += (s >> j) & 1;
+  // The sums and the invariants P^2, P^2 - M^2 (where the top pole cancels)
+  // are FP64; the divisions then run in T.
   if (nbits >= 2) {
-    double iq = 1.0 / q2;
-    ev.gv3[s] = ccast<T>(cx<double>{gc10.re * iq, gc10.im * iq});
-    ev.gv4[s] = ccast<T>(cx<double>{gc12.im * iq, -gc12.re * iq});
+    T iq = T(1) / (T)q2;
+    ev.gv3[s] = cx<T>{(T)gc10.re * iq, (T)gc10.im * iq};
+    ev.gv4[s] = cx<T>{(T)gc12.im * iq, -(T)gc12.re * iq};
   } else {
     ev.gv3[s] = cx<T>{T(0), T(0)};
     ev.gv4[s] = cx<T>{T(0), T(0)};
   }
-  cx<double> den = {t2 - mt * mt, mt * wt};
-  ev.tden[s] = ccast<T>(cdiv(mul_i(gc11), den));
+  cx<T> den = {(T)(t2 - mt * mt), (T)(mt * wt)};
+  ev.tden[s] = cdiv(mul_i(ccast<T>(gc11)), den);
 }

@@ -29,17 +29,9 @@ static double smatrix_one(const double* p, const double* coup, double mt, double
     for (int c = 0; c < 4; ++c) ev->pext[i][c] = (T)pd[i][c];
   ev->mt = (T)mt;
   const int nt = 7;  // an odd "block size" exercises the item striding
-  for (int t = 0; t < nt; ++t) rec_st_ext<T, K>(*ws, *ev, t, nt);
-  for (int L = 2; L < K; ++L)
-    for (int t = 0; t < nt; ++t) rec_st_J<T, K>(*ws, *ev, L, t, nt);
-  for (int t = 0; t < nt; ++t) rec_st_mid<T, K>(*ws, *ev, t, nt);
-  for (int L = 2; L < K; ++L)
-    for (int t = 0; t < nt; ++t) rec_st_O<T, K>(*ws, *ev, L, t, nt);
-  for (int t = 0; t < nt; ++t) rec_st_A<T, K>(*ws, t, nt);
   T cm[R::NPERM * R::NPERM];
   for (int i = 0; i < R::NPERM * R::NPERM; ++i) cm[i] = (T)R::colour(i);
-  double tot = 0.0;
-  for (int t = 0; t < nt; ++t) tot += rec_st_colour<T, K>(*ws, cm, t, nt);
+  double tot = RecHostRun<T, K>::run(*ws, *ev, cm, nt);
   double sc = (c11.re * c11.re + c11.im * c11.im) / (R::COLOUR_DEN * R::DENOMINATOR);
   if (hel_out)
     for (int c = 0; c < (1 << (K + 2)); ++c)
