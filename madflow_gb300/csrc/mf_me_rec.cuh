@@ -76,7 +76,7 @@ template <class T, int K> struct RecWS {
   W4Planes<T, R::O_TOTAL> O;
   W4Planes<T, R::R_TOTAL> RW;
   W4<T> WT[2], WTB[2];
-  cx<T> A[1 << (K + 2)][R::NPERM];
+  cx<T> A[R::NPERM * (1 << (K + 2))];  // [ordering][helicity combination]
 };
 
 MF_D int bit_reverse(int hp, int len) {
@@ -141,109 +141,111 @@ template <class T> MF_D cx<T> dot4(const W4<T>& a, const W4<T>& b) {
   return a.v[0] * b.v[0] + a.v[1] * b.v[1] + a.v[2] * b.v[2] + a.v[3] * b.v[3];
 }
 
-// one stage (1..K-1) of the program
+// one item of a program part
+template <class T, int K>
+MF_D void rec_item(RecWS<T, K>& ws, const EvData<T, K>& ev, int type, int L, int r, int sub) {
+  using R = RecTraits<K>;
+  constexpr int NC = 1 << (K + 2);
+  if (type == 0) {  // gluon current, written for s and reverse(s)
+    W4<T> v = rec_current<T, K>(ws, ev, r, L, sub);
+    ws.J.put(R::prog(r) + sub, v);
+    ws.J.put(R::prog(r + 1) + bit_reverse(sub, L), R::prog(r + 2) < 0 ? neg(v) : v);
+  } else if (type == 1) {  // full length: bare contractions into the amplitudes
+    W4<T> Jf = rec_current<T, K>(ws, ev, r, K, sub);
+    const int s = R::prog(r), srev = R::prog(r + 1), sg = R::prog(r + 2);
+    const int hg = R::hunpack(s * (1 << K) + sub);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      cx<T> t = dot4(sandwich_row(ws.WTB[q >> 1], Jf), ws.WT[q & 1]);
+      int c = hg | ((q & 1) << K) | ((q >> 1) << (K + 1));
+      ws.A[s * NC + c] = t;
+      ws.A[srev * NC + c] = sg < 0 ? -t : t;
+    }
+  } else if (type == 2) {  // top-line current
+    const int ht = sub >> L, hp = sub & ((1 << L) - 1);
+    W4<T> y = w4zero<T>();
+    for (int i = 0; i < L; ++i) {
+      int prev = R::prog(r + 2 + 2 * i), jsuf = R::prog(r + 3 + 2 * i);
+      W4<T> Jb = ws.J.get(jsuf + (hp >> i));
+      if (prev < 0) sv_add<T>(Jb, ws.WT[ht], y);
+      else sv_add<T>(Jb, ws.O.get(prev + (ht << i) + (hp & ((1 << i) - 1))), y);
+    }
+    int m = R::prog(r + 1);
+    ws.O.put(R::prog(r) + sub, topprop<T>(ev.Qt[m], ev.mt, ev.tden[m], y));
+  } else {  // t~ row
+    const int htb = sub >> L, hp = sub & ((1 << L) - 1);
+    ws.RW.put(R::prog(r) + sub, sandwich_row(ws.WTB[htb], ws.J.get(R::prog(r + 1) + hp)));
+  }
+}
+
+// one stage (1..K-1) of the program: the parts' items are dealt to the
+// threads round-robin as if they formed one list
 template <class T, int K>
 MF_D void rec_stage(RecWS<T, K>& ws, const EvData<T, K>& ev, int stage, int tid, int nt) {
   using R = RecTraits<K>;
   const int p0 = R::stage_first(stage - 1), p1 = R::stage_first(stage);
-  int total = 0;
+  int base = 0;
   for (int p = p0; p < p1; ++p) {
-    int L = R::pdesc(5 * p + 1);
-    int per = (R::pdesc(5 * p) == 0 || R::pdesc(5 * p) == 1) ? (1 << L) : (2 << L);
-    total += R::pdesc(5 * p + 2) * per;
-  }
-  for (int it = tid; it < total; it += nt) {
-    int p = p0, local = it;
-    int type, L, per;
-    for (;;) {
-      type = R::pdesc(5 * p);
-      L = R::pdesc(5 * p + 1);
-      per = (type <= 1) ? (1 << L) : (2 << L);
-      int cnt = R::pdesc(5 * p + 2) * per;
-      if (local < cnt) break;
-      local -= cnt;
-      ++p;
-    }
-    const int node = local / per, sub = local % per;
-    const int r = R::pdesc(5 * p + 3) + node * R::pdesc(5 * p + 4);
-    if (type == 0) {  // gluon current, written for s and reverse(s)
-      W4<T> v = rec_current<T, K>(ws, ev, r, L, sub);
-      ws.J.put(R::prog(r) + sub, v);
-      ws.J.put(R::prog(r + 1) + bit_reverse(sub, L), R::prog(r + 2) < 0 ? neg(v) : v);
-    } else if (type == 1) {  // full length: bare contractions into the amplitudes
-      W4<T> Jf = rec_current<T, K>(ws, ev, r, K, sub);
-      const int s = R::prog(r), srev = R::prog(r + 1), sg = R::prog(r + 2);
-      const int hg = R::hunpack(s * (1 << K) + sub);
-      for (int q = 0; q < 4; ++q) {
-        cx<T> t = dot4(sandwich_row(ws.WTB[q >> 1], Jf), ws.WT[q & 1]);
-        int c = hg | ((q & 1) << K) | ((q >> 1) << (K + 1));
-        ws.A[c][s] = t;
-        ws.A[c][srev] = sg < 0 ? -t : t;
-      }
-    } else if (type == 2) {  // top-line current
-      const int ht = sub >> L, hp = sub & ((1 << L) - 1);
-      W4<T> y = w4zero<T>();
-      for (int i = 0; i < L; ++i) {
-        int prev = R::prog(r + 2 + 2 * i), jsuf = R::prog(r + 3 + 2 * i);
-        W4<T> Jb = ws.J.get(jsuf + (hp >> i));
-        if (prev < 0) sv_add<T>(Jb, ws.WT[ht], y);
-        else sv_add<T>(Jb, ws.O.get(prev + (ht << i) + (hp & ((1 << i) - 1))), y);
-      }
-      int m = R::prog(r + 1);
-      ws.O.put(R::prog(r) + sub, topprop<T>(ev.Qt[m], ev.mt, ev.tden[m], y));
-    } else {  // t~ row
-      const int htb = sub >> L, hp = sub & ((1 << L) - 1);
-      ws.RW.put(R::prog(r) + sub, sandwich_row(ws.WTB[htb], ws.J.get(R::prog(r + 1) + hp)));
-    }
+    const int type = R::pdesc(5 * p), L = R::pdesc(5 * p + 1);
+    const int lper = (type <= 1) ? L : L + 1;  // items per node = 1 << lper
+    const int cnt = R::pdesc(5 * p + 2) << lper;
+    const int rec0 = R::pdesc(5 * p + 3), rsz = R::pdesc(5 * p + 4);
+    int first = (tid - base) % nt;
+    if (first < 0) first += nt;
+    for (int local = first; local < cnt; local += nt)
+      rec_item<T, K>(ws, ev, type, L, rec0 + (local >> lper) * rsz, local & ((1 << lper) - 1));
+    base += cnt;
   }
 }
 
-// stage A: add the top-line terms to every (helicity combination, ordering)
+// stage A: add the top-line terms to every amplitude; items run over the
+// helicity combinations fastest so that neighbouring threads share operands
 template <class T, int K> MF_D void rec_st_A(RecWS<T, K>& ws, int tid, int nt) {
   using R = RecTraits<K>;
   constexpr int NC = 1 << (K + 2);
   for (int it = tid; it < NC * R::NPERM; it += nt) {
-    int c = it / R::NPERM, s = it % R::NPERM;
+    int s = it / NC, c = it % NC;
     int hg = c & ((1 << K) - 1), ht = (c >> K) & 1, htb = (c >> (K + 1)) & 1;
     int hfull = R::hpack(s * (1 << K) + hg);
-    cx<T> a = ws.A[c][s];
+    cx<T> a = ws.A[it];
+#pragma unroll
     for (int i = 1; i < K; ++i) {
       int oo = R::arec(s * 2 * (K - 1) + 2 * (i - 1)), ro = R::arec(s * 2 * (K - 1) + 2 * (i - 1) + 1);
       W4<T> O = ws.O.get(oo + (ht << i) + (hfull & ((1 << i) - 1)));
       W4<T> Rw = ws.RW.get(ro + (htb << (K - i)) + (hfull >> i));
       a += dot4(Rw, O);
     }
-    ws.A[c][s] = a;
+    ws.A[it] = a;
   }
 }
 
-// stage colour: sum over this thread's (combination, row) items of
-// C_aa |A_a|^2 + 2 sum_{b>a} C_ab Re(A_a A_b^*); cm = integer numerators
+// stage colour: sum over this thread's (row, combination) items of
+// C_aa |A_a|^2 + 2 sum_{b>a} C_ab Re(A_a A_b^*); cm = integer numerators.
+// Summed in T per thread (the per-event sums are FP64).
 template <class T, int K> MF_D double rec_st_colour(const RecWS<T, K>& ws, const T* cm, int tid, int nt) {
   using R = RecTraits<K>;
   constexpr int NP = R::NPERM, NC = 1 << (K + 2);
-  double acc = 0.0;
+  T acc = T(0);
   for (int it = tid; it < NC * NP; it += nt) {
-    int c = it / NP, a = it % NP;
-    const cx<T>* A = ws.A[c];
+    int a = it / NC, c = it % NC;
     cx<T> z = {T(0), T(0)};
-    for (int b = a + 1; b < NP; ++b) z += cm[a * NP + b] * A[b];
-    T s = cm[a * NP + a] * (A[a].re * A[a].re + A[a].im * A[a].im) + T(2) * (A[a].re * z.re + A[a].im * z.im);
-    acc += (double)s;
+    for (int b = a + 1; b < NP; ++b) z += cm[a * NP + b] * ws.A[b * NC + c];
+    cx<T> Aa = ws.A[it];
+    acc += cm[a * NP + a] * (Aa.re * Aa.re + Aa.im * Aa.im) + T(2) * (Aa.re * z.re + Aa.im * z.im);
   }
-  return acc;
+  return (double)acc;
 }
 
 // colour sum of one helicity combination c (per-helicity outputs)
 template <class T, int K> MF_D double rec_colour_one(const RecWS<T, K>& ws, const T* cm, int c) {
   using R = RecTraits<K>;
-  constexpr int NP = R::NPERM;
+  constexpr int NP = R::NPERM, NC = 1 << (K + 2);
   double acc = 0.0;
-  const cx<T>* A = ws.A[c];
   for (int a = 0; a < NP; ++a) {
     cx<T> z = {T(0), T(0)};
-    for (int b = a + 1; b < NP; ++b) z += cm[a * NP + b] * A[b];
-    acc += (double)(cm[a * NP + a] * (A[a].re * A[a].re + A[a].im * A[a].im) + T(2) * (A[a].re * z.re + A[a].im * z.im));
+    for (int b = a + 1; b < NP; ++b) z += cm[a * NP + b] * ws.A[b * NC + c];
+    cx<T> Aa = ws.A[a * NC + c];
+    acc += (double)(cm[a * NP + a] * (Aa.re * Aa.re + Aa.im * Aa.im) + T(2) * (Aa.re * z.re + Aa.im * z.im));
   }
   return acc;
 }

@@ -52,6 +52,42 @@ extern "C" int me_host_smatrix(int k, int prec, const double* p, int64_t N, cons
   return 0;
 }
 
+// ---- operation count of the recycled evaluation ------------------------------
+// A scalar that counts every +, -, *, / and sqrt (complex mul = 6, add = 2,
+// the convention the oracle's count uses).
+struct CountF {
+  double v;
+  static inline unsigned long long n = 0;
+  CountF() : v(0) {}
+  template <class A> CountF(A x) : v((double)x) {}
+  explicit operator double() const { return v; }
+};
+inline CountF operator+(CountF a, CountF b) { ++CountF::n; return CountF(a.v + b.v); }
+inline CountF operator-(CountF a, CountF b) { ++CountF::n; return CountF(a.v - b.v); }
+inline CountF operator*(CountF a, CountF b) { ++CountF::n; return CountF(a.v * b.v); }
+inline CountF operator/(CountF a, CountF b) { ++CountF::n; return CountF(a.v / b.v); }
+inline CountF operator-(CountF a) { return CountF(-a.v); }
+inline CountF& operator+=(CountF& a, CountF b) { a = a + b; return a; }
+inline bool operator==(CountF a, CountF b) { return a.v == b.v; }
+inline bool operator!=(CountF a, CountF b) { return a.v != b.v; }
+inline bool operator<(CountF a, CountF b) { return a.v < b.v; }
+inline bool operator>(CountF a, CountF b) { return a.v > b.v; }
+inline CountF sqrt(CountF a) { ++CountF::n; return CountF(std::sqrt(a.v)); }
+inline CountF fabs(CountF a) { return CountF(std::fabs(a.v)); }
+inline CountF fmin(CountF a, CountF b) { return a.v < b.v ? a : b; }
+inline CountF fmax(CountF a, CountF b) { return a.v < b.v ? b : a; }
+
+// Flops of one event of the recycled evaluation (all helicity combinations).
+extern "C" double me_host_flops(int k, const double* p, const double* coup, double mt, double wt) {
+  CountF::n = 0;
+  double out = 0.0;
+  if (k == 2) out = smatrix_one<2, CountF>(p, coup, mt, wt, nullptr);
+  else if (k == 3) out = smatrix_one<3, CountF>(p, coup, mt, wt, nullptr);
+  else if (k == 4) out = smatrix_one<4, CountF>(p, coup, mt, wt, nullptr);
+  (void)out;
+  return (double)CountF::n;
+}
+
 extern "C" int me_host_helicities(int k, const double* p, const double* coup, double mt, double wt, double* hel_out) {
   if (k == 2) smatrix_one<2, double>(p, coup, mt, wt, hel_out);
   else if (k == 3) smatrix_one<3, double>(p, coup, mt, wt, hel_out);
