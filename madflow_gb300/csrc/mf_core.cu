@@ -411,7 +411,7 @@ struct mf_process {
   double* d_partials = nullptr;
   size_t partial_cap = 0;
   int* d_zero_iter = nullptr;
-  double* d_ps = nullptr;   // [K+2][4][cap]
+  int4* d_prep = nullptr;   // [cap] per-event matrix-element records
   double* d_pref = nullptr; // [cap]
   double* d_me = nullptr;   // [cap]
   unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
@@ -421,6 +421,7 @@ struct mf_process {
 static const int kDiagrams[6] = {0, 0, 3, 16, 123, 1240};
 
 extern "C" {
+static int ensure_events(mf_process* p, int64_t N);
 
 const char* mf_version(void) { return "madflow_gb300 0.1 (sm_103a)"; }
 
@@ -466,7 +467,7 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_kmin) cudaFree(p->d_kmin);
   if (p->d_partials) cudaFree(p->d_partials);
   if (p->d_zero_iter) cudaFree(p->d_zero_iter);
-  if (p->d_ps) cudaFree(p->d_ps);
+  if (p->d_prep) cudaFree(p->d_prep);
   if (p->d_pref) cudaFree(p->d_pref);
   if (p->d_me) cudaFree(p->d_me);
   if (p->d_bins) cudaFree(p->d_bins);
@@ -500,7 +501,11 @@ int mf_smatrix(const mf_process* p, const double* ps, int64_t N, double mt, doub
                int64_t cstride, double* out, double* hel_out, void* stream) {
   if (!p || (N > 0 && (!ps || !coup || !out)) || N < 0 || (cstride != 0 && cstride != 1)) return MF_ERR_ARG;
   if (N == 0) return MF_OK;
-  int st = mf_launch_me(p->k, p->prec, ps, N, mt, wt, coup, cstride, nullptr, out, hel_out, S(stream));
+  mf_process* pm = const_cast<mf_process*>(p);
+  int st = ensure_events(pm, N);
+  if (st) return st;
+  if (mf_launch_prep(p->k, p->prec, ps, N, mt, wt, coup, cstride, pm->d_prep, S(stream))) return last_launch();
+  st = mf_launch_me(p->k, p->prec, pm->d_prep, N, nullptr, out, hel_out, S(stream));
   if (st == 3) return MF_ERR_UNSUPPORTED;
   return st ? last_launch() : MF_OK;
 }
@@ -670,14 +675,15 @@ static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, Ite
 
 static int ensure_events(mf_process* p, int64_t N) {
   if (p->event_cap >= N) return MF_OK;
-  cudaFree(p->d_ps);
+  cudaFree(p->d_prep);
   cudaFree(p->d_pref);
   cudaFree(p->d_me);
   cudaFree(p->d_bins);
-  p->d_ps = p->d_pref = p->d_me = nullptr;
+  p->d_prep = nullptr;
+  p->d_pref = p->d_me = nullptr;
   p->d_bins = nullptr;
   p->event_cap = 0;
-  int st = cuda_status(cudaMalloc(&p->d_ps, sizeof(double) * (size_t)(p->k + 2) * 4 * N));
+  int st = cuda_status(cudaMalloc(&p->d_prep, (size_t)mf_prep_bytes(p->k, p->prec) * N));
   if (!st) st = cuda_status(cudaMalloc(&p->d_pref, sizeof(double) * (size_t)N));
   if (!st) st = cuda_status(cudaMalloc(&p->d_me, sizeof(double) * (size_t)N));
   if (!st) st = cuda_status(cudaMalloc(&p->d_bins, (size_t)MF_MAX_DIM * N));
@@ -686,17 +692,13 @@ static int ensure_events(mf_process* p, int64_t N) {
   return MF_OK;
 }
 
-__global__ void set_couplings_kernel(double* c, cx<double> a, cx<double> b, cx<double> d) {
-  c[0] = a.re; c[1] = a.im; c[2] = b.re; c[3] = b.im; c[4] = d.re; c[5] = d.im;
-}
-
 // One pass of the pipeline over A.N events: Newton first pass, phase space,
 // |M|^2, accumulation.  results (optional) [2 + ndim*nb]; f_out (optional) [N].
 static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, double* results, double* f_out,
                      void* stream) {
   int st = ensure_events(p, A.N);
   if (st) return st;
-  A.ps = p->d_ps;
+  A.prep = p->d_prep;
   A.pref = p->d_pref;
   A.me = p->d_me;
   A.bins = A.x_in ? nullptr : p->d_bins;
@@ -709,9 +711,8 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
     if (accum_grid > A.N) accum_grid = (int)A.N;
   }
   int width = 2 + A.ndim * A.nb;
-  st = ensure_partials(p, (size_t)accum_grid * width + 6);
+  st = ensure_partials(p, (size_t)accum_grid * width);
   if (st) return st;
-  double* d_coup = p->d_partials + (size_t)accum_grid * width;
   if (!p->d_kmin) {
     st = cuda_status(cudaMalloc(&p->d_kmin, sizeof(int)));
     if (st) return st;
@@ -719,11 +720,9 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   A.newton_iters = p->d_kmin;
   bool per_event = c->newton_rule == MF_NEWTON_PER_EVENT;
   set_int_kernel<<<1, 1, 0, S(stream)>>>(p->d_kmin, per_event ? 0 : 11);
-  set_couplings_kernel<<<1, 1, 0, S(stream)>>>(d_coup, A.gc10, A.gc11, A.gc12);
   if (!per_event && mf_launch_newton(p->k, A, p->d_kmin, S(stream))) return last_launch();
-  if (mf_launch_ps(p->k, A, S(stream))) return last_launch();
-  if (mf_launch_me(p->k, p->prec, A.ps, A.N, A.mt, A.wt, d_coup, 0, A.pref, A.me, nullptr, S(stream)))
-    return last_launch();
+  if (mf_launch_ps(p->k, p->prec, A, S(stream))) return last_launch();
+  if (mf_launch_me(p->k, p->prec, A.prep, A.N, A.pref, A.me, nullptr, S(stream))) return last_launch();
   size_t shm = (size_t)(A.ndim * A.nb + 2 * 256) * sizeof(double);
   cudaFuncSetAttribute(accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   accum_kernel<<<accum_grid, 256, shm, S(stream)>>>(A.pref, A.me, A.bins, A.N, A.ndim, A.nb, A.inv_n, f_out,

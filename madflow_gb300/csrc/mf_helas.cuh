@@ -6,7 +6,8 @@
 #include "mf_common.cuh"
 
 template <class T> MF_D T tf_sign(T y) { return y > T(0) ? T(1) : (y < T(0) ? T(-1) : T(0)); }
-MF_D int floordiv2(double a) { return (int)floor(a * 0.5); }
+// floor(a / 2) of the small integers the helicity projectors take, in T
+template <class T> MF_D int floordiv2(T a) { return (int)floor(a * T(0.5)); }
 
 // _ox_massive_pp_zero (wavefunctions_flow.py:370-392)
 template <class T> MF_D void ox_massive_pp_zero(T fmass, T nsf, int ip, int im, W4<T>& f) {
@@ -25,7 +26,7 @@ template <class T> MF_D W4<T> ixxxxx(const T* p, T fmass, T nhel, T nsf) {
   T nh = nhel * nsf;
   if (fmass != T(0)) {
     T pp = fmin(p[0], sqrt(p[1] * p[1] + p[2] * p[2] + p[3] * p[3]));
-    int ip = floordiv2(1.0 + (double)nh), im = floordiv2(1.0 - (double)nh);
+    int ip = floordiv2<T>(T(1) + nh), im = floordiv2<T>(T(1) - nh);
     if (pp == T(0)) {
       ox_massive_pp_zero<T>(fmass, nsf, im, ip, f);
       return f;
@@ -65,8 +66,8 @@ template <class T> MF_D W4<T> oxxxxx(const T* p, T fmass, T nhel, T nsf) {
   if (fmass != T(0)) {
     T pp = fmin(p[0], sqrt(p[1] * p[1] + p[2] * p[2] + p[3] * p[3]));
     if (pp == T(0)) {
-      int ipz = (int)(-(double)floordiv2(1.0 - (double)nh) * (double)nhel);
-      int imz = (int)((double)floordiv2(1.0 + (double)nh) * (double)nhel);
+      int ipz = -floordiv2<T>(T(1) - nh) * (int)nhel;
+      int imz = floordiv2<T>(T(1) + nh) * (int)nhel;
       ox_massive_pp_zero<T>(fmass, nsf, ipz, imz, f);
       return f;
     }
@@ -74,7 +75,7 @@ template <class T> MF_D W4<T> oxxxxx(const T* p, T fmass, T nhel, T nsf) {
     T sf1 = (T(1) + nsf - (T(1) - nsf) * nh) * T(0.5);
     T sq = sqrt(p[0] + pp);
     T om[2] = {sq, fmass / sq};
-    int ip = floordiv2(1.0 + (double)nh), im = floordiv2(1.0 - (double)nh);
+    int ip = floordiv2<T>(T(1) + nh), im = floordiv2<T>(T(1) - nh);
     T sfo0 = sf0 * om[ip], sfo1 = sf1 * om[im];
     T pp3 = fmax(pp + p[3], T(0));
     cx<T> chi1;

@@ -7,9 +7,12 @@ struct IterArgs;
 #define MF_DECLARE_PROCESS(KK)                                                                              \
   void mf_host_tables_k##KK(int* nperm, int* ncomb, double* den, double* cden, const float** cn,             \
                             const signed char** hh);                                                        \
-  int mf_launch_me_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,    \
-                         int64_t cstride, const double* skip, double* out, double* hel_out, cudaStream_t st); \
-  int mf_launch_ps_k##KK(const IterArgs& A, cudaStream_t st);                                               \
+  int64_t mf_prep_bytes_k##KK(int prec);                                                                     \
+  int mf_launch_me_k##KK(int prec, const int4* prep, int64_t N, const double* skip, double* out,             \
+                         double* hel_out, cudaStream_t st);                                                 \
+  int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,  \
+                           int64_t cstride, int4* prep, cudaStream_t st);                                   \
+  int mf_launch_ps_k##KK(int prec, const IterArgs& A, cudaStream_t st);                                     \
   int mf_launch_newton_k##KK(const IterArgs& A, int* kmin, cudaStream_t st);
 MF_DECLARE_PROCESS(2)
 MF_DECLARE_PROCESS(3)
@@ -23,20 +26,36 @@ inline void mf_host_tables(int k, int* nperm, int* ncomb, double* den, double* c
     default: mf_host_tables_k4(nperm, ncomb, den, cden, cn, hh); break;
   }
 }
-inline int mf_launch_me(int k, int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,
-                        int64_t cstride, const double* skip, double* out, double* hel_out, cudaStream_t st) {
+inline int64_t mf_prep_bytes(int k, int prec) {
   switch (k) {
-    case 2: return mf_launch_me_k2(prec, ps, N, mt, wt, coup, cstride, skip, out, hel_out, st);
-    case 3: return mf_launch_me_k3(prec, ps, N, mt, wt, coup, cstride, skip, out, hel_out, st);
-    case 4: return mf_launch_me_k4(prec, ps, N, mt, wt, coup, cstride, skip, out, hel_out, st);
+    case 2: return mf_prep_bytes_k2(prec);
+    case 3: return mf_prep_bytes_k3(prec);
+    default: return mf_prep_bytes_k4(prec);
+  }
+}
+inline int mf_launch_me(int k, int prec, const int4* prep, int64_t N, const double* skip, double* out,
+                        double* hel_out, cudaStream_t st) {
+  switch (k) {
+    case 2: return mf_launch_me_k2(prec, prep, N, skip, out, hel_out, st);
+    case 3: return mf_launch_me_k3(prec, prep, N, skip, out, hel_out, st);
+    case 4: return mf_launch_me_k4(prec, prep, N, skip, out, hel_out, st);
   }
   return 3;
 }
-inline int mf_launch_ps(int k, const IterArgs& A, cudaStream_t st) {
+inline int mf_launch_prep(int k, int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,
+                          int64_t cstride, int4* prep, cudaStream_t st) {
   switch (k) {
-    case 2: return mf_launch_ps_k2(A, st);
-    case 3: return mf_launch_ps_k3(A, st);
-    case 4: return mf_launch_ps_k4(A, st);
+    case 2: return mf_launch_prep_k2(prec, ps, N, mt, wt, coup, cstride, prep, st);
+    case 3: return mf_launch_prep_k3(prec, ps, N, mt, wt, coup, cstride, prep, st);
+    case 4: return mf_launch_prep_k4(prec, ps, N, mt, wt, coup, cstride, prep, st);
+  }
+  return 3;
+}
+inline int mf_launch_ps(int k, int prec, const IterArgs& A, cudaStream_t st) {
+  switch (k) {
+    case 2: return mf_launch_ps_k2(prec, A, st);
+    case 3: return mf_launch_ps_k3(prec, A, st);
+    case 4: return mf_launch_ps_k4(prec, A, st);
   }
   return 3;
 }

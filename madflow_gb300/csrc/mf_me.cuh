@@ -38,7 +38,7 @@ struct IterArgs {
   const double* x_in;  // optional [ndim][N] points (integrand API): no Philox / VEGAS map, jac = 1
   float* u_out;        // optional [ndim][N] uniforms
   // pipeline buffers (scratch)
-  double* ps;              // [K+2][4][N]
+  int4* prep;              // [N] per-event records (PrepRec), passing events only
   double* pref;            // [N]
   unsigned char* bins;     // [ndim][N]
   double* me;              // [N]
@@ -145,9 +145,11 @@ __global__ void __launch_bounds__(256) newton_pass_kernel(IterArgs A, int* kmin)
   if ((threadIdx.x & 31) == 0) atomicMin(kmin, local);
 }
 
-// Phase space of every event of the iteration (one thread per event).
-template <int K> __global__ void __launch_bounds__(128) ps_iter_kernel(IterArgs A) {
+// Phase space of every event of the iteration (one thread per event), and
+// the per-event record of the matrix element for the events that pass.
+template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(IterArgs A) {
   constexpr int NPART = K + 2;
+  constexpr int NW = prep_words<T, K>();
   const int it = *A.iteration;
   // the batch rule runs at most 10 iterations (11 = no event converged)
   const int niter = min(*A.newton_iters, 10);
@@ -156,8 +158,13 @@ template <int K> __global__ void __launch_bounds__(128) ps_iter_kernel(IterArgs 
     event_point(A, e, it, x, jac, true);
     bool ok = event_phase_space(A, NPART, x, niter, p, wl);
     A.pref[e] = ok ? jac * wl : 0.0;
-    for (int i = 0; i < NPART; ++i)
-      for (int c = 0; c < 4; ++c) A.ps[((int64_t)i * 4 + c) * A.N + e] = p[i][c];
+    if (ok) {
+      PrepRec<T, K> r;
+      prep_event<T, K>(r, p, A.mt, A.wt, A.gc10, A.gc11, A.gc12);
+      const int4* src = reinterpret_cast<const int4*>(&r);
+      int4* dst = A.prep + e * NW;
+      for (int w = 0; w < NW; ++w) dst[w] = src[w];
+    }
   }
 }
 

@@ -85,22 +85,46 @@ MF_D int bit_reverse(int hp, int len) {
   return r;
 }
 
-// stage 0: external wavefunctions (the gluons go to their length-1 J slots)
-template <class T, int K> MF_D void rec_st_ext(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid, int nt) {
+// Per-event data of the evaluation, built by one thread per event (in the
+// phase-space kernel of an iteration, or prep_kernel for mf_smatrix) and
+// loaded by the event's block: subset momenta and propagators, the external
+// wavefunctions for both helicities, and the |M|^2 scale factor.
+template <class T, int K> struct alignas(16) PrepRec {
+  EvData<T, K> ev;
+  W4<T> G[K][2];
+  W4<T> WT[2], WTB[2];
+  double scale;  // |GC_11|^2 / (colour denominator x average)
+};
+
+template <class T, int K>
+MF_D void prep_event(PrepRec<T, K>& r, const double (*p)[4], double mt, double wt, cx<double> c10, cx<double> c11,
+                     cx<double> c12) {
   using R = RecTraits<K>;
+  for (int s = 0; s < (1 << K); ++s) evdata_subset<T, K>(r.ev, s, p, mt, wt, c10, c11, c12);
+  for (int i = 0; i < K + 2; ++i)
+    for (int c = 0; c < 4; ++c) r.ev.pext[i][c] = (T)p[i][c];
+  r.ev.mt = (T)mt;
   const T sqh = (T)0.70710676908493042;  // madflow's float32-rounded sqrt(1/2)
+  for (int q = 0; q < K; ++q) {
+    int part = gluon_particle<K>(q);
+    for (int b = 0; b < 2; ++b)
+      r.G[q][b] = vxxxxx<T>(r.ev.pext[part], T(0), b ? T(1) : T(-1), part < 2 ? T(-1) : T(1), sqh);
+  }
+  for (int b = 0; b < 2; ++b) {
+    r.WT[b] = oxxxxx<T>(r.ev.pext[2], r.ev.mt, b ? T(1) : T(-1), T(1));
+    r.WTB[b] = ixxxxx<T>(r.ev.pext[3], r.ev.mt, b ? T(1) : T(-1), T(-1));
+  }
+  r.scale = (c11.re * c11.re + c11.im * c11.im) / (R::COLOUR_DEN * R::DENOMINATOR);
+}
+
+// stage 0: the external wavefunctions go to their slots (gluons: the
+// length-1 J entries)
+template <class T, int K> MF_D void rec_st_ext(RecWS<T, K>& ws, const PrepRec<T, K>& pr, int tid, int nt) {
+  using R = RecTraits<K>;
   for (int i = tid; i < 2 * K + 4; i += nt) {
-    if (i < 2 * K) {
-      int q = i >> 1, b = i & 1;
-      int part = gluon_particle<K>(q);
-      ws.J.put(R::jo_ext(q) + b, vxxxxx<T>(ev.pext[part], T(0), b ? T(1) : T(-1), part < 2 ? T(-1) : T(1), sqh));
-    } else if (i < 2 * K + 2) {
-      int b = i - 2 * K;
-      ws.WT[b] = oxxxxx<T>(ev.pext[2], ev.mt, b ? T(1) : T(-1), T(1));
-    } else {
-      int b = i - 2 * K - 2;
-      ws.WTB[b] = ixxxxx<T>(ev.pext[3], ev.mt, b ? T(1) : T(-1), T(-1));
-    }
+    if (i < 2 * K) ws.J.put(R::jo_ext(i >> 1) + (i & 1), pr.G[i >> 1][i & 1]);
+    else if (i < 2 * K + 2) ws.WT[i - 2 * K] = pr.WT[i - 2 * K];
+    else ws.WTB[i - 2 * K - 2] = pr.WTB[i - 2 * K - 2];
   }
 }
 
@@ -252,10 +276,10 @@ template <class T, int K> MF_D double rec_colour_one(const RecWS<T, K>& ws, cons
 
 // the whole evaluation of one event by nt "threads" run one at a time (host tests)
 template <class T, int K> struct RecHostRun {
-  static double run(RecWS<T, K>& ws, const EvData<T, K>& ev, const T* cm, int nt) {
-    for (int t = 0; t < nt; ++t) rec_st_ext<T, K>(ws, ev, t, nt);
+  static double run(RecWS<T, K>& ws, const PrepRec<T, K>& pr, const T* cm, int nt) {
+    for (int t = 0; t < nt; ++t) rec_st_ext<T, K>(ws, pr, t, nt);
     for (int st = 1; st < K; ++st)
-      for (int t = 0; t < nt; ++t) rec_stage<T, K>(ws, ev, st, t, nt);
+      for (int t = 0; t < nt; ++t) rec_stage<T, K>(ws, pr.ev, st, t, nt);
     for (int t = 0; t < nt; ++t) rec_st_A<T, K>(ws, t, nt);
     double tot = 0.0;
     for (int t = 0; t < nt; ++t) tot += rec_st_colour<T, K>(ws, cm, t, nt);
@@ -267,45 +291,59 @@ constexpr int MF_REC_NT = 128;  // threads per event block
 
 template <class T, int K> struct RecSmem {
   RecWS<T, K> ws;
-  EvData<T, K> ev;
+  PrepRec<T, K> pr;
   T cm[RecTraits<K>::NPERM * RecTraits<K>::NPERM];
-  double pd[K + 2][4];
   double red[MF_REC_NT / 32];
 };
+template <class T, int K> MF_HD constexpr int prep_words() { return (int)(sizeof(PrepRec<T, K>) / 16); }
 
 #ifdef __CUDACC__
-// Block-per-event |M|^2: ps [K+2][4][N]; couplings [N or 1][3] complex;
+// Per-event records from momenta ps [K+2][4][N] and couplings [N or 1][3]
+// complex (one thread per event).
+template <int K, class T>
+__global__ void __launch_bounds__(128) prep_kernel(const double* __restrict__ ps, int64_t N, double mt, double wt,
+                                                   const double* __restrict__ coup, int64_t cstride,
+                                                   int4* __restrict__ prep) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double p[K + 2][4];
+    for (int i = 0; i < K + 2; ++i)
+      for (int c = 0; c < 4; ++c) p[i][c] = ps[((int64_t)i * 4 + c) * N + e];
+    const double* cp = coup + 6 * cstride * e;
+    PrepRec<T, K> r;
+    prep_event<T, K>(r, p, mt, wt, {cp[0], cp[1]}, {cp[2], cp[3]}, {cp[4], cp[5]});
+    const int4* src = reinterpret_cast<const int4*>(&r);
+    int4* dst = prep + (int64_t)e * prep_words<T, K>();
+    for (int w = 0; w < prep_words<T, K>(); ++w) dst[w] = src[w];
+  }
+}
+
+// Block-per-event |M|^2 from the per-event records prep [N][prep_words];
 // skip (optional) [N]: events with skip[e] == 0 get out[e] = 0 without work;
 // out [N]; hel_out (optional) [ncomb][N] in MadGraph helicity order.
 template <int K, class T>
-__global__ void __launch_bounds__(MF_REC_NT) me_rec_kernel(const double* __restrict__ ps, int64_t N, double mt,
-                                                          double wt, const double* __restrict__ coup,
-                                                          int64_t cstride, const double* __restrict__ skip,
-                                                          double* __restrict__ out, double* __restrict__ hel_out) {
+__global__ void __launch_bounds__(MF_REC_NT) me_rec_kernel(const int4* __restrict__ prep, int64_t N,
+                                                          const double* __restrict__ skip, double* __restrict__ out,
+                                                          double* __restrict__ hel_out) {
   using R = RecTraits<K>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   RecSmem<T, K>& S = *reinterpret_cast<RecSmem<T, K>*>(smem_raw);
   const int tid = threadIdx.x, nt = blockDim.x;
+  constexpr int NW = prep_words<T, K>();
   for (int i = tid; i < R::NPERM * R::NPERM; i += nt) S.cm[i] = (T)R::colour(i);
-  const double scale_c = 1.0 / (R::COLOUR_DEN * R::DENOMINATOR);
   for (int64_t e = blockIdx.x; e < N; e += gridDim.x) {
     if (skip && skip[e] == 0.0) {
       if (tid == 0) out[e] = 0.0;
       continue;
     }
     __syncthreads();
-    for (int i = tid; i < 4 * (K + 2); i += nt) S.pd[i / 4][i % 4] = ps[(int64_t)i * N + e];
-    const double* cp = coup + 6 * cstride * e;
-    cx<double> c10 = {cp[0], cp[1]}, c11 = {cp[2], cp[3]}, c12 = {cp[4], cp[5]};
+    int4* dst = reinterpret_cast<int4*>(&S.pr);
+    const int4* src = prep + e * NW;
+    for (int w = tid; w < NW; w += nt) dst[w] = src[w];
     __syncthreads();
-    for (int s = tid; s < (1 << K); s += nt) evdata_subset<T, K>(S.ev, s, S.pd, mt, wt, c10, c11, c12);
-    for (int i = tid; i < 4 * (K + 2); i += nt) S.ev.pext[i / 4][i % 4] = (T)S.pd[i / 4][i % 4];
-    if (tid == 0) S.ev.mt = (T)mt;
-    __syncthreads();
-    rec_st_ext<T, K>(S.ws, S.ev, tid, nt);
+    rec_st_ext<T, K>(S.ws, S.pr, tid, nt);
     __syncthreads();
     for (int st = 1; st < K; ++st) {
-      rec_stage<T, K>(S.ws, S.ev, st, tid, nt);
+      rec_stage<T, K>(S.ws, S.pr.ev, st, tid, nt);
       __syncthreads();
     }
     rec_st_A<T, K>(S.ws, tid, nt);
@@ -313,7 +351,7 @@ __global__ void __launch_bounds__(MF_REC_NT) me_rec_kernel(const double* __restr
     double part = rec_st_colour<T, K>(S.ws, S.cm, tid, nt);
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((tid & 31) == 0) S.red[tid >> 5] = part;
-    const double sc = (c11.re * c11.re + c11.im * c11.im) * scale_c;
+    const double sc = S.pr.scale;
     if (hel_out)
       for (int c = tid; c < (1 << (K + 2)); c += nt)
         hel_out[(int64_t)R::cfg_to_mg(c) * N + e] = rec_colour_one<T, K>(S.ws, S.cm, c) * sc * R::DENOMINATOR;

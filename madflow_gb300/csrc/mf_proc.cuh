@@ -24,9 +24,8 @@ static int sm_count() {
     *cn = ttng##KK::colour_num_h;                                                                              \
     *hh = &ttng##KK::hel_h[0][0];                                                                              \
   }                                                                                                            \
-  template <class T> static int me_rec_launch_k##KK(const double* ps, int64_t N, double mt, double wt,        \
-                                                    const double* coup, int64_t cstride, const double* skip,  \
-                                                    double* out, double* hel_out, cudaStream_t st) {          \
+  template <class T> static int me_rec_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out,  \
+                                                    double* hel_out, cudaStream_t st) {                           \
     const void* fn = (const void*)me_rec_kernel<KK, T>;                                                        \
     int bytes = rec_smem_bytes<KK, T>();                                                                       \
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                              \
@@ -36,19 +35,33 @@ static int sm_count() {
     int64_t g = (int64_t)sm_count() * per * 8;                                                                 \
     if (g > N) g = N;                                                                                          \
     if (g < 1) g = 1;                                                                                          \
-    me_rec_kernel<KK, T><<<(int)g, MF_REC_NT, bytes, st>>>(ps, N, mt, wt, coup, cstride, skip, out, hel_out);  \
+    me_rec_kernel<KK, T><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out);                       \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }                                                                                                            \
-  int mf_launch_me_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,      \
-                         int64_t cstride, const double* skip, double* out, double* hel_out, cudaStream_t st) { \
-    return prec == 0 ? me_rec_launch_k##KK<double>(ps, N, mt, wt, coup, cstride, skip, out, hel_out, st)      \
-                     : me_rec_launch_k##KK<float>(ps, N, mt, wt, coup, cstride, skip, out, hel_out, st);      \
+  int64_t mf_prep_bytes_k##KK(int prec) {                                                                      \
+    return prec == 0 ? (int64_t)sizeof(PrepRec<double, KK>) : (int64_t)sizeof(PrepRec<float, KK>);           \
   }                                                                                                            \
-  int mf_launch_ps_k##KK(const IterArgs& A, cudaStream_t st) {                                                 \
+  int mf_launch_me_k##KK(int prec, const int4* prep, int64_t N, const double* skip, double* out,               \
+                         double* hel_out, cudaStream_t st) {                                                   \
+    return prec == 0 ? me_rec_launch_k##KK<double>(prep, N, skip, out, hel_out, st)                           \
+                     : me_rec_launch_k##KK<float>(prep, N, skip, out, hel_out, st);                           \
+  }                                                                                                            \
+  int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,    \
+                           int64_t cstride, int4* prep, cudaStream_t st) {                                     \
+    int64_t b = (N + 127) / 128, cap = (int64_t)sm_count() * 16;                                               \
+    if (b > cap) b = cap;                                                                                      \
+    if (b < 1) b = 1;                                                                                          \
+    if (prec == 0) prep_kernel<KK, double><<<(int)b, 128, 0, st>>>(ps, N, mt, wt, coup, cstride, prep);       \
+    else prep_kernel<KK, float><<<(int)b, 128, 0, st>>>(ps, N, mt, wt, coup, cstride, prep);                  \
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
+  }                                                                                                            \
+  int mf_launch_ps_k##KK(int prec, const IterArgs& A, cudaStream_t st) {                                       \
     int64_t b = (A.N + 127) / 128;                                                                             \
     int64_t cap = (int64_t)sm_count() * 16;                                                                    \
     if (b > cap) b = cap;                                                                                      \
-    ps_iter_kernel<KK><<<(int)(b < 1 ? 1 : b), 128, 0, st>>>(A);                                               \
+    if (b < 1) b = 1;                                                                                          \
+    if (prec == 0) ps_iter_kernel<KK, double><<<(int)b, 128, 0, st>>>(A);                                      \
+    else ps_iter_kernel<KK, float><<<(int)b, 128, 0, st>>>(A);                                                 \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }                                                                                                            \
   int mf_launch_newton_k##KK(const IterArgs& A, int* kmin, cudaStream_t st) {                                  \

@@ -20,19 +20,16 @@ template <int K, class T>
 static double smatrix_one(const double* p, const double* coup, double mt, double wt, double* hel_out) {
   using R = RecTraits<K>;
   auto ws = std::make_unique<RecWS<T, K>>();
-  auto ev = std::make_unique<EvData<T, K>>();
+  auto pr = std::make_unique<PrepRec<T, K>>();
   double pd[K + 2][4];
   std::memcpy(pd, p, sizeof(pd));
   cx<double> c10 = {coup[0], coup[1]}, c11 = {coup[2], coup[3]}, c12 = {coup[4], coup[5]};
-  for (int s = 0; s < (1 << K); ++s) evdata_subset<T, K>(*ev, s, pd, mt, wt, c10, c11, c12);
-  for (int i = 0; i < K + 2; ++i)
-    for (int c = 0; c < 4; ++c) ev->pext[i][c] = (T)pd[i][c];
-  ev->mt = (T)mt;
+  prep_event<T, K>(*pr, pd, mt, wt, c10, c11, c12);
   const int nt = 7;  // an odd "block size" exercises the item striding
   T cm[R::NPERM * R::NPERM];
   for (int i = 0; i < R::NPERM * R::NPERM; ++i) cm[i] = (T)R::colour(i);
-  double tot = RecHostRun<T, K>::run(*ws, *ev, cm, nt);
-  double sc = (c11.re * c11.re + c11.im * c11.im) / (R::COLOUR_DEN * R::DENOMINATOR);
+  double tot = RecHostRun<T, K>::run(*ws, *pr, cm, nt);
+  double sc = pr->scale;
   if (hel_out)
     for (int c = 0; c < (1 << (K + 2)); ++c)
       hel_out[R::cfg_to_mg(c)] = rec_colour_one<T, K>(*ws, cm, c) * sc * R::DENOMINATOR;
@@ -61,6 +58,7 @@ struct CountF {
   CountF() : v(0) {}
   template <class A> CountF(A x) : v((double)x) {}
   explicit operator double() const { return v; }
+  explicit operator int() const { return (int)v; }
 };
 inline CountF operator+(CountF a, CountF b) { ++CountF::n; return CountF(a.v + b.v); }
 inline CountF operator-(CountF a, CountF b) { ++CountF::n; return CountF(a.v - b.v); }
@@ -76,6 +74,7 @@ inline CountF sqrt(CountF a) { ++CountF::n; return CountF(std::sqrt(a.v)); }
 inline CountF fabs(CountF a) { return CountF(std::fabs(a.v)); }
 inline CountF fmin(CountF a, CountF b) { return a.v < b.v ? a : b; }
 inline CountF fmax(CountF a, CountF b) { return a.v < b.v ? b : a; }
+inline CountF floor(CountF a) { return CountF(std::floor(a.v)); }
 
 // Flops of one event of the recycled evaluation (all helicity combinations).
 extern "C" double me_host_flops(int k, const double* p, const double* coup, double mt, double wt) {
