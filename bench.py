@@ -33,6 +33,10 @@ CUTS = dict(ptmin=60.0, etamax=2.5, drmin=0.4)
 # div/sqrt/log 1), counted by the oracle's counting scalar
 # (tests/test_flop_counts.py keeps these in step with it).
 ALG_FLOPS = {2: 23601.0, 3: 356161.0, 4: 5744961.0}
+# Flops per phase-space point the helicity-recycling kernel executes (same
+# counting convention), counted by running its stage functions with the
+# counting scalar (tests/test_flop_counts.py).
+REC_FLOPS = {2: 5817.0, 3: 58190.0, 4: 745707.0}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max clock
 
 
@@ -109,12 +113,18 @@ def load_peaks():
         return {}
 
 
+def make_integrand(prec):
+    from madflow_gb300.vegas import FusedIntegrand
+
+    return FusedIntegrand(4, kind=1, sqrts=SQRTS, mt=MT, wt=WT, alpha_s=ALPHA_S, precision=prec, **CUTS)
+
+
 def run_gpu(args):
     import numpy as np
     import torch
 
     from madflow_gb300 import _lib
-    from madflow_gb300.vegas import FusedIntegrand, VegasFlow
+    from madflow_gb300.vegas import VegasFlow
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -126,14 +136,14 @@ def run_gpu(args):
 
         dist.init_process_group("nccl")
     prec = _lib.MF_PREC_MIXED if args.precision == "mixed" else _lib.MF_PREC_FP64
-    integ = FusedIntegrand(4, kind=1, sqrts=SQRTS, mt=MT, wt=WT, alpha_s=ALPHA_S, precision=prec, **CUTS)
+    integ = make_integrand(prec)
     N = args.events
     # replicas: each rank integrates its own Philox stream (stream id = rank)
     vegas = VegasFlow(integ.n_dim, N, seed=args.seed, stream_id=rank, use_graph=True)
     vegas.compile(integ)
     f_out = torch.empty(N, dtype=torch.float64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
-    npass = torch.zeros((), dtype=torch.int64, device="cuda")
+    npass = torch.zeros(args.steps, dtype=torch.int64, device="cuda")
 
     def step():
         integ.iteration(vegas.grid, vegas.seed, vegas.stream_id, vegas.iteration, N, vegas.results, f_out=f_out)
@@ -148,7 +158,9 @@ def run_gpu(args):
         dist.barrier()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    # also time the dominant kernel alone: the fused iteration (events on the same stream)
+    # the pipeline records events between its stages (same stream), read after each step
+    integ.set_timing(True)
+    stage_ms = []
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -157,34 +169,30 @@ def run_gpu(args):
             starts[i].record()
             step()
             ends[i].record()
-            npass += torch.count_nonzero(f_out)
+            npass[i] = torch.count_nonzero(f_out)
+            ends[i].synchronize()
+            stage_ms.append(integ.stage_ms())
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+    integ.set_timing(False)
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     step_s = sum(ms) / 1000.0
+    n_me_rank = npass.sum()
     if dist:
         t = torch.tensor([step_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         step_s = float(t.item())
-        c = npass.clone()
-        dist.all_reduce(c)
-        npass = c
-    n_me = int(npass.item())
+        dist.all_reduce(n_me_rank)
+    n_me = int(n_me_rank.item())
     pass_frac = n_me / (N * args.steps * world)
     me_per_s = n_me / step_s
 
-    # dominant kernel alone (fused iteration), timed with events on its stream
-    kt0, kt1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    kms = []
-    for _ in range(2):
-        flush.zero_()
-        kt0.record()
-        integ.iteration(vegas.grid, vegas.seed, vegas.stream_id, vegas.iteration, N, vegas.results)
-        kt1.record()
-        torch.cuda.synchronize()
-        kms.append(kt0.elapsed_time(kt1))
-    k_s = min(kms) / 1000.0
-    achieved = ALG_FLOPS[4] * N * pass_frac / k_s / 1e12
+    # dominant kernel: the block-per-event matrix element (me_rec_kernel<4,float>);
+    # flops per launch = recycled flops per event x the events passing the cuts
+    me_ms = [d["matrix_element"] for d in stage_ms]
+    per_launch = [REC_FLOPS[4] * int(n) for n in npass.tolist()]
+    achieved = sum(per_launch) / (sum(me_ms) / 1000.0) / 1e12
+    stages = {k: statistics.mean(d[k] for d in stage_ms) for k in stage_ms[0]}
 
     # end to end: the integrand contract f(x) with host buffers, copies timed
     e2e_n = min(N, args.e2e_events)
@@ -192,7 +200,6 @@ def run_gpu(args):
     x_host = torch.from_numpy(rng.uniform(size=(e2e_n, integ.n_dim))).pin_memory()
     f_host = torch.empty(e2e_n, dtype=torch.float64).pin_memory()
     x_dev = torch.empty((e2e_n, integ.n_dim), dtype=torch.float64, device="cuda")
-    f_host_nz = 0
     for _ in range(1):  # warm-up
         x_dev.copy_(x_host, non_blocking=True)
         f_host.copy_(integ(x_dev), non_blocking=True)
@@ -209,7 +216,6 @@ def run_gpu(args):
     e2e_s = e0.elapsed_time(e1) / 1000.0
     e2e_rate = f_host_nz * reps / e2e_s
 
-    peaks = load_peaks()
     out = {
         "metric": METRIC,
         "value": me_per_s,
@@ -228,45 +234,95 @@ def run_gpu(args):
         "pass_fraction": pass_frac,
         "phase_space_points_per_s": N * args.steps * world / step_s,
         "wall_s": wall,
-        "gpu_launches": 5 * args.steps,
+        # per step: set-int, newton pass, phase space, matrix element, accumulate, reduce, refine
+        "gpu_launches": 7 * args.steps,
+        "stage_ms": stages,
         "e2e": {"value": e2e_rate, "unit": "|M|^2 evals/s", "h2d_bytes_per_step": int(x_host.numel() * 8),
-                "d2h_bytes_per_step": int(f_host.numel() * 8), "api": "FusedIntegrand(x) -> f, host buffers"},
+                "d2h_bytes_per_step": int(f_host.numel() * 8), "api": "FusedIntegrand(x) -> f, host buffers",
+                "events_per_step": e2e_n},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
                      "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": None,
-                     "kernel": "iteration_kernel<4,float>",
+                     "kernel": "me_rec_kernel<4,float>",
                      "peak_source": "nominal FP32 SIMT (152 SMs x 128 lanes x 2 x 2.07 GHz); "
                                     "MEASURED_PEAKS.json holds no FP32 figure",
-                     "alg_flops_per_event": ALG_FLOPS[4], "kernel_ms": k_s * 1000.0},
+                     "flops_per_event": REC_FLOPS[4],
+                     "alg_flops_per_event": ALG_FLOPS[4],
+                     "alg_equivalent_tflops": achieved * ALG_FLOPS[4] / REC_FLOPS[4],
+                     "kernel_ms": statistics.mean(me_ms)},
         "clocks": clk.summary(),
     }
-    if args.time_to_target:
-        out["time_to_1e-3"] = time_to_target(args, integ, prec)
+    if args.time_to_target and rank == 0:
+        out["time_to_1e-3"] = time_to_target(args)
     if args.cpu_baseline and rank == 0:
         out["cpu_baseline"] = cpu_baseline(args)
+        ttt = out.get("time_to_1e-3")
+        if ttt and ttt.get("vegas_fp64", {}).get("events"):
+            ev = ttt["vegas_fp64"]["events"] * ttt["vegas_fp64"]["pass_fraction"]
+            out["cpu_baseline"]["projected_seconds_to_1e-3"] = ev / out["cpu_baseline"]["value"]
     if rank == 0:
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
 
 
-def time_to_target(args, integ, prec, target=1e-3):
-    """Wall-clock seconds of VEGAS iterations until the combined relative
-    error reaches the target (grid adapted from scratch)."""
+def _vegas_to_target(prec, n_events, seed, max_iter, target):
     import torch
 
     from madflow_gb300.vegas import VegasFlow
 
-    v = VegasFlow(integ.n_dim, args.target_events, seed=args.seed + 1, use_graph=True)
+    integ = make_integrand(prec)
+    v = VegasFlow(integ.n_dim, n_events, seed=seed, use_graph=True)
     v.compile(integ)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res, err = v.run_integration(args.max_iter, target_rel_error=target)
+    res, err = v.run_integration(max_iter, target_rel_error=target)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    return {"seconds": dt, "iterations": len(v.last_run), "events_per_iteration": args.target_events,
+    it = len(v.last_run)
+    return {"seconds": dt, "iterations": it, "events_per_iteration": n_events, "events": it * n_events,
             "result_pb": res, "error_pb": err, "rel_error": err / abs(res) if res else None,
-            "reached": bool(res and err / abs(res) <= target), "method": "VEGAS",
-            "precision": "mixed" if prec == 1 else "fp64"}
+            "reached": bool(res and err / abs(res) <= target)}
+
+
+def time_to_target(args, target=1e-3):
+    """Wall-clock seconds until the combined relative error of the integral
+    reaches the target, from a fresh start (uniform grid / untrained flow):
+    plain VEGAS in FP64 (the reference's arithmetic), VEGAS in mixed
+    precision, and the normalizing-flow sampler (training included) in mixed
+    precision.  Every iteration or training batch is an unbiased estimate
+    from a frozen proposal; all of them are combined with inverse-variance
+    weights, as VEGAS combines its iterations."""
+    import torch
+
+    from madflow_gb300 import _lib
+    from madflow_gb300.flow import NormalizingFlow, adaptive_flow_integration
+
+    out = {"target_rel_error": target}
+    out["vegas_fp64"] = _vegas_to_target(_lib.MF_PREC_FP64, args.target_events, args.seed + 1, args.max_iter, target)
+    out["vegas_mixed"] = _vegas_to_target(_lib.MF_PREC_MIXED, args.target_events, args.seed + 1, args.max_iter,
+                                          target)
+    integ = make_integrand(_lib.MF_PREC_MIXED)
+    # pass fraction of the workload (for the CPU projection)
+    x = torch.rand((200_000, integ.n_dim), dtype=torch.float64, device="cuda",
+                   generator=torch.Generator(device="cuda").manual_seed(7))
+    out["vegas_fp64"]["pass_fraction"] = float((integ(x) != 0).double().mean())
+    flow = NormalizingFlow(integ.n_dim, n_layers=args.flow_layers, bins=16, hidden=args.flow_hidden, n_hidden=2,
+                           seed=0, bf16=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res, err, info = adaptive_flow_integration(flow, integ, target_rel_error=target, batch_size=args.flow_batch,
+                                               max_batches=args.max_iter * 4, lr=args.flow_lr,
+                                               train_batches=args.flow_train_batches)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    out["flow_mixed"] = {"seconds": dt, "batches": info["batches"], "trained_batches": info["trained"],
+                         "events_per_batch": args.flow_batch, "events": info["batches"] * args.flow_batch,
+                         "result_pb": res, "error_pb": err, "rel_error": err / abs(res) if res else None,
+                         "reached": bool(res and err / abs(res) <= target),
+                         "flow": f"{args.flow_layers} piecewise-quadratic coupling layers, 16 bins, "
+                                 f"MLP 2x{args.flow_hidden} (bf16 cuBLAS), lr {args.flow_lr}",
+                         "last_std_over_mean": info["last_rel_std"]}
+    return out
 
 
 def cpu_baseline(args, sample=None):
@@ -283,29 +339,41 @@ def cpu_baseline(args, sample=None):
     rng = np.random.default_rng(args.seed)
     x = rng.uniform(size=(n, 18))
     cfg = [1, 4, SQRTS, MT, WT, ALPHA_S, CUTS["ptmin"], CUTS["etamax"], CUTS["drmin"], 0]
-    oracle.integrand(cfg, x[: min(64, n)], plan)  # warm-up
+    oracle.integrand(cfg, x[: min(256, n)], plan)  # warm-up
     t0 = time.perf_counter()
     f = oracle.integrand(cfg, x, plan)
     dt = time.perf_counter() - t0
     n_me = int((f != 0).sum())
     return {"value": n_me / dt, "unit": "|M|^2 evals/s", "cores": oracle.num_threads(), "kind": "port",
             "sample": f"{n} phase-space points of the same workload ({n_me} pass the cuts), {dt:.1f} s",
-            "seconds": dt}
+            "seconds": dt, "events": n_me}
 
 
 def run_reference(args):
+    """The reference arm: madflow's CPU path (its FP64 algorithm restated in
+    C++/OpenMP, all host cores), W warm-up and K timed steps, each step a
+    bounded sample of the same workload."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    cb = cpu_baseline(args, args.cpu_events)
+    for _ in range(args.warmup):
+        cpu_baseline(args, 2000)
+    steps = [cpu_baseline(args, args.ref_events) for _ in range(args.steps)]
+    secs = sum(s["seconds"] for s in steps)
+    n_me = sum(s["events"] for s in steps)
+    value = n_me / secs
+    cb = dict(steps[0])
+    cb.update(value=value, seconds=secs,
+              sample=f"{args.steps} steps x {args.ref_events} phase-space points of the same workload "
+                     f"({n_me} pass the cuts), {secs:.1f} s")
     out = {
         "metric": METRIC,
-        "value": cb["value"],
+        "value": value,
         "unit": cb["unit"],
         "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": 1000.0 * cb["seconds"],
+        "ms_per_step": 1000.0 * secs / args.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -314,7 +382,7 @@ def run_reference(args):
         "config": workload(args.events),
         "impl": "reference",
         "cpu_baseline": cb,
-        "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": value, "unit": cb["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
 
@@ -324,17 +392,23 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--events", type=int, default=2_000_000)
+    ap.add_argument("--events", type=int, default=10_000_000)
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--seed", type=int, default=4)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--cpu-events", type=int, default=4000)
+    ap.add_argument("--cpu-events", type=int, default=200_000)
+    ap.add_argument("--ref-events", type=int, default=40_000)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--time-to-target", action="store_true")
-    ap.add_argument("--target-events", type=int, default=1_000_000)
-    ap.add_argument("--max-iter", type=int, default=30)
-    ap.add_argument("--e2e-events", type=int, default=1_000_000)
-    ap.add_argument("--e2e-reps", type=int, default=2)
+    ap.add_argument("--no-time-to-target", dest="time_to_target", action="store_false")
+    ap.add_argument("--target-events", type=int, default=4_000_000)
+    ap.add_argument("--max-iter", type=int, default=40)
+    ap.add_argument("--flow-layers", type=int, default=8)
+    ap.add_argument("--flow-hidden", type=int, default=128)
+    ap.add_argument("--flow-batch", type=int, default=1_000_000)
+    ap.add_argument("--flow-lr", type=float, default=2e-3)
+    ap.add_argument("--flow-train-batches", type=int, default=30)
+    ap.add_argument("--e2e-events", type=int, default=4_000_000)
+    ap.add_argument("--e2e-reps", type=int, default=3)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -31,7 +31,8 @@ typedef enum {
   MF_ERR_CUDA = 2,        /* a CUDA call failed; see mf_last_cuda_error() */
   MF_ERR_UNSUPPORTED = 3, /* process / precision not built */
   MF_ERR_CAPACITY = 4,    /* request exceeds a documented maximum */
-  MF_ERR_NONFINITE = 5    /* non-finite weights were produced (counted and zeroed) */
+  MF_ERR_NONFINITE = 5,   /* non-finite weights were produced (counted and zeroed) */
+  MF_ERR_STATE = 6        /* the requested result does not exist yet */
 } mf_status;
 
 typedef enum { MF_PREC_FP64 = 0, MF_PREC_MIXED = 1 } mf_precision;
@@ -145,6 +146,18 @@ int mf_integrand(const mf_process* proc, const mf_integrand_config* cfg, const d
 int mf_vegas_iteration(const mf_process* proc, const mf_integrand_config* cfg, const double* grid, int nbins,
                        uint64_t seed, uint32_t stream_id, const int* iteration, int64_t n_events, double* results,
                        double* f_out, float* u_out, void* stream);
+
+/* Stage timing of the fused pipeline behind mf_integrand / mf_vegas_iteration
+ * (no counterpart in the reference).  With timing enabled, each call records
+ * CUDA events on its stream between its stages; mf_process_stage_ms then
+ * gives, once the caller has synchronised that stream, the milliseconds of the
+ * last call's MF_STAGES stages: [0] batch Newton pass, [1] phase space + cuts
+ * + PDF + matrix-element records, [2] matrix element, [3] accumulation.
+ * Calls made while their stream is being captured into a CUDA graph record
+ * nothing (MF_ERR_STATE until an uncaptured call has run). */
+#define MF_STAGES 4
+int mf_process_set_timing(mf_process* proc, int enable);
+int mf_process_stage_ms(const mf_process* proc, float* ms);
 
 /* VEGAS accumulation for an integrand evaluated by the caller: f [N], jac
  * [N], bins [ndim][N] (from mf_vegas_sample); results (device)

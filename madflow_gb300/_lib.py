@@ -17,7 +17,8 @@ c_int, c_int64, c_uint32, c_uint64, c_double = ctypes.c_int, ctypes.c_int64, cty
 c_void_p, c_char_p = ctypes.c_void_p, ctypes.c_char_p
 c_dp = ctypes.c_void_p  # device pointers are passed as integers
 
-MF_OK, MF_ERR_ARG, MF_ERR_CUDA, MF_ERR_UNSUPPORTED, MF_ERR_CAPACITY, MF_ERR_NONFINITE = range(6)
+MF_OK, MF_ERR_ARG, MF_ERR_CUDA, MF_ERR_UNSUPPORTED, MF_ERR_CAPACITY, MF_ERR_NONFINITE, MF_ERR_STATE = range(7)
+MF_STAGES = 4
 MF_PREC_FP64, MF_PREC_MIXED = 0, 1
 MF_NEWTON_BATCH, MF_NEWTON_PER_EVENT = 0, 1
 
@@ -76,6 +77,8 @@ _SIGS = {
     "mf_vegas_iteration": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int, c_uint64, c_uint32, c_dp,
                                    c_int64, c_dp, c_dp, c_dp, c_void_p]),
     "mf_vegas_accumulate": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
+    "mf_process_set_timing": (c_int, [c_void_p, c_int]),
+    "mf_process_stage_ms": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float)]),
     "mf_vegas_accumulate_noalloc": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
     "mf_vegas_refine": (c_int, [c_dp, c_dp, c_int, c_int, c_double, c_void_p]),
     "mf_vegas_sample": (c_int, [c_dp, c_int, c_int, c_dp, c_int64, c_dp, c_dp, c_dp, c_void_p]),

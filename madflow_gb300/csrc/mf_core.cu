@@ -416,6 +416,10 @@ struct mf_process {
   double* d_me = nullptr;   // [cap]
   unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
   int64_t event_cap = 0;
+  // optional stage timing of the fused iteration (events on the caller's stream)
+  int timing = 0;
+  bool timed_last = false;
+  cudaEvent_t tev[MF_STAGES + 1] = {};
 };
 
 static const int kDiagrams[6] = {0, 0, 3, 16, 123, 1240};
@@ -433,6 +437,7 @@ const char* mf_status_string(int s) {
     case MF_ERR_UNSUPPORTED: return "unsupported process or precision";
     case MF_ERR_CAPACITY: return "request exceeds the supported maximum";
     case MF_ERR_NONFINITE: return "non-finite weights produced";
+    case MF_ERR_STATE: return "no result of that kind yet";
   }
   return "unknown status";
 }
@@ -471,6 +476,8 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_pref) cudaFree(p->d_pref);
   if (p->d_me) cudaFree(p->d_me);
   if (p->d_bins) cudaFree(p->d_bins);
+  for (cudaEvent_t e : p->tev)
+    if (e) cudaEventDestroy(e);
   delete p;
   return MF_OK;
 }
@@ -719,17 +726,52 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   }
   A.newton_iters = p->d_kmin;
   bool per_event = c->newton_rule == MF_NEWTON_PER_EVENT;
+  // stage timing: not while the stream is being captured into a graph
+  bool timed = false;
+  if (p->timing) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(S(stream), &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
+      timed = true;
+      for (cudaEvent_t& e : p->tev)
+        if (!e && cudaEventCreate(&e) != cudaSuccess) timed = false;
+    }
+  }
+  p->timed_last = timed;
+  auto mark = [&](int i) {
+    if (timed) cudaEventRecord(p->tev[i], S(stream));
+  };
+  mark(0);
   set_int_kernel<<<1, 1, 0, S(stream)>>>(p->d_kmin, per_event ? 0 : 11);
   if (!per_event && mf_launch_newton(p->k, A, p->d_kmin, S(stream))) return last_launch();
+  mark(1);
   if (mf_launch_ps(p->k, p->prec, A, S(stream))) return last_launch();
+  mark(2);
   if (mf_launch_me(p->k, p->prec, A.prep, A.N, A.pref, A.me, nullptr, S(stream))) return last_launch();
+  mark(3);
   size_t shm = (size_t)(A.ndim * A.nb + 2 * 256) * sizeof(double);
   cudaFuncSetAttribute(accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   accum_kernel<<<accum_grid, 256, shm, S(stream)>>>(A.pref, A.me, A.bins, A.N, A.ndim, A.nb, A.inv_n, f_out,
                                                      results ? p->d_partials : nullptr);
   if (results)
     reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(p->d_partials, accum_grid, width, results);
+  mark(4);
   return last_launch();
+}
+
+int mf_process_set_timing(mf_process* p, int enable) {
+  if (!p) return MF_ERR_ARG;
+  p->timing = enable != 0;
+  return MF_OK;
+}
+
+int mf_process_stage_ms(const mf_process* p, float* ms) {
+  if (!p || !ms) return MF_ERR_ARG;
+  if (!p->timed_last) return MF_ERR_STATE;
+  for (int i = 0; i < MF_STAGES; ++i) {
+    int st = cuda_status(cudaEventElapsedTime(&ms[i], p->tev[i], p->tev[i + 1]));
+    if (st) return st;
+  }
+  return MF_OK;
 }
 
 int mf_integrand(const mf_process* pc, const mf_integrand_config* c, const double* x, int64_t N, double* f,

@@ -222,77 +222,116 @@ MF_D void rec_stage(RecWS<T, K>& ws, const EvData<T, K>& ev, int stage, int tid,
   }
 }
 
-// stage A: add the top-line terms to every amplitude; items run over the
-// helicity combinations fastest so that neighbouring threads share operands
+// stage A: add the top-line terms to every amplitude.  An item is one
+// ordering and one assignment of the gluon helicities (in ordering
+// position); it owns the four (top, anti-top) helicity combinations, so each
+// top-line current and t~ row it reads serves two products.
 template <class T, int K> MF_D void rec_st_A(RecWS<T, K>& ws, int tid, int nt) {
   using R = RecTraits<K>;
-  constexpr int NC = 1 << (K + 2);
-  for (int it = tid; it < NC * R::NPERM; it += nt) {
-    int s = it / NC, c = it % NC;
-    int hg = c & ((1 << K) - 1), ht = (c >> K) & 1, htb = (c >> (K + 1)) & 1;
-    int hfull = R::hpack(s * (1 << K) + hg);
-    cx<T> a = ws.A[it];
+  constexpr int NC = 1 << (K + 2), NG = 1 << K;
+  for (int it = tid; it < NG * R::NPERM; it += nt) {
+    const int s = it / NG, hfull = it % NG;
+    const int hg = R::hunpack(s * NG + hfull);
+    cx<T> a[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) a[q] = ws.A[s * NC + (hg | ((q & 1) << K) | ((q >> 1) << (K + 1)))];
 #pragma unroll
     for (int i = 1; i < K; ++i) {
-      int oo = R::arec(s * 2 * (K - 1) + 2 * (i - 1)), ro = R::arec(s * 2 * (K - 1) + 2 * (i - 1) + 1);
-      W4<T> O = ws.O.get(oo + (ht << i) + (hfull & ((1 << i) - 1)));
-      W4<T> Rw = ws.RW.get(ro + (htb << (K - i)) + (hfull >> i));
-      a += dot4(Rw, O);
+      const int oo = R::arec(s * 2 * (K - 1) + 2 * (i - 1)), ro = R::arec(s * 2 * (K - 1) + 2 * (i - 1) + 1);
+      const int lo = hfull & ((1 << i) - 1), hi = hfull >> i;
+      W4<T> O0 = ws.O.get(oo + lo), O1 = ws.O.get(oo + (1 << i) + lo);
+      W4<T> R0 = ws.RW.get(ro + hi), R1 = ws.RW.get(ro + (1 << (K - i)) + hi);
+      a[0] += dot4(R0, O0);
+      a[1] += dot4(R0, O1);
+      a[2] += dot4(R1, O0);
+      a[3] += dot4(R1, O1);
     }
-    ws.A[it] = a;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ws.A[s * NC + (hg | ((q & 1) << K) | ((q >> 1) << (K + 1)))] = a[q];
   }
 }
 
-// stage colour: sum over this thread's (row, combination) items of
-// C_aa |A_a|^2 + 2 sum_{b>a} C_ab Re(A_a A_b^*); cm = integer numerators.
-// Summed in T per thread (the per-event sums are FP64).
-template <class T, int K> MF_D double rec_st_colour(const RecWS<T, K>& ws, const T* cm, int tid, int nt) {
+// Colour sum sum_c A(c)^dagger C A(c) with C real symmetric:
+//   sum_a C_aa |A_a|^2 + 2 sum_{b>a} C_ab Re(A_a A_b^*).
+// Rows a and NP-1-a together hold NP+1 matrix entries, so the NP/2 row pairs
+// are equal shares; an item is one helicity combination and one of
+// COLOUR_PARTS groups of row pairs.  The amplitudes of the combination sit in
+// registers and the integer numerators are compile-time operands.
+template <int K> MF_HD constexpr int colour_parts() {
+  constexpr int np = RecTraits<K>::NPERM, nc = 1 << (K + 2);
+  constexpr int want = 192 / nc > 0 ? 192 / nc : 1;
+  return want < np / 2 ? want : np / 2;
+}
+template <class T, int K, int PART> MF_D T colour_rows(const RecWS<T, K>& ws, int c) {
   using R = RecTraits<K>;
-  constexpr int NP = R::NPERM, NC = 1 << (K + 2);
+  constexpr int NP = R::NPERM, NC = 1 << (K + 2), P = colour_parts<K>();
+  static_assert(NP % 2 == 0, "row pairing needs an even number of orderings");
+  cx<T> A[NP];
+#pragma unroll
+  for (int b = 0; b < NP; ++b) A[b] = ws.A[b * NC + c];
   T acc = T(0);
-  for (int it = tid; it < NC * NP; it += nt) {
-    int a = it / NC, c = it % NC;
-    cx<T> z = {T(0), T(0)};
-    for (int b = a + 1; b < NP; ++b) z += cm[a * NP + b] * ws.A[b * NC + c];
-    cx<T> Aa = ws.A[it];
-    acc += cm[a * NP + a] * (Aa.re * Aa.re + Aa.im * Aa.im) + T(2) * (Aa.re * z.re + Aa.im * z.im);
+#pragma unroll
+  for (int g = PART; g < NP / 2; g += P) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int a = h ? NP - 1 - g : g;
+      cx<T> z = {T(0), T(0)};
+#pragma unroll
+      for (int b = a + 1; b < NP; ++b) z += (T)R::colour(a * NP + b) * A[b];
+      acc += (T)R::colour(a * NP + a) * (A[a].re * A[a].re + A[a].im * A[a].im) +
+             T(2) * (A[a].re * z.re + A[a].im * z.im);
+    }
   }
+  return acc;
+}
+template <class T, int K, int PART, bool LAST = (PART == colour_parts<K>() - 1)> struct ColourDispatch {
+  MF_D static T run(const RecWS<T, K>& ws, int c, int p) {
+    if (p == PART) return colour_rows<T, K, PART>(ws, c);
+    return ColourDispatch<T, K, PART + 1>::run(ws, c, p);
+  }
+};
+template <class T, int K, int PART> struct ColourDispatch<T, K, PART, true> {
+  MF_D static T run(const RecWS<T, K>& ws, int c, int) { return colour_rows<T, K, PART>(ws, c); }
+};
+template <class T, int K> MF_D double rec_st_colour(const RecWS<T, K>& ws, int tid, int nt) {
+  constexpr int NC = 1 << (K + 2), P = colour_parts<K>();
+  T acc = T(0);
+  for (int it = tid; it < NC * P; it += nt) acc += ColourDispatch<T, K, 0>::run(ws, it % NC, it / NC);
   return (double)acc;
 }
 
 // colour sum of one helicity combination c (per-helicity outputs)
-template <class T, int K> MF_D double rec_colour_one(const RecWS<T, K>& ws, const T* cm, int c) {
+template <class T, int K> MF_D double rec_colour_one(const RecWS<T, K>& ws, int c) {
   using R = RecTraits<K>;
   constexpr int NP = R::NPERM, NC = 1 << (K + 2);
   double acc = 0.0;
   for (int a = 0; a < NP; ++a) {
     cx<T> z = {T(0), T(0)};
-    for (int b = a + 1; b < NP; ++b) z += cm[a * NP + b] * ws.A[b * NC + c];
+    for (int b = a + 1; b < NP; ++b) z += (T)R::colour(a * NP + b) * ws.A[b * NC + c];
     cx<T> Aa = ws.A[a * NC + c];
-    acc += (double)(cm[a * NP + a] * (Aa.re * Aa.re + Aa.im * Aa.im) + T(2) * (Aa.re * z.re + Aa.im * z.im));
+    acc += (double)((T)R::colour(a * NP + a) * (Aa.re * Aa.re + Aa.im * Aa.im) + T(2) * (Aa.re * z.re + Aa.im * z.im));
   }
   return acc;
 }
 
 // the whole evaluation of one event by nt "threads" run one at a time (host tests)
 template <class T, int K> struct RecHostRun {
-  static double run(RecWS<T, K>& ws, const PrepRec<T, K>& pr, const T* cm, int nt) {
+  static double run(RecWS<T, K>& ws, const PrepRec<T, K>& pr, int nt) {
     for (int t = 0; t < nt; ++t) rec_st_ext<T, K>(ws, pr, t, nt);
     for (int st = 1; st < K; ++st)
       for (int t = 0; t < nt; ++t) rec_stage<T, K>(ws, pr.ev, st, t, nt);
     for (int t = 0; t < nt; ++t) rec_st_A<T, K>(ws, t, nt);
     double tot = 0.0;
-    for (int t = 0; t < nt; ++t) tot += rec_st_colour<T, K>(ws, cm, t, nt);
+    for (int t = 0; t < nt; ++t) tot += rec_st_colour<T, K>(ws, t, nt);
     return tot;
   }
 };
 
-constexpr int MF_REC_NT = 128;  // threads per event block
+constexpr int MF_REC_NT = 192;  // threads per event block
 
 template <class T, int K> struct RecSmem {
   RecWS<T, K> ws;
   PrepRec<T, K> pr;
-  T cm[RecTraits<K>::NPERM * RecTraits<K>::NPERM];
   double red[MF_REC_NT / 32];
 };
 template <class T, int K> MF_HD constexpr int prep_words() { return (int)(sizeof(PrepRec<T, K>) / 16); }
@@ -321,7 +360,7 @@ __global__ void __launch_bounds__(128) prep_kernel(const double* __restrict__ ps
 // skip (optional) [N]: events with skip[e] == 0 get out[e] = 0 without work;
 // out [N]; hel_out (optional) [ncomb][N] in MadGraph helicity order.
 template <int K, class T>
-__global__ void __launch_bounds__(MF_REC_NT) me_rec_kernel(const int4* __restrict__ prep, int64_t N,
+__global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2) me_rec_kernel(const int4* __restrict__ prep, int64_t N,
                                                           const double* __restrict__ skip, double* __restrict__ out,
                                                           double* __restrict__ hel_out) {
   using R = RecTraits<K>;
@@ -329,7 +368,6 @@ __global__ void __launch_bounds__(MF_REC_NT) me_rec_kernel(const int4* __restric
   RecSmem<T, K>& S = *reinterpret_cast<RecSmem<T, K>*>(smem_raw);
   const int tid = threadIdx.x, nt = blockDim.x;
   constexpr int NW = prep_words<T, K>();
-  for (int i = tid; i < R::NPERM * R::NPERM; i += nt) S.cm[i] = (T)R::colour(i);
   for (int64_t e = blockIdx.x; e < N; e += gridDim.x) {
     if (skip && skip[e] == 0.0) {
       if (tid == 0) out[e] = 0.0;
@@ -348,13 +386,13 @@ __global__ void __launch_bounds__(MF_REC_NT) me_rec_kernel(const int4* __restric
     }
     rec_st_A<T, K>(S.ws, tid, nt);
     __syncthreads();
-    double part = rec_st_colour<T, K>(S.ws, S.cm, tid, nt);
+    double part = rec_st_colour<T, K>(S.ws, tid, nt);
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((tid & 31) == 0) S.red[tid >> 5] = part;
     const double sc = S.pr.scale;
     if (hel_out)
       for (int c = tid; c < (1 << (K + 2)); c += nt)
-        hel_out[(int64_t)R::cfg_to_mg(c) * N + e] = rec_colour_one<T, K>(S.ws, S.cm, c) * sc * R::DENOMINATOR;
+        hel_out[(int64_t)R::cfg_to_mg(c) * N + e] = rec_colour_one<T, K>(S.ws, c) * sc * R::DENOMINATOR;
     __syncthreads();
     if (tid == 0) {
       double tot = 0.0;

@@ -142,6 +142,20 @@ def _clamp_open(x, eps=1e-7):
     return x.clamp(eps, 1.0 - eps)
 
 
+def _train_step(flow, opt, x, w, minibatch):
+    """Variance-loss updates on one batch (x, w = f/q) drawn from the flow."""
+    mean_w = w.mean()
+    scale = (mean_w * mean_w).clamp_min(1e-300)
+    n = x.shape[0]
+    for s in range(0, n, minibatch):
+        lq = flow.log_prob(x[s: s + minibatch])
+        wm = w[s: s + minibatch]
+        loss = -((wm * wm / scale).float() * lq).mean()
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        opt.step()
+
+
 def train_flow(flow, integrand, n_batches=20, batch_size=1_000_000, minibatch=100_000, lr=2e-3, seed=99,
                log=None):
     """Variance-loss training on weights f/q of batches drawn from the flow."""
@@ -150,23 +164,49 @@ def train_flow(flow, integrand, n_batches=20, batch_size=1_000_000, minibatch=10
     for b in range(n_batches):
         x, logq = flow.sample(batch_size, seed=seed, iteration=b)
         x = _clamp_open(x)
-        f = integrand(x)
-        w = f * torch.exp(-logq)
-        mean_w = w.mean()
-        scale = (mean_w * mean_w).clamp_min(1e-300)
-        for s in range(0, batch_size, minibatch):
-            xm = x[s: s + minibatch]
-            wm = w[s: s + minibatch]
-            lq = flow.log_prob(xm)
-            loss = -((wm * wm / scale).float() * lq).mean()
-            opt.zero_grad(set_to_none=True)
-            loss.backward()
-            opt.step()
-        rel = float(w.std() / w.mean()) if float(mean_w) != 0 else float("nan")
+        w = integrand(x) * torch.exp(-logq)
+        mean_w = float(w.mean())
+        _train_step(flow, opt, x, w, minibatch)
+        rel = float(w.std()) / mean_w if mean_w != 0 else float("nan")
         hist.append(rel)
         if log:
-            log(f"flow batch {b}: mean {float(mean_w):.5g}, std/mean {rel:.4f}")
+            log(f"flow batch {b}: mean {mean_w:.5g}, std/mean {rel:.4f}")
     return hist
+
+
+def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size=1_000_000, max_batches=200,
+                              train_batches=30, minibatch=100_000, lr=2e-3, seed=99):
+    """Integrate while training: every batch is drawn from the current (frozen)
+    flow, so mean(f/q) over it is an unbiased estimate with variance
+    var(f/q)/n; the estimates of all batches are combined with
+    inverse-variance weights (as VEGAS combines its iterations), and the first
+    ``train_batches`` batches also update the flow afterwards.  Stops when the
+    combined relative error reaches ``target_rel_error``.
+
+    Returns (result, error, info)."""
+    opt = torch.optim.Adam(flow.parameters(), lr=lr)
+    wsum = wres = 0.0
+    rel_std = float("nan")
+    b = 0
+    for b in range(int(max_batches)):
+        x, logq = flow.sample(batch_size, seed=seed, iteration=b)
+        x = _clamp_open(x)
+        w = integrand(x) * torch.exp(-logq)
+        mv = torch.stack([w.mean(), w.var()]).tolist()
+        res, var = mv[0], mv[1] / w.numel()
+        rel_std = math.sqrt(max(mv[1], 0.0)) / res if res != 0 else float("nan")
+        if var > 0:
+            wsum += 1.0 / var
+            wres += res / var
+            cur = wres / wsum
+            if cur != 0 and (1.0 / math.sqrt(wsum)) / abs(cur) <= target_rel_error:
+                break
+        if b < train_batches:
+            _train_step(flow, opt, x, w, minibatch)
+    info = {"batches": b + 1, "trained": min(b + 1, int(train_batches)), "last_rel_std": rel_std}
+    if wsum == 0:
+        return 0.0, 0.0, info
+    return wres / wsum, 1.0 / math.sqrt(wsum), info
 
 
 class FlowIntegrator:

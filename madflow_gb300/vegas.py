@@ -75,6 +75,17 @@ class FusedIntegrand:
                   results.data_ptr(), f_out.data_ptr() if f_out is not None else None,
                   u_out.data_ptr() if u_out is not None else None, stream_ptr())
 
+    def set_timing(self, enable=True):
+        """Record CUDA events between the pipeline stages of later calls."""
+        _lib.call("mf_process_set_timing", self.matrix.handle, int(bool(enable)))
+
+    def stage_ms(self):
+        """Milliseconds of the last call's stages (newton, phase space, matrix
+        element, accumulation); the caller synchronises first."""
+        ms = (ctypes.c_float * _lib.MF_STAGES)()
+        _lib.call("mf_process_stage_ms", self.matrix.handle, ms)
+        return dict(zip(("newton", "phase_space", "matrix_element", "accumulate"), list(ms)))
+
 
 class VegasFlow:
     """VEGAS integrator (the vegasflow interface madflow calls).

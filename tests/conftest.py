@@ -13,6 +13,31 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu)")
 
 
+HOST_SO = os.path.join(ROOT, "tests", "host", "_build", "libme_host.so")
+
+
+@pytest.fixture(scope="session")
+def host_lib():
+    """The generated recursion and the product's stage functions compiled as
+    host code (tests/host/me_host.cu)."""
+    import ctypes
+    import subprocess
+
+    from madflow_gb300 import codegen
+
+    src = os.path.join(ROOT, "tests", "host", "me_host.cu")
+    gen = os.path.join(ROOT, "madflow_gb300", "csrc", "generated")
+    codegen.write_generated(gen)
+    csrc = os.path.join(ROOT, "madflow_gb300", "csrc")
+    deps = [src] + [os.path.join(gen, f) for f in os.listdir(gen)] + [
+        os.path.join(csrc, f) for f in os.listdir(csrc) if f.endswith((".cuh", ".h"))]
+    if not os.path.exists(HOST_SO) or any(os.path.getmtime(d) > os.path.getmtime(HOST_SO) for d in deps):
+        os.makedirs(os.path.dirname(HOST_SO), exist_ok=True)
+        subprocess.run(["nvcc", "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-x", "cu", src, "-o", HOST_SO],
+                       check=True, capture_output=True)
+    return ctypes.CDLL(HOST_SO)
+
+
 @pytest.fixture(scope="session")
 def golden():
     return np.load(os.path.join(ROOT, "tests", "golden", "golden.npz"))

@@ -26,13 +26,11 @@ static double smatrix_one(const double* p, const double* coup, double mt, double
   cx<double> c10 = {coup[0], coup[1]}, c11 = {coup[2], coup[3]}, c12 = {coup[4], coup[5]};
   prep_event<T, K>(*pr, pd, mt, wt, c10, c11, c12);
   const int nt = 7;  // an odd "block size" exercises the item striding
-  T cm[R::NPERM * R::NPERM];
-  for (int i = 0; i < R::NPERM * R::NPERM; ++i) cm[i] = (T)R::colour(i);
-  double tot = RecHostRun<T, K>::run(*ws, *pr, cm, nt);
+  double tot = RecHostRun<T, K>::run(*ws, *pr, nt);
   double sc = pr->scale;
   if (hel_out)
     for (int c = 0; c < (1 << (K + 2)); ++c)
-      hel_out[R::cfg_to_mg(c)] = rec_colour_one<T, K>(*ws, cm, c) * sc * R::DENOMINATOR;
+      hel_out[R::cfg_to_mg(c)] = rec_colour_one<T, K>(*ws, c) * sc * R::DENOMINATOR;
   return tot * sc;
 }
 

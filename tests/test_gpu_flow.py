@@ -108,3 +108,27 @@ def test_flow_training_reduces_variance(cuda):
     flow = NormalizingFlow(4, n_layers=4, bins=16, hidden=64, seed=1)
     hist = train_flow(flow, peaked, n_batches=12, batch_size=100_000, minibatch=25_000, lr=5e-3)
     assert hist[-1] < 0.5 * hist[0]
+
+
+def test_adaptive_flow_integration(cuda):
+    """Training batches double as estimates: the combined result of a
+    normalised bump agrees with its integral within the quoted error, and the
+    quoted error reaches the target."""
+    import math
+
+    import torch
+
+    from madflow_gb300.flow import NormalizingFlow, adaptive_flow_integration
+
+    sig = 0.1
+    norm = (sig * math.sqrt(math.pi) * math.erf(0.5 / sig)) ** 3  # integral over the unit cube
+
+    def bump(x):
+        return torch.exp(-(((x - 0.5) / sig) ** 2).sum(-1)) / norm
+
+    flow = NormalizingFlow(3, n_layers=4, bins=16, hidden=32, seed=2)
+    res, err, info = adaptive_flow_integration(flow, bump, target_rel_error=3e-3, batch_size=50_000,
+                                               max_batches=60, train_batches=20, minibatch=25_000, lr=5e-3)
+    assert err / res <= 3e-3
+    assert abs(res - 1.0) < 4 * err
+    assert info["batches"] <= 60

@@ -314,3 +314,28 @@ def test_cuda_graph_replay_matches(cuda):
     b.compile(integ)
     rb = b.run_integration(4)
     assert ra == rb
+
+
+def test_stage_timing(cuda):
+    """Stage timing: nothing before an uncaptured timed call, then four
+    non-negative stage times whose matrix-element share is positive; the
+    integrand values are unchanged by the timing events."""
+    import torch
+
+    from madflow_gb300 import _lib
+    from madflow_gb300.vegas import FusedIntegrand
+
+    integ = FusedIntegrand(3, kind=1, sqrts=13000.0, ptmin=30.0, etamax=4.0, precision=1)
+    x = torch.rand((20000, integ.n_dim), dtype=torch.float64, device="cuda",
+                   generator=torch.Generator(device="cuda").manual_seed(3))
+    f0 = integ(x)
+    with pytest.raises(_lib.MadflowError):
+        integ.stage_ms()
+    integ.set_timing(True)
+    f1 = integ(x)
+    torch.cuda.synchronize()
+    ms = integ.stage_ms()
+    integ.set_timing(False)
+    assert set(ms) == {"newton", "phase_space", "matrix_element", "accumulate"}
+    assert all(v >= 0.0 for v in ms.values()) and ms["matrix_element"] > 0.0
+    assert torch.equal(f0, f1)

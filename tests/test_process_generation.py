@@ -1,8 +1,6 @@
 """The process generator (colour matrix, helicities, diagram counts) and the
 generated recursion, compiled as host code, against the oracle (CPU only)."""
 import ctypes
-import os
-import subprocess
 
 import numpy as np
 import pytest
@@ -47,23 +45,6 @@ def test_colour_matrix_bf16_tf32_exact():
     num, _ = codegen.colour_matrix(4)
     vals = np.unique(np.abs(np.array(num)))
     assert np.all(vals < 2**11)
-
-
-HOST_SO = os.path.join(ROOT, "tests", "host", "_build", "libme_host.so")
-
-
-@pytest.fixture(scope="module")
-def host_lib():
-    src = os.path.join(ROOT, "tests", "host", "me_host.cu")
-    gen = os.path.join(ROOT, "madflow_gb300", "csrc", "generated")
-    codegen.write_generated(gen)
-    deps = [src] + [os.path.join(gen, f) for f in os.listdir(gen)] + [
-        os.path.join(ROOT, "madflow_gb300", "csrc", f) for f in ("mf_vertex.cuh", "mf_helas.cuh", "mf_common.cuh")]
-    if not os.path.exists(HOST_SO) or any(os.path.getmtime(d) > os.path.getmtime(HOST_SO) for d in deps):
-        os.makedirs(os.path.dirname(HOST_SO), exist_ok=True)
-        subprocess.run(["nvcc", "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-x", "cu", src, "-o", HOST_SO],
-                       check=True, capture_output=True)
-    return ctypes.CDLL(HOST_SO)
 
 
 def _dp(a):
