@@ -234,7 +234,7 @@ def run_gpu(args):
         "pass_fraction": pass_frac,
         "phase_space_points_per_s": N * args.steps * world / step_s,
         "wall_s": wall,
-        # per step: set-int, newton pass, phase space, matrix element, accumulate, reduce, refine
+        # per step: set-int, phase-space first pass, phase space, matrix element, accumulate, reduce, refine
         "gpu_launches": 7 * args.steps,
         "stage_ms": stages,
         "e2e": {"value": e2e_rate, "unit": "|M|^2 evals/s", "h2d_bytes_per_step": int(x_host.numel() * 8),

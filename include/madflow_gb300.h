@@ -151,8 +151,9 @@ int mf_vegas_iteration(const mf_process* proc, const mf_integrand_config* cfg, c
  * (no counterpart in the reference).  With timing enabled, each call records
  * CUDA events on its stream between its stages; mf_process_stage_ms then
  * gives, once the caller has synchronised that stream, the milliseconds of the
- * last call's MF_STAGES stages: [0] batch Newton pass, [1] phase space + cuts
- * + PDF + matrix-element records, [2] matrix element, [3] accumulation.
+ * last call's MF_STAGES stages: [0] uniforms, grid map, massless phase space
+ * and the batch Newton minimum, [1] massive correction + cuts + PDF +
+ * matrix-element records, [2] matrix element, [3] accumulation.
  * Calls made while their stream is being captured into a CUDA graph record
  * nothing (MF_ERR_STATE until an uncaptured call has run). */
 #define MF_STAGES 4

@@ -412,6 +412,7 @@ struct mf_process {
   size_t partial_cap = 0;
   int* d_zero_iter = nullptr;
   int4* d_prep = nullptr;   // [cap] per-event matrix-element records
+  double* d_state = nullptr; // [state words][cap] first-pass phase-space state
   double* d_pref = nullptr; // [cap]
   double* d_me = nullptr;   // [cap]
   unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
@@ -473,6 +474,7 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_partials) cudaFree(p->d_partials);
   if (p->d_zero_iter) cudaFree(p->d_zero_iter);
   if (p->d_prep) cudaFree(p->d_prep);
+  if (p->d_state) cudaFree(p->d_state);
   if (p->d_pref) cudaFree(p->d_pref);
   if (p->d_me) cudaFree(p->d_me);
   if (p->d_bins) cudaFree(p->d_bins);
@@ -683,14 +685,17 @@ static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, Ite
 static int ensure_events(mf_process* p, int64_t N) {
   if (p->event_cap >= N) return MF_OK;
   cudaFree(p->d_prep);
+  cudaFree(p->d_state);
   cudaFree(p->d_pref);
   cudaFree(p->d_me);
   cudaFree(p->d_bins);
   p->d_prep = nullptr;
+  p->d_state = nullptr;
   p->d_pref = p->d_me = nullptr;
   p->d_bins = nullptr;
   p->event_cap = 0;
   int st = cuda_status(cudaMalloc(&p->d_prep, (size_t)mf_prep_bytes(p->k, p->prec) * N));
+  if (!st) st = cuda_status(cudaMalloc(&p->d_state, sizeof(double) * (size_t)mf_state_words(p->k) * N));
   if (!st) st = cuda_status(cudaMalloc(&p->d_pref, sizeof(double) * (size_t)N));
   if (!st) st = cuda_status(cudaMalloc(&p->d_me, sizeof(double) * (size_t)N));
   if (!st) st = cuda_status(cudaMalloc(&p->d_bins, (size_t)MF_MAX_DIM * N));
@@ -699,13 +704,14 @@ static int ensure_events(mf_process* p, int64_t N) {
   return MF_OK;
 }
 
-// One pass of the pipeline over A.N events: Newton first pass, phase space,
-// |M|^2, accumulation.  results (optional) [2 + ndim*nb]; f_out (optional) [N].
+// One pass of the pipeline over A.N events: phase-space first pass (with the
+// batch Newton minimum), phase space, |M|^2, accumulation.  results (optional) [2 + ndim*nb]; f_out (optional) [N].
 static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, double* results, double* f_out,
                      void* stream) {
   int st = ensure_events(p, A.N);
   if (st) return st;
   A.prep = p->d_prep;
+  A.state = p->d_state;
   A.pref = p->d_pref;
   A.me = p->d_me;
   A.bins = A.x_in ? nullptr : p->d_bins;
@@ -742,7 +748,7 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   };
   mark(0);
   set_int_kernel<<<1, 1, 0, S(stream)>>>(p->d_kmin, per_event ? 0 : 11);
-  if (!per_event && mf_launch_newton(p->k, A, p->d_kmin, S(stream))) return last_launch();
+  if (mf_launch_seed(p->k, A, p->d_kmin, per_event ? 0 : 1, S(stream))) return last_launch();
   mark(1);
   if (mf_launch_ps(p->k, p->prec, A, S(stream))) return last_launch();
   mark(2);

@@ -13,7 +13,8 @@ struct IterArgs;
   int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,  \
                            int64_t cstride, int4* prep, cudaStream_t st);                                   \
   int mf_launch_ps_k##KK(int prec, const IterArgs& A, cudaStream_t st);                                     \
-  int mf_launch_newton_k##KK(const IterArgs& A, int* kmin, cudaStream_t st);
+  int64_t mf_state_words_k##KK();                                                                            \
+  int mf_launch_seed_k##KK(const IterArgs& A, int* kmin, int batch_rule, cudaStream_t st);
 MF_DECLARE_PROCESS(2)
 MF_DECLARE_PROCESS(3)
 MF_DECLARE_PROCESS(4)
@@ -59,11 +60,18 @@ inline int mf_launch_ps(int k, int prec, const IterArgs& A, cudaStream_t st) {
   }
   return 3;
 }
-inline int mf_launch_newton(int k, const IterArgs& A, int* kmin, cudaStream_t st) {
+inline int64_t mf_state_words(int k) {
   switch (k) {
-    case 2: return mf_launch_newton_k2(A, kmin, st);
-    case 3: return mf_launch_newton_k3(A, kmin, st);
-    case 4: return mf_launch_newton_k4(A, kmin, st);
+    case 2: return mf_state_words_k2();
+    case 3: return mf_state_words_k3();
+    default: return mf_state_words_k4();
+  }
+}
+inline int mf_launch_seed(int k, const IterArgs& A, int* kmin, int batch_rule, cudaStream_t st) {
+  switch (k) {
+    case 2: return mf_launch_seed_k2(A, kmin, batch_rule, st);
+    case 3: return mf_launch_seed_k3(A, kmin, batch_rule, st);
+    case 4: return mf_launch_seed_k4(A, kmin, batch_rule, st);
   }
   return 3;
 }

@@ -1,12 +1,16 @@
 // One VEGAS iteration of the g g > t t~ + (K-2) g integrand as a pipeline of
 // persistent kernels over all N events of the iteration:
 //
-//   newton_pass_kernel  first pass of madflow's batch Newton rule
-//   ps_iter_kernel      one thread per event, FP64: Philox uniforms -> VEGAS
-//                       grid map -> ramboflow -> lab boost -> cuts -> PDF;
-//                       writes momenta [K+2][4][N], the prefactor
-//                       jac * weight * luminosity (0 for events failing the
-//                       cuts) and the bin indices
+//   ps_seed_kernel      one thread per event, FP64: Philox uniforms -> VEGAS
+//                       grid map (bin indices) -> x1, x2 -> massless rambo;
+//                       stores that state and takes the first pass of
+//                       madflow's batch Newton rule (the batch minimum of
+//                       the iteration at which an event converges)
+//   ps_iter_kernel      one thread per event, FP64: massive rambo correction
+//                       with the batch iteration count -> lab boost -> cuts
+//                       -> PDF; writes the prefactor jac * weight *
+//                       luminosity (0 for events failing the cuts) and the
+//                       matrix-element record of every passing event
 //   me_rec_kernel       one thread block per passing event: |M|^2 summed over
 //                       helicities and colours (mf_me_rec.cuh)
 //   accum_kernel        w = prefactor * |M|^2 / N; fixed-order block sums of
@@ -38,6 +42,7 @@ struct IterArgs {
   const double* x_in;  // optional [ndim][N] points (integrand API): no Philox / VEGAS map, jac = 1
   float* u_out;        // optional [ndim][N] uniforms
   // pipeline buffers (scratch)
+  double* state;            // [4(K)+6][N] first-pass state (ps_state_words)
   int4* prep;              // [N] per-event records (PrepRec), passing events only
   double* pref;            // [N]
   unsigned char* bins;     // [ndim][N]
@@ -46,13 +51,18 @@ struct IterArgs {
 
 constexpr int MF_MAX_DIM = 32;
 
-// Phase-space part of one event; returns false when it fails the cuts.
-// p: [npart][4] FP64 momenta in the partonic c.o.m. frame.
-MF_DO bool event_phase_space(const IterArgs& A, int npart, const double* x, int newton_iters, double (*p)[4],
-                             double& wgt_lum) {
+// Per-event state of the first pass, stored SoA [ps_state_words][N]: the
+// massless rambo momenta of the K outgoing particles [K][4], its log-weight,
+// s-hat, the x1 x2 weight, x1, x2 and the VEGAS jacobian.
+template <int K> MF_HD constexpr int ps_state_words() { return 4 * K + 6; }
+
+// First part of the phase space of one event (phasespace.py:257-300 up to
+// the massive correction).  p: [npart][4].
+MF_DO void event_massless(const IterArgs& A, int npart, const double* x, double (*p)[4], double& logw, double& shat,
+                          double& wgt, double& x1, double& x2) {
   MfConsts KC = mf_consts(A.f32q != 0);
-  int nout = npart - 2;
-  double shat, wgt, x1 = 1.0, x2 = 1.0;
+  x1 = 1.0;
+  x2 = 1.0;
   const double* xr = x;
   if (A.kind == 0) {
     shat = A.sqrts * A.sqrts;
@@ -62,7 +72,17 @@ MF_DO bool event_phase_space(const IterArgs& A, int npart, const double* x, int 
     xr = x + 2;
   }
   double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
-  double logw = rambo_massless(xr, nout, roots, KC.pi, p + 2);
+  logw = rambo_massless(xr, npart - 2, roots, KC.pi, p + 2);
+}
+
+// Rest of the phase space of one event: massive correction with
+// newton_iters iterations (<= 0: per event), incoming momenta, flux, lab
+// boost, cuts and luminosity.  Returns false when the event fails the cuts.
+MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (*p)[4], double logw, double shat,
+                        double wgt, double x1, double x2, double& wgt_lum) {
+  MfConsts KC = mf_consts(A.f32q != 0);
+  int nout = npart - 2;
+  double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
   logw = rambo_massive(nout, A.masses, p + 2, roots, logw, KC.acc, newton_iters);
   double wps = exp(logw) / pow(2.0 * KC.pi, (double)(3 * nout - 4));
   double ein = roots / 2.0;
@@ -120,43 +140,61 @@ MF_DO void event_point(const IterArgs& A, int64_t e, int it, double* x, double& 
     for (int d = 0; d < A.ndim; ++d) A.u_out[(int64_t)d * A.N + e] = (float)u[d];
 }
 
-// Batch Newton rule, first pass: the iteration at which the first event of the
-// batch converges (atomicMin into *kmin).
-template <int K>
-__global__ void __launch_bounds__(256) newton_pass_kernel(IterArgs A, int* kmin) {
+// First pass: the phase-space state of every event and, when batch_rule is
+// set, the batch minimum of the Newton convergence iteration (atomicMin into
+// *kmin, which starts at 11).  An event only needs to be followed up to the
+// smallest iteration seen so far, read from *kmin as it goes.
+template <int K> __global__ void __launch_bounds__(256) ps_seed_kernel(IterArgs A, int* kmin, int batch_rule) {
   constexpr int NPART = K + 2;
-  int local = 11;
   const int it = *A.iteration;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < A.N; e += (int64_t)gridDim.x * blockDim.x) {
-    double x[MF_MAX_DIM], jac;
-    event_point(A, e, it, x, jac, false);
-    MfConsts KC = mf_consts(A.f32q != 0);
-    double shat, wgt, x1, x2;
-    const double* xr = x;
-    if (A.kind == 0) shat = A.sqrts * A.sqrts;
-    else { get_x1x2(x[0], x[1], A.shat_min, A.sqrts * A.sqrts, shat, wgt, x1, x2); xr = x + 2; }
-    double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
-    double p[NPART][4];
-    rambo_massless(xr, NPART - 2, roots, KC.pi, p);
-    int c = newton_conv_iter(NPART - 2, A.masses, p, roots, KC.acc);
-    local = min(local, c);
+  const int64_t N = A.N;
+  int local = 11;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double x[MF_MAX_DIM], jac, p[NPART][4], logw, shat, wgt, x1, x2;
+    event_point(A, e, it, x, jac, true);
+    event_massless(A, NPART, x, p, logw, shat, wgt, x1, x2);
+    double* st = A.state + e;
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) st[(int64_t)(4 * i + c) * N] = p[i + 2][c];
+    st[(int64_t)(4 * K) * N] = logw;
+    st[(int64_t)(4 * K + 1) * N] = shat;
+    st[(int64_t)(4 * K + 2) * N] = wgt;
+    st[(int64_t)(4 * K + 3) * N] = x1;
+    st[(int64_t)(4 * K + 4) * N] = x2;
+    st[(int64_t)(4 * K + 5) * N] = jac;
+    if (batch_rule) {
+      const int lim = min(local, *(volatile int*)kmin);
+      const double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
+      const int c = newton_conv_iter(K, A.masses, p + 2, roots, mf_consts(A.f32q != 0).acc, lim);
+      if (c < lim) {
+        local = c;
+        atomicMin(kmin, c);
+      }
+    }
   }
-  for (int o = 16; o > 0; o >>= 1) local = min(local, __shfl_xor_sync(0xffffffffu, local, o));
-  if ((threadIdx.x & 31) == 0) atomicMin(kmin, local);
 }
 
-// Phase space of every event of the iteration (one thread per event), and
-// the per-event record of the matrix element for the events that pass.
+// Second pass: the rest of the phase space of every event, and the per-event
+// record of the matrix element for the events that pass.
 template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(IterArgs A) {
   constexpr int NPART = K + 2;
   constexpr int NW = prep_words<T, K>();
-  const int it = *A.iteration;
+  const int64_t N = A.N;
   // the batch rule runs at most 10 iterations (11 = no event converged)
   const int niter = min(*A.newton_iters, 10);
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < A.N; e += (int64_t)gridDim.x * blockDim.x) {
-    double x[MF_MAX_DIM], jac, p[NPART][4], wl;
-    event_point(A, e, it, x, jac, true);
-    bool ok = event_phase_space(A, NPART, x, niter, p, wl);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double p[NPART][4], wl;
+    const double* st = A.state + e;
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) p[i + 2][c] = st[(int64_t)(4 * i + c) * N];
+    const double logw = st[(int64_t)(4 * K) * N], shat = st[(int64_t)(4 * K + 1) * N];
+    const double wgt = st[(int64_t)(4 * K + 2) * N], x1 = st[(int64_t)(4 * K + 3) * N];
+    const double x2 = st[(int64_t)(4 * K + 4) * N], jac = st[(int64_t)(4 * K + 5) * N];
+    bool ok = event_finish(A, NPART, niter, p, logw, shat, wgt, x1, x2, wl);
     A.pref[e] = ok ? jac * wl : 0.0;
     if (ok) {
       PrepRec<T, K> r;

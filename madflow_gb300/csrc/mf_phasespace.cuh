@@ -66,14 +66,19 @@ MF_HD bool newton_step(int n, const double* m2, const double* e2, double sqrts, 
 }
 
 // Iteration (1..10) at which this event's f0 <= ACC first holds; 11 if never.
-MF_HD int newton_conv_iter(int n, const double* masses, const double (*p)[4], double sqrts, double acc) {
+// With lim <= 10 the search stops before iteration lim and returns lim when
+// the event has not converged by then (callers that only need the batch
+// minimum pass the smallest value found so far).
+MF_HD int newton_conv_iter(int n, const double* masses, const double (*p)[4], double sqrts, double acc,
+                           int lim = 11) {
   double m2[MF_MAX_OUT], e2[MF_MAX_OUT], newE[MF_MAX_OUT], tm = 0.0;
   for (int i = 0; i < n; ++i) { m2[i] = masses[i] * masses[i]; e2[i] = p[i][0] * p[i][0]; tm += masses[i]; }
   double r = tm / sqrts;
   double xf = sqrt(1.0 - r * r);
-  for (int it = 1; it <= 10; ++it)
+  const int last = lim - 1 < 10 ? lim - 1 : 10;
+  for (int it = 1; it <= last; ++it)
     if (!newton_step(n, m2, e2, sqrts, acc, xf, newE)) return it;
-  return 11;
+  return lim < 11 ? lim : 11;
 }
 
 // Massive correction of rambo (phasespace.py:194-212) running `iters` Newton

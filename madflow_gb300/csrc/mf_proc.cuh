@@ -64,11 +64,12 @@ static int sm_count() {
     else ps_iter_kernel<KK, float><<<(int)b, 128, 0, st>>>(A);                                                 \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }                                                                                                            \
-  int mf_launch_newton_k##KK(const IterArgs& A, int* kmin, cudaStream_t st) {                                  \
+  int64_t mf_state_words_k##KK() { return ps_state_words<KK>(); }                                               \
+  int mf_launch_seed_k##KK(const IterArgs& A, int* kmin, int batch_rule, cudaStream_t st) {                    \
     int64_t blocks = (A.N + 255) / 256;                                                                        \
     int64_t cap = (int64_t)sm_count() * 8;                                                                     \
     if (blocks > cap) blocks = cap;                                                                            \
     if (blocks < 1) blocks = 1;                                                                                \
-    newton_pass_kernel<KK><<<(int)blocks, 256, 0, st>>>(A, kmin);                                              \
+    ps_seed_kernel<KK><<<(int)blocks, 256, 0, st>>>(A, kmin, batch_rule);                                      \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }

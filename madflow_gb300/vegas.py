@@ -80,11 +80,12 @@ class FusedIntegrand:
         _lib.call("mf_process_set_timing", self.matrix.handle, int(bool(enable)))
 
     def stage_ms(self):
-        """Milliseconds of the last call's stages (newton, phase space, matrix
-        element, accumulation); the caller synchronises first."""
+        """Milliseconds of the last call's stages (phase-space first pass with
+        the batch Newton minimum, phase space, matrix element, accumulation);
+        the caller synchronises first."""
         ms = (ctypes.c_float * _lib.MF_STAGES)()
         _lib.call("mf_process_stage_ms", self.matrix.handle, ms)
-        return dict(zip(("newton", "phase_space", "matrix_element", "accumulate"), list(ms)))
+        return dict(zip(("seed", "phase_space", "matrix_element", "accumulate"), list(ms)))
 
 
 class VegasFlow:

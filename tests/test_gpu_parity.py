@@ -336,6 +336,6 @@ def test_stage_timing(cuda):
     torch.cuda.synchronize()
     ms = integ.stage_ms()
     integ.set_timing(False)
-    assert set(ms) == {"newton", "phase_space", "matrix_element", "accumulate"}
+    assert set(ms) == {"seed", "phase_space", "matrix_element", "accumulate"}
     assert all(v >= 0.0 for v in ms.values()) and ms["matrix_element"] > 0.0
     assert torch.equal(f0, f1)
