@@ -251,6 +251,8 @@ def run_gpu(args):
                      "kernel_ms": statistics.mean(me_ms)},
         "clocks": clk.summary(),
     }
+    if args.precision_points and rank == 0:
+        out["mixed_vs_fp64"] = precision_study(args.precision_points, args.seed + 2)
     if args.time_to_target and rank == 0:
         out["time_to_1e-3"] = time_to_target(args)
     if args.cpu_baseline and rank == 0:
@@ -263,6 +265,40 @@ def run_gpu(args):
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
+
+
+def precision_study(n_events, seed):
+    """|M|^2 and integrand error of the mixed-precision path against the FP64
+    path (which agrees with the FP64 oracle to 1e-12) on the same fixed
+    points: ramboflow momenta of n_events uniforms for |M|^2, the same
+    uniforms through the whole integrand (phase space, cuts, PDF)."""
+    import torch
+
+    from madflow_gb300 import _lib
+    from madflow_gb300.matrix import Matrix_1_gg_ttxgg
+    from madflow_gb300.phasespace import ramboflow
+
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    x = torch.rand((n_events, 18), dtype=torch.float64, device="cuda", generator=g)
+    p, *_ = ramboflow(x, 6, SQRTS, [MT, MT, 0.0, 0.0])
+    gs = math.sqrt(4.0 * math.pi * ALPHA_S)
+    coup = (complex(-gs, 0.0), complex(0.0, gs), complex(0.0, gs * gs))
+    me64 = Matrix_1_gg_ttxgg(precision=_lib.MF_PREC_FP64).smatrix(p, MT, WT, *coup)
+    me32 = Matrix_1_gg_ttxgg(precision=_lib.MF_PREC_MIXED).smatrix(p, MT, WT, *coup)
+    rel = ((me32 - me64).abs() / me64.abs()).double()
+    q = torch.quantile(rel[: min(n_events, 1 << 24)], torch.tensor([0.5, 0.99, 0.999], dtype=torch.float64,
+                                                                    device="cuda")).tolist()
+    f64 = make_integrand(_lib.MF_PREC_FP64)(x)
+    f32 = make_integrand(_lib.MF_PREC_MIXED)(x)
+    same = (f64 == 0) == (f32 == 0)
+    both = same & (f64 != 0)
+    frel = ((f32 - f64).abs() / f64.abs())[both]
+    return {"points": n_events, "me_rel_err": {"median": q[0], "p99": q[1], "p999": q[2], "max": float(rel.max())},
+            "integrand_rel_err": {"median": float(frel.median()), "max": float(frel.max()),
+                                  "sum": float(abs(f32[same].sum() - f64[same].sum()) / f64[same].abs().sum()),
+                                  "cut_decisions_differing": int((~same).sum())},
+            "momenta": "ramboflow of uniform points, sqrt(S) = 13 TeV, no cuts (|M|^2); "
+                       "the integrand with the benchmark cuts"}
 
 
 def _vegas_to_target(prec, n_events, seed, max_iter, target):
@@ -407,6 +443,7 @@ def main():
     ap.add_argument("--flow-batch", type=int, default=1_000_000)
     ap.add_argument("--flow-lr", type=float, default=2e-3)
     ap.add_argument("--flow-train-batches", type=int, default=30)
+    ap.add_argument("--precision-points", type=int, default=1_000_000)
     ap.add_argument("--e2e-events", type=int, default=4_000_000)
     ap.add_argument("--e2e-reps", type=int, default=3)
     args = ap.parse_args()

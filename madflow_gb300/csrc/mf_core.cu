@@ -56,23 +56,34 @@ const PdfHost& pdf_host() {
 }
 std::mutex g_pdf_mu;
 double* g_pdf_dev[64] = {nullptr};
+float* g_pdf_devf[64] = {nullptr};
 int pdf_device_table(PdfTable& T) {
   int dev = 0;
   int st = cuda_status(cudaGetDevice(&dev));
   if (st) return st;
+  if (dev < 0 || dev >= 64) return MF_ERR_CAPACITY;
   const PdfHost& H = pdf_host();
   {
     std::lock_guard<std::mutex> lk(g_pdf_mu);
     if (!g_pdf_dev[dev]) {
       double* d = nullptr;
+      float* f = nullptr;
+      std::vector<float> tf(H.tab.begin(), H.tab.end());
       st = cuda_status(cudaMalloc(&d, sizeof(double) * kNX * kNQ));
-      if (st) return st;
-      st = cuda_status(cudaMemcpy(d, H.tab.data(), sizeof(double) * kNX * kNQ, cudaMemcpyHostToDevice));
-      if (st) return st;
+      if (!st) st = cuda_status(cudaMalloc(&f, sizeof(float) * kNX * kNQ));
+      if (!st) st = cuda_status(cudaMemcpy(d, H.tab.data(), sizeof(double) * kNX * kNQ, cudaMemcpyHostToDevice));
+      if (!st) st = cuda_status(cudaMemcpy(f, tf.data(), sizeof(float) * kNX * kNQ, cudaMemcpyHostToDevice));
+      if (st) {
+        cudaFree(d);
+        cudaFree(f);
+        return st;
+      }
       g_pdf_dev[dev] = d;
+      g_pdf_devf[dev] = f;
     }
   }
   T.tab = g_pdf_dev[dev];
+  T.tabf = g_pdf_devf[dev];
   T.nx = kNX;
   T.nq = kNQ;
   T.lx0 = H.lx0;
@@ -748,7 +759,7 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   };
   mark(0);
   set_int_kernel<<<1, 1, 0, S(stream)>>>(p->d_kmin, per_event ? 0 : 11);
-  if (mf_launch_seed(p->k, A, p->d_kmin, per_event ? 0 : 1, S(stream))) return last_launch();
+  if (mf_launch_seed(p->k, p->prec, A, p->d_kmin, per_event ? 0 : 1, S(stream))) return last_launch();
   mark(1);
   if (mf_launch_ps(p->k, p->prec, A, S(stream))) return last_launch();
   mark(2);

@@ -14,7 +14,7 @@ struct IterArgs;
                            int64_t cstride, int4* prep, cudaStream_t st);                                   \
   int mf_launch_ps_k##KK(int prec, const IterArgs& A, cudaStream_t st);                                     \
   int64_t mf_state_words_k##KK();                                                                            \
-  int mf_launch_seed_k##KK(const IterArgs& A, int* kmin, int batch_rule, cudaStream_t st);
+  int mf_launch_seed_k##KK(int prec, const IterArgs& A, int* kmin, int batch_rule, cudaStream_t st);
 MF_DECLARE_PROCESS(2)
 MF_DECLARE_PROCESS(3)
 MF_DECLARE_PROCESS(4)
@@ -67,11 +67,11 @@ inline int64_t mf_state_words(int k) {
     default: return mf_state_words_k4();
   }
 }
-inline int mf_launch_seed(int k, const IterArgs& A, int* kmin, int batch_rule, cudaStream_t st) {
+inline int mf_launch_seed(int k, int prec, const IterArgs& A, int* kmin, int batch_rule, cudaStream_t st) {
   switch (k) {
-    case 2: return mf_launch_seed_k2(A, kmin, batch_rule, st);
-    case 3: return mf_launch_seed_k3(A, kmin, batch_rule, st);
-    case 4: return mf_launch_seed_k4(A, kmin, batch_rule, st);
+    case 2: return mf_launch_seed_k2(prec, A, kmin, batch_rule, st);
+    case 3: return mf_launch_seed_k3(prec, A, kmin, batch_rule, st);
+    case 4: return mf_launch_seed_k4(prec, A, kmin, batch_rule, st);
   }
   return 3;
 }

@@ -56,35 +56,98 @@ constexpr int MF_MAX_DIM = 32;
 // s-hat, the x1 x2 weight, x1, x2 and the VEGAS jacobian.
 template <int K> MF_HD constexpr int ps_state_words() { return 4 * K + 6; }
 
+// Uniforms of dimensions 2j, 2j+1 of an event: 53-bit in FP64, 24-bit in
+// FP32 (the high words of the same Philox4x32-10 block, so an FP32 uniform
+// is the FP64 one rounded down to 24 bits, plus half an FP32 step).
+MF_HD float u24(uint32_t hi) { return ((float)(hi >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+template <class P> MF_HD void uniform_pair(uint64_t seed, uint32_t stream, uint32_t it, uint64_t e, uint32_t j, P& u0,
+                                           P& u1);
+template <> MF_HD void uniform_pair<double>(uint64_t seed, uint32_t stream, uint32_t it, uint64_t e, uint32_t j,
+                                            double& u0, double& u1) {
+  philox_pair(seed, stream, it, e, j, u0, u1);
+}
+template <> MF_HD void uniform_pair<float>(uint64_t seed, uint32_t stream, uint32_t it, uint64_t e, uint32_t j,
+                                           float& u0, float& u1) {
+  uint32_t c[4] = {(uint32_t)e, (uint32_t)(e >> 32), j, it};
+  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32) ^ stream);
+  u0 = u24(c[0]);
+  u1 = u24(c[2]);
+}
+
+// VEGAS map of one event: x = lo + w*frac (fma), jac = prod w*nb; div is
+// the grid [ndim][nb+1] in P.
+template <class P>
+MF_DO P vegas_map(const P* __restrict__ div, int ndim, int nb, const P* u, P* x, unsigned char* bins, int64_t N) {
+  P jac = P(1);
+  for (int d = 0; d < ndim; ++d) {
+    P xn = u[d] * (P)nb;
+    int i = (int)xn;
+    if (i > nb - 1) i = nb - 1;
+    P frac = xn - (P)i;
+    P lo = div[d * (nb + 1) + i];
+    P w = div[d * (nb + 1) + i + 1] - lo;
+    x[d] = fma(w, frac, lo);
+    jac *= w * (P)nb;
+    if (bins) bins[(int64_t)d * N] = (unsigned char)i;
+  }
+  return jac;
+}
+
+// The point of event e: the caller's x (integrand API, jac = 1) or Philox
+// uniforms through the VEGAS grid (sdiv: the grid in P).
+template <class P>
+MF_DO void event_point(const IterArgs& A, int64_t e, int it, const P* sdiv, P* x, P& jac, bool store) {
+  if (A.x_in) {
+    for (int d = 0; d < A.ndim; ++d) x[d] = (P)A.x_in[(int64_t)d * A.N + e];
+    jac = P(1);
+    return;
+  }
+  P u[MF_MAX_DIM];
+  for (int d = 0; d < A.ndim; d += 2) uniform_pair<P>(A.seed, A.stream, (uint32_t)it, (uint64_t)e, d / 2, u[d], u[d + 1]);
+  jac = vegas_map<P>(sdiv, A.ndim, A.nb, u, x, store ? A.bins + e : nullptr, A.N);
+  if (store && A.u_out)
+    for (int d = 0; d < A.ndim; ++d) A.u_out[(int64_t)d * A.N + e] = (float)u[d];
+}
+
 // First part of the phase space of one event (phasespace.py:257-300 up to
-// the massive correction).  p: [npart][4].
-MF_DO void event_massless(const IterArgs& A, int npart, const double* x, double (*p)[4], double& logw, double& shat,
-                          double& wgt, double& x1, double& x2) {
+// the massive correction).  p: [npart][4]; w0 = rambo_w0(npart - 2, pi).
+template <class P>
+MF_DO void event_massless(const IterArgs& A, int npart, const P* x, double w0, double (*p)[4], double& logw,
+                          double& shat, double& wgt, double& x1, double& x2) {
   MfConsts KC = mf_consts(A.f32q != 0);
   x1 = 1.0;
   x2 = 1.0;
-  const double* xr = x;
+  const P* xr = x;
   if (A.kind == 0) {
     shat = A.sqrts * A.sqrts;
     wgt = 1.0;
   } else {
-    get_x1x2(x[0], x[1], A.shat_min, A.sqrts * A.sqrts, shat, wgt, x1, x2);
+    P sh, wg, a1, a2;
+    get_x1x2<P>(x[0], x[1], (P)A.shat_min, (P)(A.sqrts * A.sqrts), sh, wg, a1, a2);
+    shat = sh;
+    wgt = wg;
+    x1 = a1;
+    x2 = a2;
     xr = x + 2;
   }
   double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
-  logw = rambo_massless(xr, npart - 2, roots, KC.pi, p + 2);
+  double q[MF_MAX_OUT][4];
+  rambo_generate<P>(xr, npart - 2, (P)KC.pi, q);
+  logw = rambo_conformal(q, npart - 2, roots, w0, p + 2);
 }
 
 // Rest of the phase space of one event: massive correction with
 // newton_iters iterations (<= 0: per event), incoming momenta, flux, lab
-// boost, cuts and luminosity.  Returns false when the event fails the cuts.
+// boost, cuts and luminosity.  v: the PDF table coordinate of Q^2; pw:
+// (2 pi)^(3 nout - 4).  Returns false when the event fails the cuts.
+template <class P>
 MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (*p)[4], double logw, double shat,
-                        double wgt, double x1, double x2, double& wgt_lum) {
+                        double wgt, double x1, double x2, P v, double pw, double& wgt_lum) {
   MfConsts KC = mf_consts(A.f32q != 0);
   int nout = npart - 2;
   double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
   logw = rambo_massive(nout, A.masses, p + 2, roots, logw, KC.acc, newton_iters);
-  double wps = exp(logw) / pow(2.0 * KC.pi, (double)(3 * nout - 4));
+  double wps = (double)ps_exp((P)logw) / pw;
   double ein = roots / 2.0;
   p[0][0] = ein; p[0][1] = 0.0; p[0][2] = 0.0; p[0][3] = ein;
   p[1][0] = ein; p[1][1] = 0.0; p[1][2] = 0.0; p[1][3] = -ein;
@@ -97,62 +160,40 @@ MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (
   wgt = wgt / (2.0 * shat);
   bool ok = true;
   if (A.ptmin > 0.0 || A.etamax > 0.0 || A.drmin > 0.0) {
-    double plab[MF_MAX_OUT + 2][4];
+    P plab[MF_MAX_OUT + 2][4];
     for (int i = 0; i < npart; ++i) {
-      for (int c = 0; c < 4; ++c) plab[i][c] = p[i][c];
-      boost_lab(plab[i], x1, x2);
+      for (int c = 0; c < 4; ++c) plab[i][c] = (P)p[i][c];
+      boost_lab<P>(plab[i], (P)x1, (P)x2);
     }
-    ok = pass_gluon_cuts(plab, npart, A.ptmin, A.etamax, A.drmin);
+    ok = pass_gluon_cuts<P>(plab, npart, (P)A.ptmin, (P)A.etamax, (P)A.drmin);
   }
-  double lum = pdf_xfx(A.pdf, x1, A.q2) * pdf_xfx(A.pdf, x2, A.q2) / x1 / x2;
-  wgt_lum = wgt * lum;
+  P lum = pdf_xfx_v<P>(A.pdf, (P)x1, v) * pdf_xfx_v<P>(A.pdf, (P)x2, v) / (P)x1 / (P)x2;
+  wgt_lum = wgt * (double)lum;
   return ok;
-}
-
-// VEGAS map of one event: x = lo + w*frac (fma), jac = prod w*nb.
-MF_DO double vegas_map(const double* __restrict__ div, int ndim, int nb, const double* u, double* x,
-                       unsigned char* bins, int64_t N) {
-  double jac = 1.0;
-  for (int d = 0; d < ndim; ++d) {
-    double xn = u[d] * (double)nb;
-    int i = (int)xn;
-    if (i > nb - 1) i = nb - 1;
-    double frac = xn - (double)i;
-    double lo = div[d * (nb + 1) + i];
-    double w = div[d * (nb + 1) + i + 1] - lo;
-    x[d] = fma(w, frac, lo);
-    jac *= w * (double)nb;
-    if (bins) bins[(int64_t)d * N] = (unsigned char)i;
-  }
-  return jac;
-}
-
-MF_DO void event_point(const IterArgs& A, int64_t e, int it, double* x, double& jac, bool store) {
-  if (A.x_in) {
-    for (int d = 0; d < A.ndim; ++d) x[d] = A.x_in[(int64_t)d * A.N + e];
-    jac = 1.0;
-    return;
-  }
-  double u[MF_MAX_DIM];
-  for (int d = 0; d < A.ndim; d += 2) philox_pair(A.seed, A.stream, (uint32_t)it, (uint64_t)e, d / 2, u[d], u[d + 1]);
-  jac = vegas_map(A.div, A.ndim, A.nb, u, x, store ? A.bins + e : nullptr, A.N);
-  if (store && A.u_out)
-    for (int d = 0; d < A.ndim; ++d) A.u_out[(int64_t)d * A.N + e] = (float)u[d];
 }
 
 // First pass: the phase-space state of every event and, when batch_rule is
 // set, the batch minimum of the Newton convergence iteration (atomicMin into
 // *kmin, which starts at 11).  An event only needs to be followed up to the
-// smallest iteration seen so far, read from *kmin as it goes.
-template <int K> __global__ void __launch_bounds__(256) ps_seed_kernel(IterArgs A, int* kmin, int batch_rule) {
+// smallest iteration seen so far, read from *kmin as it goes.  Dynamic
+// shared memory: the VEGAS grid in P.
+template <int K, class P> __global__ void __launch_bounds__(256) ps_seed_kernel(IterArgs A, int* kmin, int batch_rule) {
   constexpr int NPART = K + 2;
+  extern __shared__ __align__(16) unsigned char seed_smem[];
+  P* sdiv = reinterpret_cast<P*>(seed_smem);
+  if (!A.x_in)
+    for (int i = threadIdx.x; i < A.ndim * (A.nb + 1); i += blockDim.x) sdiv[i] = (P)A.div[i];
+  __syncthreads();
   const int it = *A.iteration;
   const int64_t N = A.N;
+  const MfConsts KC = mf_consts(A.f32q != 0);
+  const double w0 = rambo_w0(K, KC.pi);
   int local = 11;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
-    double x[MF_MAX_DIM], jac, p[NPART][4], logw, shat, wgt, x1, x2;
-    event_point(A, e, it, x, jac, true);
-    event_massless(A, NPART, x, p, logw, shat, wgt, x1, x2);
+    P x[MF_MAX_DIM], jacp;
+    double p[NPART][4], logw, shat, wgt, x1, x2;
+    event_point<P>(A, e, it, sdiv, x, jacp, true);
+    event_massless<P>(A, NPART, x, w0, p, logw, shat, wgt, x1, x2);
     double* st = A.state + e;
 #pragma unroll
     for (int i = 0; i < K; ++i)
@@ -163,11 +204,11 @@ template <int K> __global__ void __launch_bounds__(256) ps_seed_kernel(IterArgs 
     st[(int64_t)(4 * K + 2) * N] = wgt;
     st[(int64_t)(4 * K + 3) * N] = x1;
     st[(int64_t)(4 * K + 4) * N] = x2;
-    st[(int64_t)(4 * K + 5) * N] = jac;
+    st[(int64_t)(4 * K + 5) * N] = (double)jacp;
     if (batch_rule) {
       const int lim = min(local, *(volatile int*)kmin);
       const double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
-      const int c = newton_conv_iter(K, A.masses, p + 2, roots, mf_consts(A.f32q != 0).acc, lim);
+      const int c = newton_conv_iter(K, A.masses, p + 2, roots, KC.acc, lim);
       if (c < lim) {
         local = c;
         atomicMin(kmin, c);
@@ -176,14 +217,18 @@ template <int K> __global__ void __launch_bounds__(256) ps_seed_kernel(IterArgs 
   }
 }
 
-// Second pass: the rest of the phase space of every event, and the per-event
-// record of the matrix element for the events that pass.
+// Second pass: the rest of the phase space of every event (phase-space
+// precision = the matrix-element precision T), and the per-event record of
+// the matrix element for the events that pass.
 template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(IterArgs A) {
   constexpr int NPART = K + 2;
   constexpr int NW = prep_words<T, K>();
   const int64_t N = A.N;
   // the batch rule runs at most 10 iterations (11 = no event converged)
   const int niter = min(*A.newton_iters, 10);
+  const MfConsts KC = mf_consts(A.f32q != 0);
+  const T v = (T)pdf_qcoord(A.pdf, A.q2);
+  const double pw = pow(2.0 * KC.pi, (double)(3 * K - 4));
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
     double p[NPART][4], wl;
     const double* st = A.state + e;
@@ -194,7 +239,7 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
     const double logw = st[(int64_t)(4 * K) * N], shat = st[(int64_t)(4 * K + 1) * N];
     const double wgt = st[(int64_t)(4 * K + 2) * N], x1 = st[(int64_t)(4 * K + 3) * N];
     const double x2 = st[(int64_t)(4 * K + 4) * N], jac = st[(int64_t)(4 * K + 5) * N];
-    bool ok = event_finish(A, NPART, niter, p, logw, shat, wgt, x1, x2, wl);
+    bool ok = event_finish<T>(A, NPART, niter, p, logw, shat, wgt, x1, x2, v, pw, wl);
     A.pref[e] = ok ? jac * wl : 0.0;
     if (ok) {
       PrepRec<T, K> r;

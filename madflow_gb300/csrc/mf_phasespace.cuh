@@ -1,5 +1,8 @@
-// Phase space on the device (madflow phasespace.py), FP64, one event per
-// thread.  The massive rescaling is split so that madflow's batch-wide Newton
+// Phase space on the device (madflow phasespace.py), one event per thread,
+// in a precision P: FP64 throughout for the FP64 path; for the mixed path
+// the uniforms, the massless momentum generation, x1 x2, the lab boost, the
+// cuts and the PDF run in FP32, the conformal transformation, the massive
+// rescaling and the weights in FP64.  The massive rescaling is split so that madflow's batch-wide Newton
 // stopping rule (phasespace.py:84-103) can be reproduced: newton_conv_iter()
 // gives the iteration at which an event first meets f0 <= ACC, the batch
 // minimum of that is the iteration count every event then runs.
@@ -8,26 +11,62 @@
 
 constexpr int MF_MAX_OUT = 8;
 
-// _gen_unconstrained_momenta (phasespace.py:121-142) + the conformal
-// transformation and scaling of rambo (phasespace.py:166-192) for one event.
-// p: [n][4]; returns the log-weight before the massive correction.
-MF_HD double rambo_massless(const double* x, int n, double sqrts, double pi, double (*p)[4]) {
-  double q[MF_MAX_OUT][4];
-  double sum[4] = {0, 0, 0, 0};
+// Elementary functions for a phase-space precision P (float: the
+// single-precision library functions).
+MF_HD double ps_log(double x) { return log(x); }
+MF_HD float ps_log(float x) { return logf(x); }
+MF_HD double ps_sqrt(double x) { return sqrt(x); }
+MF_HD float ps_sqrt(float x) { return sqrtf(x); }
+MF_HD double ps_exp(double x) { return exp(x); }
+MF_HD float ps_exp(float x) { return expf(x); }
+MF_HD double ps_pow(double x, double y) { return pow(x, y); }
+MF_HD float ps_pow(float x, float y) { return powf(x, y); }
+MF_HD double ps_atan2(double y, double x) { return atan2(y, x); }
+MF_HD float ps_atan2(float y, float x) { return atan2f(y, x); }
+MF_HD double ps_cosh(double x) { return cosh(x); }
+MF_HD float ps_cosh(float x) { return coshf(x); }
+MF_HD double ps_sinh(double x) { return sinh(x); }
+MF_HD float ps_sinh(float x) { return sinhf(x); }
+MF_HD void ps_sincos(double x, double* s, double* c) { sincos(x, s, c); }
+MF_HD void ps_sincos(float x, float* s, float* c) { sincosf(x, s, c); }
+MF_HD double ps_fabs(double x) { return fabs(x); }
+MF_HD float ps_fabs(float x) { return fabsf(x); }
+MF_HD double ps_floor(double x) { return floor(x); }
+MF_HD float ps_floor(float x) { return floorf(x); }
+
+// _gen_unconstrained_momenta (phasespace.py:121-142): n massless momenta q
+// [n][4] from 4n uniforms, computed in P and returned in FP64.
+template <class P> MF_HD void rambo_generate(const P* x, int n, P pi, double (*q)[4]) {
   for (int i = 0; i < n; ++i) {
-    const double* xi = x + 4 * i;
-    double costh = 2.0 * xi[0] - 1.0;
-    double sinth = sqrt(1.0 - costh * costh);
-    double phi = (2.0 * pi) * xi[1];
-    double energy = -1.0 * log(xi[2] * xi[3]);
-    double sphi, cphi;
-    sincos(phi, &sphi, &cphi);
+    const P* xi = x + 4 * i;
+    P costh = P(2) * xi[0] - P(1);
+    P sinth = ps_sqrt(P(1) - costh * costh);
+    P phi = (P(2) * pi) * xi[1];
+    P energy = P(-1) * ps_log(xi[2] * xi[3]);
+    P sphi, cphi;
+    ps_sincos(phi, &sphi, &cphi);
     q[i][0] = energy;
     q[i][1] = energy * sinth * sphi;
     q[i][2] = energy * sinth * cphi;
     q[i][3] = energy * costh;
-    for (int k = 0; k < 4; ++k) sum[k] += q[i][k];
   }
+}
+
+// The constant part of the massless rambo log-weight (phasespace.py:186-192).
+MF_HD double rambo_w0(int n, double pi) {
+  double wt = log(pi / 2.0) * (double)(n - 1);
+  wt -= 2.0 * lgamma((double)(n - 1));
+  wt -= log((double)(n - 1));
+  return wt;
+}
+
+// Conformal transformation and scaling of rambo (phasespace.py:166-192),
+// FP64: p [n][4] from q; returns the log-weight before the massive
+// correction (w0 = rambo_w0(n, pi)).
+MF_HD double rambo_conformal(const double (*q)[4], int n, double sqrts, double w0, double (*p)[4]) {
+  double sum[4] = {0, 0, 0, 0};
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 4; ++k) sum[k] += q[i][k];
   double qmass = sqrt(sum[0] * sum[0] - (sum[1] * sum[1] + sum[2] * sum[2] + sum[3] * sum[3]));
   double xs = sqrts / qmass;
   double b[4];
@@ -42,11 +81,15 @@ MF_HD double rambo_massless(const double* x, int n, double sqrts, double pi, dou
     p[i][3] = (q[i][3] + b[3] * tmp) * xs;
     p[i][0] = (q[i][0] * gamma + bq) * xs;
   }
-  double wt = log(pi / 2.0) * (double)(n - 1);
-  wt -= 2.0 * lgamma((double)(n - 1));
-  wt -= log((double)(n - 1));
-  wt += (double)(2 * n - 4) * log(sqrts);
-  return wt;
+  return w0 + (double)(2 * n - 4) * log(sqrts);
+}
+
+// rambo without the massive correction (FP64): p [n][4]; returns the
+// log-weight before the massive correction.
+MF_HD double rambo_massless(const double* x, int n, double sqrts, double pi, double (*p)[4]) {
+  double q[MF_MAX_OUT][4];
+  rambo_generate<double>(x, n, pi, q);
+  return rambo_conformal(q, n, sqrts, rambo_w0(n, pi), p);
 }
 
 // One Newton step of _massive_xfactor (phasespace.py:77-92).
@@ -115,50 +158,50 @@ MF_HD double rambo_massive(int n, const double* masses, double (*p)[4], double s
 }
 
 // _get_x1x2 (phasespace.py:215-233)
-MF_HD void get_x1x2(double xr0, double xr1, double shat_min, double s_in, double& shat, double& wgt, double& x1,
-                    double& x2) {
-  double taumin = shat_min / s_in;
-  double delta = 1.0 - taumin;
-  double tau = xr0 * delta + taumin;
+template <class P>
+MF_HD void get_x1x2(P xr0, P xr1, P shat_min, P s_in, P& shat, P& wgt, P& x1, P& x2) {
+  P taumin = shat_min / s_in;
+  P delta = P(1) - taumin;
+  P tau = xr0 * delta + taumin;
   wgt = delta;
-  x1 = pow(tau, xr1);
+  x1 = ps_pow(tau, xr1);
   x2 = tau / x1;
-  wgt = wgt * (-1.0 * log(tau));
+  wgt = wgt * (P(-1) * ps_log(tau));
   shat = x1 * x2 * s_in;
 }
 
 // _boost_to_lab (phasespace.py:322-356) of one momentum
-MF_HD void boost_lab(double* q, double x1, double x2) {
-  double eta = -0.5 * log(x1 / x2);
-  double c = cosh(eta), s = sinh(eta);
-  double E = q[0], pz = q[3];
+template <class P> MF_HD void boost_lab(P* q, P x1, P x2) {
+  P eta = P(-0.5) * ps_log(x1 / x2);
+  P c = ps_cosh(eta), s = ps_sinh(eta);
+  P E = q[0], pz = q[3];
   q[0] = E * c - pz * s;
   q[3] = pz * c - E * s;
 }
 
 // Cut decision on the outgoing gluons (particles 4..) in the lab frame: pT,
 // |eta| and Delta R between gluon pairs.  A threshold <= 0 disables a cut.
-MF_HD bool pass_gluon_cuts(const double (*plab)[4], int npart, double ptmin, double etamax, double drmin) {
+template <class P> MF_HD bool pass_gluon_cuts(const P (*plab)[4], int npart, P ptmin, P etamax, P drmin) {
   int ng = npart - 4;
-  double eta[MF_MAX_OUT], phi[MF_MAX_OUT];
+  P eta[MF_MAX_OUT], phi[MF_MAX_OUT];
   for (int g = 0; g < ng; ++g) {
-    const double* q = plab[4 + g];
-    double pt = sqrt(q[1] * q[1] + q[2] * q[2]);
-    if (ptmin > 0.0 && !(pt > ptmin)) return false;
-    double pabs = sqrt(pt * pt + q[3] * q[3]);
-    eta[g] = 0.5 * log((pabs + q[3]) / (pabs - q[3]));
-    phi[g] = atan2(q[2], q[1]);
-    if (etamax > 0.0 && !(fabs(eta[g]) < etamax)) return false;
+    const P* q = plab[4 + g];
+    P pt = ps_sqrt(q[1] * q[1] + q[2] * q[2]);
+    if (ptmin > P(0) && !(pt > ptmin)) return false;
+    P pabs = ps_sqrt(pt * pt + q[3] * q[3]);
+    eta[g] = P(0.5) * ps_log((pabs + q[3]) / (pabs - q[3]));
+    phi[g] = ps_atan2(q[2], q[1]);
+    if (etamax > P(0) && !(ps_fabs(eta[g]) < etamax)) return false;
   }
-  if (drmin > 0.0)
+  if (drmin > P(0))
     for (int a = 0; a < ng; ++a)
       for (int b = a + 1; b < ng; ++b) {
-        double de = eta[a] - eta[b];
-        double dp = phi[a] - phi[b];
-        const double pi = 3.141592653589793;
-        while (dp > pi) dp -= 2.0 * pi;
-        while (dp < -pi) dp += 2.0 * pi;
-        if (!(sqrt(de * de + dp * dp) > drmin)) return false;
+        P de = eta[a] - eta[b];
+        P dp = phi[a] - phi[b];
+        const P pi = P(3.141592653589793);
+        while (dp > pi) dp -= P(2) * pi;
+        while (dp < -pi) dp += P(2) * pi;
+        if (!(ps_sqrt(de * de + dp * dp) > drmin)) return false;
       }
   return true;
 }
@@ -167,27 +210,38 @@ MF_HD bool pass_gluon_cuts(const double (*plab)[4], int npart, double ptmin, dou
 // bicubic convolution (Keys 1981, a = -1/2) with clamped edge nodes.
 struct PdfTable {
   const double* tab;  // [nq][nx]
+  const float* tabf;  // the same table rounded to FP32
   int nx, nq;
   double lx0, dlx, lq0, dlq;
 };
-MF_HD double keys_w(double t) {
-  t = fabs(t);
-  if (t <= 1.0) return (1.5 * t - 2.5) * t * t + 1.0;
-  if (t < 2.0) return ((-0.5 * t + 2.5) * t - 4.0) * t + 2.0;
-  return 0.0;
+template <class P> MF_HD P keys_w(P t) {
+  t = ps_fabs(t);
+  if (t <= P(1)) return (P(1.5) * t - P(2.5)) * t * t + P(1);
+  if (t < P(2)) return ((P(-0.5) * t + P(2.5)) * t - P(4)) * t + P(2);
+  return P(0);
 }
-MF_HD double pdf_xfx(const PdfTable& P, double x, double q2) {
-  double u = (log(x) - P.lx0) / P.dlx, v = (log(q2) - P.lq0) / P.dlq;
-  int iu = (int)floor(u), iv = (int)floor(v);
-  double fu = u - iu, fv = v - iv;
-  double s = 0.0;
+template <class P> MF_HD const P* pdf_tab(const PdfTable& T);
+template <> MF_HD const double* pdf_tab<double>(const PdfTable& T) { return T.tab; }
+template <> MF_HD const float* pdf_tab<float>(const PdfTable& T) { return T.tabf; }
+// table coordinate of log Q^2 (the same for every event of a batch)
+MF_HD double pdf_qcoord(const PdfTable& T, double q2) { return (log(q2) - T.lq0) / T.dlq; }
+// x g(x, Q^2) with v = pdf_qcoord(T, q2)
+template <class P> MF_HD P pdf_xfx_v(const PdfTable& T, P x, P v) {
+  const P* tab = pdf_tab<P>(T);
+  P u = (ps_log(x) - (P)T.lx0) / (P)T.dlx;
+  int iu = (int)ps_floor(u), iv = (int)ps_floor(v);
+  P fu = u - iu, fv = v - iv;
+  P wu[4];
+  for (int b = -1; b <= 2; ++b) wu[b + 1] = keys_w<P>(fu - b);
+  P s = P(0);
   for (int a = -1; a <= 2; ++a) {
-    int qi = min(max(iv + a, 0), P.nq - 1);
-    double wv = keys_w(fv - a);
+    int qi = min(max(iv + a, 0), T.nq - 1);
+    P wv = keys_w<P>(fv - a);
     for (int b = -1; b <= 2; ++b) {
-      int xi = min(max(iu + b, 0), P.nx - 1);
-      s += wv * keys_w(fu - b) * P.tab[qi * P.nx + xi];
+      int xi = min(max(iu + b, 0), T.nx - 1);
+      s += wv * wu[b + 1] * tab[qi * T.nx + xi];
     }
   }
-  return s > 0.0 ? s : 0.0;  // the cubic can overshoot below zero next to x = 1
+  return s > P(0) ? s : P(0);  // the cubic can overshoot below zero next to x = 1
 }
+MF_HD double pdf_xfx(const PdfTable& T, double x, double q2) { return pdf_xfx_v<double>(T, x, pdf_qcoord(T, q2)); }

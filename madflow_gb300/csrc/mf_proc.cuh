@@ -65,11 +65,15 @@ static int sm_count() {
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }                                                                                                            \
   int64_t mf_state_words_k##KK() { return ps_state_words<KK>(); }                                               \
-  int mf_launch_seed_k##KK(const IterArgs& A, int* kmin, int batch_rule, cudaStream_t st) {                    \
+  int mf_launch_seed_k##KK(int prec, const IterArgs& A, int* kmin, int batch_rule, cudaStream_t st) {          \
     int64_t blocks = (A.N + 255) / 256;                                                                        \
     int64_t cap = (int64_t)sm_count() * 8;                                                                     \
     if (blocks > cap) blocks = cap;                                                                            \
     if (blocks < 1) blocks = 1;                                                                                \
-    ps_seed_kernel<KK><<<(int)blocks, 256, 0, st>>>(A, kmin, batch_rule);                                      \
+    size_t grid_words = A.x_in ? 0 : (size_t)A.ndim * (A.nb + 1);                                              \
+    if (prec == 0)                                                                                             \
+      ps_seed_kernel<KK, double><<<(int)blocks, 256, grid_words * sizeof(double), st>>>(A, kmin, batch_rule);   \
+    else                                                                                                       \
+      ps_seed_kernel<KK, float><<<(int)blocks, 256, grid_words * sizeof(float), st>>>(A, kmin, batch_rule);     \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }

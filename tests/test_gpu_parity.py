@@ -241,6 +241,27 @@ def test_integrand_vs_oracle(cuda, oracle, k, cuts):
     assert rel_err(f[big], fo[big]) < 1e-9
 
 
+@pytest.mark.parametrize("k,cuts", [(3, (30.0, 4.0, 0.0)), (4, (60.0, 2.5, 0.4))])
+def test_integrand_mixed_vs_oracle(cuda, oracle, k, cuts):
+    """Mixed precision (FP32 phase space, cuts, PDF and wavefunctions; FP64
+    rambo rescaling and propagator denominators) against the FP64 oracle:
+    cut decisions may differ only for events within FP32 rounding of a cut
+    boundary; elsewhere each value within 1e-4 of the largest and the sum
+    within 1e-5."""
+    from madflow_gb300.vegas import FusedIntegrand
+
+    integ = FusedIntegrand(k, kind=1, sqrts=13000.0, ptmin=cuts[0], etamax=cuts[1], drmin=cuts[2], precision=1)
+    rng = np.random.default_rng(50 + k)
+    x = rng.uniform(size=(4000, integ.n_dim))
+    f = _np(integ(x))
+    fo = oracle.integrand(_cfg_vec(1, k, 13000.0, *cuts), x, oracle.TTNG(k))
+    same = (f == 0) == (fo == 0)
+    assert (~same).sum() <= 2
+    assert (fo != 0).sum() > 100
+    assert np.max(np.abs(f - fo)[same]) < 1e-4 * np.abs(fo).max()
+    assert abs(f[same].sum() - fo[same].sum()) < 1e-5 * np.abs(fo[same]).sum()
+
+
 def test_integrand_ggttx_fixed_sqrts(cuda, oracle):
     from madflow_gb300.vegas import FusedIntegrand
 
