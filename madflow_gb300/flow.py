@@ -174,8 +174,20 @@ def train_flow(flow, integrand, n_batches=20, batch_size=1_000_000, minibatch=10
     return hist
 
 
+def _vegas_map(grid, z):
+    """x = G(z) through a frozen VEGAS grid [ndim][nb+1]; returns (x (N, ndim), jac)."""
+    n, dim = z.shape
+    u = z.T.contiguous()
+    x = torch.empty_like(u)
+    jac = torch.empty(n, dtype=torch.float64, device=z.device)
+    bins = torch.empty((dim, n), dtype=torch.int32, device=z.device)
+    _lib.call("mf_vegas_sample", grid.data_ptr(), dim, grid.shape[1] - 1, u.data_ptr(), n, x.data_ptr(),
+              jac.data_ptr(), bins.data_ptr(), stream_ptr())
+    return x.T, jac
+
+
 def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size=1_000_000, max_batches=200,
-                              train_batches=30, minibatch=100_000, lr=2e-3, seed=99):
+                              train_batches=30, minibatch=100_000, lr=2e-3, seed=99, grid=None, prior=None):
     """Integrate while training: every batch is drawn from the current (frozen)
     flow, so mean(f/q) over it is an unbiased estimate with variance
     var(f/q)/n; the estimates of all batches are combined with
@@ -183,15 +195,25 @@ def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size
     ``train_batches`` batches also update the flow afterwards.  Stops when the
     combined relative error reaches ``target_rel_error``.
 
+    grid (optional): a frozen VEGAS grid [ndim][nb+1]; the flow then models
+    the density of the grid's input variables, x = G(z), and the weights are
+    f(G(z)) |dG/dz| / q(z).  prior (optional): (wsum, wres) of earlier
+    unbiased estimates (e.g. the VEGAS iterations that adapted the grid), in
+    the same inverse-variance form.
+
     Returns (result, error, info)."""
     opt = torch.optim.Adam(flow.parameters(), lr=lr)
-    wsum = wres = 0.0
+    wsum, wres = prior if prior is not None else (0.0, 0.0)
     rel_std = float("nan")
     b = 0
     for b in range(int(max_batches)):
-        x, logq = flow.sample(batch_size, seed=seed, iteration=b)
-        x = _clamp_open(x)
-        w = integrand(x) * torch.exp(-logq)
+        z, logq = flow.sample(batch_size, seed=seed, iteration=b)
+        z = _clamp_open(z)
+        if grid is None:
+            w = integrand(z) * torch.exp(-logq)
+        else:
+            x, jac = _vegas_map(grid, z)
+            w = integrand(x) * jac * torch.exp(-logq)
         mv = torch.stack([w.mean(), w.var()]).tolist()
         res, var = mv[0], mv[1] / w.numel()
         rel_std = math.sqrt(max(mv[1], 0.0)) / res if res != 0 else float("nan")
@@ -202,7 +224,7 @@ def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size
             if cur != 0 and (1.0 / math.sqrt(wsum)) / abs(cur) <= target_rel_error:
                 break
         if b < train_batches:
-            _train_step(flow, opt, x, w, minibatch)
+            _train_step(flow, opt, z, w, minibatch)
     info = {"batches": b + 1, "trained": min(b + 1, int(train_batches)), "last_rel_std": rel_std}
     if wsum == 0:
         return 0.0, 0.0, info
