@@ -158,6 +158,12 @@ int mf_vegas_iteration(const mf_process* proc, const mf_integrand_config* cfg, c
  * nothing (MF_ERR_STATE until an uncaptured call has run). */
 #define MF_STAGES 4
 int mf_process_set_timing(mf_process* proc, int enable);
+
+/* Device error flags the handle's kernels raised (no counterpart in the
+ * reference): bit 0 = a bounded wait on the tensor cores ran out (the
+ * affected events got NaN).  Synchronous device-to-host read; clear != 0
+ * resets the flags. */
+int mf_process_error_flags(mf_process* proc, int* flags, int clear);
 int mf_process_stage_ms(const mf_process* proc, float* ms);
 
 /* VEGAS accumulation for an integrand evaluated by the caller: f [N], jac

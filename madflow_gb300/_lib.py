@@ -78,6 +78,7 @@ _SIGS = {
                                    c_int64, c_dp, c_dp, c_dp, c_void_p]),
     "mf_vegas_accumulate": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
     "mf_process_set_timing": (c_int, [c_void_p, c_int]),
+    "mf_process_error_flags": (c_int, [c_void_p, ctypes.POINTER(c_int), c_int]),
     "mf_process_stage_ms": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float)]),
     "mf_vegas_accumulate_noalloc": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
     "mf_vegas_refine": (c_int, [c_dp, c_dp, c_int, c_int, c_double, c_void_p]),

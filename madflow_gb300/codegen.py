@@ -238,6 +238,26 @@ def _canonical(seq):
     return rev, (-1) ** (len(seq) + 1)
 
 
+def colour_tc_operand(k):
+    """The colour numerators as the B operand (N x K, K-major, 32-bit) of a
+    tensor-core MMA, in the no-swizzle canonical shared-memory layout: core
+    matrices of 8 rows x 16 bytes stored contiguously, neighbours along K
+    TC_LBO = 128 bytes apart, neighbouring 8-row groups TC_SBO = NPERM/4 x
+    128 bytes apart.  N is padded to a multiple of 16 with zero rows.
+    B[n][k] = C[k][n].  Returns (padded N, flat list of floats)."""
+    num, _ = colour_matrix(k)
+    n = len(num)
+    if n % 4:
+        raise ValueError("the canonical layout needs a multiple of 4 colour flows")
+    npad = -(-n // 16) * 16
+    lbo, sbo = 32, (n // 4) * 32  # in 4-byte elements
+    out = [0.0] * ((npad // 8) * sbo)
+    for r in range(npad):
+        for c in range(n):
+            out[(r // 8) * sbo + (c // 4) * lbo + (r % 8) * 4 + (c % 4)] = float(num[c][r]) if r < n else 0.0
+    return npad, out
+
+
 def emit_process_header(k):
     """Header with the process constants and the amplitude recursion."""
     num, den = colour_matrix(k)
@@ -262,6 +282,16 @@ def emit_process_header(k):
     for h in hels:
         L.append("  {" + ", ".join(str(int(v)) for v in h) + "},")
     L.append("};")
+    if n % 4 == 0:
+        npad, tcb = colour_tc_operand(k)
+        L.append("// the colour numerators as a tensor-core B operand (colour_tc_operand)")
+        L.append(f"constexpr int TC_N = {npad};")
+        L.append("constexpr int TC_LBO = 128;")
+        L.append(f"constexpr int TC_SBO = {(n // 4) * 128};")
+        L.append(f"__device__ __align__(16) const float colour_tc_b[{len(tcb)}] = {{")
+        for i in range(0, len(tcb), 16):
+            L.append("  " + ", ".join(f"{v!r}f" for v in tcb[i:i + 16]) + ",")
+        L.append("};")
     L.append("// host copies for the handle's info calls")
     L.append(f"static const float colour_num_h[{n * n}] = {{")
     for r in num:

@@ -428,6 +428,7 @@ struct mf_process {
   double* d_me = nullptr;   // [cap]
   unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
   int64_t event_cap = 0;
+  int* d_err = nullptr;     // device error flags of the kernels (bit 0: a tensor-core wait ran out)
   // optional stage timing of the fused iteration (events on the caller's stream)
   int timing = 0;
   bool timed_last = false;
@@ -489,6 +490,7 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_pref) cudaFree(p->d_pref);
   if (p->d_me) cudaFree(p->d_me);
   if (p->d_bins) cudaFree(p->d_bins);
+  if (p->d_err) cudaFree(p->d_err);
   for (cudaEvent_t e : p->tev)
     if (e) cudaEventDestroy(e);
   delete p;
@@ -525,7 +527,7 @@ int mf_smatrix(const mf_process* p, const double* ps, int64_t N, double mt, doub
   int st = ensure_events(pm, N);
   if (st) return st;
   if (mf_launch_prep(p->k, p->prec, ps, N, mt, wt, coup, cstride, pm->d_prep, S(stream))) return last_launch();
-  st = mf_launch_me(p->k, p->prec, pm->d_prep, N, nullptr, out, hel_out, S(stream));
+  st = mf_launch_me(p->k, p->prec, pm->d_prep, N, nullptr, out, hel_out, pm->d_err, S(stream));
   if (st == 3) return MF_ERR_UNSUPPORTED;
   return st ? last_launch() : MF_OK;
 }
@@ -694,6 +696,11 @@ static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, Ite
 }
 
 static int ensure_events(mf_process* p, int64_t N) {
+  if (!p->d_err) {
+    int st = cuda_status(cudaMalloc(&p->d_err, sizeof(int)));
+    if (!st) st = cuda_status(cudaMemset(p->d_err, 0, sizeof(int)));
+    if (st) return st;
+  }
   if (p->event_cap >= N) return MF_OK;
   cudaFree(p->d_prep);
   cudaFree(p->d_state);
@@ -763,7 +770,7 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   mark(1);
   if (mf_launch_ps(p->k, p->prec, A, S(stream))) return last_launch();
   mark(2);
-  if (mf_launch_me(p->k, p->prec, A.prep, A.N, A.pref, A.me, nullptr, S(stream))) return last_launch();
+  if (mf_launch_me(p->k, p->prec, A.prep, A.N, A.pref, A.me, nullptr, p->d_err, S(stream))) return last_launch();
   mark(3);
   size_t shm = (size_t)(A.ndim * A.nb + 2 * 256) * sizeof(double);
   cudaFuncSetAttribute(accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
@@ -773,6 +780,15 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
     reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(p->d_partials, accum_grid, width, results);
   mark(4);
   return last_launch();
+}
+
+int mf_process_error_flags(mf_process* p, int* flags, int clear) {
+  if (!p || !flags) return MF_ERR_ARG;
+  *flags = 0;
+  if (!p->d_err) return MF_OK;
+  int st = cuda_status(cudaMemcpy(flags, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!st && clear) st = cuda_status(cudaMemset(p->d_err, 0, sizeof(int)));
+  return st;
 }
 
 int mf_process_set_timing(mf_process* p, int enable) {

@@ -9,7 +9,7 @@ struct IterArgs;
                             const signed char** hh);                                                        \
   int64_t mf_prep_bytes_k##KK(int prec);                                                                     \
   int mf_launch_me_k##KK(int prec, const int4* prep, int64_t N, const double* skip, double* out,             \
-                         double* hel_out, cudaStream_t st);                                                 \
+                         double* hel_out, int* err, cudaStream_t st);                                       \
   int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,  \
                            int64_t cstride, int4* prep, cudaStream_t st);                                   \
   int mf_launch_ps_k##KK(int prec, const IterArgs& A, cudaStream_t st);                                     \
@@ -35,11 +35,11 @@ inline int64_t mf_prep_bytes(int k, int prec) {
   }
 }
 inline int mf_launch_me(int k, int prec, const int4* prep, int64_t N, const double* skip, double* out,
-                        double* hel_out, cudaStream_t st) {
+                        double* hel_out, int* err, cudaStream_t st) {
   switch (k) {
-    case 2: return mf_launch_me_k2(prec, prep, N, skip, out, hel_out, st);
-    case 3: return mf_launch_me_k3(prec, prep, N, skip, out, hel_out, st);
-    case 4: return mf_launch_me_k4(prec, prep, N, skip, out, hel_out, st);
+    case 2: return mf_launch_me_k2(prec, prep, N, skip, out, hel_out, err, st);
+    case 3: return mf_launch_me_k3(prec, prep, N, skip, out, hel_out, err, st);
+    case 4: return mf_launch_me_k4(prec, prep, N, skip, out, hel_out, err, st);
   }
   return 3;
 }

@@ -333,8 +333,13 @@ template <class T, int K> struct RecSmem {
   RecWS<T, K> ws;
   PrepRec<T, K> pr;
   double red[MF_REC_NT / 32];
+  unsigned long long mbar;  // tensor-core colour stage: MMA completion
+  uint32_t tmem;            // its tensor-memory accumulator
+  int tc_err;               // a bounded wait ran out
 };
 template <class T, int K> MF_HD constexpr int prep_words() { return (int)(sizeof(PrepRec<T, K>) / 16); }
+
+#include "mf_colour_tc.cuh"
 
 #ifdef __CUDACC__
 // Per-event records from momenta ps [K+2][4][N] and couplings [N or 1][3]
@@ -359,15 +364,42 @@ __global__ void __launch_bounds__(128) prep_kernel(const double* __restrict__ ps
 // Block-per-event |M|^2 from the per-event records prep [N][prep_words];
 // skip (optional) [N]: events with skip[e] == 0 get out[e] = 0 without work;
 // out [N]; hel_out (optional) [ncomb][N] in MadGraph helicity order.
+// FP32 processes with a tensor-core colour operand take the colour sum on
+// the tensor cores (mf_colour_tc.cuh); err (optional) gets bit 0 set, and the
+// remaining events of the block NaN, if a wait on the tensor cores ran out.
+template <class T, int K> constexpr bool use_colour_tc() {
+  return MF_TCGEN05 && TcTraits<K>::enabled && sizeof(T) == 4 && (2 << (K + 2)) == 128 &&
+         MF_REC_NT >= 128;
+}
 template <int K, class T>
-__global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2) me_rec_kernel(const int4* __restrict__ prep, int64_t N,
-                                                          const double* __restrict__ skip, double* __restrict__ out,
-                                                          double* __restrict__ hel_out) {
+__global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
+    me_rec_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
+                  double* __restrict__ out, double* __restrict__ hel_out, int* __restrict__ err) {
   using R = RecTraits<K>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr bool TC = use_colour_tc<T, K>();
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
   RecSmem<T, K>& S = *reinterpret_cast<RecSmem<T, K>*>(smem_raw);
   const int tid = threadIdx.x, nt = blockDim.x;
   constexpr int NW = prep_words<T, K>();
+#if MF_TCGEN05
+  // operands in the shared memory of the top-line currents and t~ rows,
+  // which are dead once the amplitudes are complete
+  float* tc_region = nullptr;
+  uint32_t phase = 0;
+  if constexpr (TC) {
+    static_assert(sizeof(S.ws.O) + sizeof(S.ws.RW) >= (size_t)tc_operand_bytes<K>() + 128, "operand space");
+    uintptr_t o = reinterpret_cast<uintptr_t>(&S.ws.O);
+    tc_region = reinterpret_cast<float*>((o + 127) & ~(uintptr_t)127);
+    if (tid < 32) tc_tmem_alloc(&S.tmem, 32);
+    if (tid == 0) {
+      tc_mbar_init(&S.mbar, 1);
+      S.tc_err = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+  }
+#endif
   for (int64_t e = blockIdx.x; e < N; e += gridDim.x) {
     if (skip && skip[e] == 0.0) {
       if (tid == 0) out[e] = 0.0;
@@ -386,7 +418,62 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2) me_rec_kern
     }
     rec_st_A<T, K>(S.ws, tid, nt);
     __syncthreads();
-    double part = rec_st_colour<T, K>(S.ws, tid, nt);
+    double part = 0.0;
+    bool bad = false;
+#if MF_TCGEN05
+    if constexpr (TC) {
+      constexpr int NP = R::NPERM, NC = 1 << (K + 2);
+      tc_fill<K>(S.ws, tc_region, tid, nt);
+      tc_fence_proxy_async();
+      __syncthreads();
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t b = tc_smem_u32(tc_region);
+        const uint32_t hi = b + TcTraits<K>::N * NP * 4, lo = hi + 2 * NC * NP * 4;
+        constexpr uint32_t idesc = tc_idesc_tf32(2 * NC, TcTraits<K>::N);
+        constexpr uint32_t L = TcTraits<K>::LBO, SB = TcTraits<K>::SBO;
+#pragma unroll
+        for (int s = 0; s < NP / 8; ++s)
+          tc_mma_tf32(S.tmem, tc_smem_desc(hi + 256 * s, L, SB), tc_smem_desc(b + 256 * s, L, SB), idesc, s > 0);
+#pragma unroll
+        for (int s = 0; s < NP / 8; ++s)
+          tc_mma_tf32(S.tmem, tc_smem_desc(lo + 256 * s, L, SB), tc_smem_desc(b + 256 * s, L, SB), idesc, 1);
+        tc_commit(&S.mbar);
+      }
+      if (tid < 2 * NC) {
+        // bounded, warp-uniform wait (the accumulator loads are warp-collective)
+        bool done = false;
+        for (uint32_t spin = 0; spin < (1u << 22); ++spin) {
+          done = tc_mbar_try_wait(&S.mbar, phase);
+          if (__all_sync(0xffffffffu, done)) break;
+        }
+        done = __all_sync(0xffffffffu, done);
+        if (done) {
+          tc_fence_after();
+          float d[32];
+          const uint32_t ta = S.tmem + ((uint32_t)(32 * (tid >> 5)) << 16);
+          tc_ld_x16(ta, d);
+          tc_ld_x8(ta + 16, d + 16);
+          tc_wait_ld();
+          const int c = tid % NC, im = tid / NC;
+          float acc = 0.0f;
+#pragma unroll
+          for (int t = 0; t < NP; ++t) {
+            const cx<float> a = S.ws.A[t * NC + c];
+            acc += d[t] * (im ? a.im : a.re);
+          }
+          part = (double)acc;
+        } else {
+          S.tc_err = 1;
+        }
+        tc_fence_before();
+      }
+      phase ^= 1u;
+    } else
+#endif
+    {
+      part = rec_st_colour<T, K>(S.ws, tid, nt);
+    }
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((tid & 31) == 0) S.red[tid >> 5] = part;
     const double sc = S.pr.scale;
@@ -394,11 +481,28 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2) me_rec_kern
       for (int c = tid; c < (1 << (K + 2)); c += nt)
         hel_out[(int64_t)R::cfg_to_mg(c) * N + e] = rec_colour_one<T, K>(S.ws, c) * sc * R::DENOMINATOR;
     __syncthreads();
+    if constexpr (TC) bad = S.tc_err != 0;
     if (tid == 0) {
       double tot = 0.0;
       for (int w = 0; w < nt / 32; ++w) tot += S.red[w];
-      out[e] = tot * sc;
+      out[e] = bad ? __longlong_as_double(0x7ff8000000000000ll) : tot * sc;
+      if (bad && err) atomicOr(err, 1);
+    }
+    if (bad) break;
+  }
+#if MF_TCGEN05
+  if constexpr (TC) {
+    __syncthreads();
+    if (S.tc_err) {
+      // let an unfinished MMA drain (bounded) before its accumulator is freed
+      bool done = false;
+      for (uint32_t spin = 0; spin < (1u << 22) && !done; ++spin) done = tc_mbar_try_wait(&S.mbar, phase ^ 1u);
+    }
+    if (tid < 32) {
+      tc_fence_after();
+      tc_tmem_dealloc(S.tmem, 32);
     }
   }
+#endif
 }
 #endif

@@ -25,7 +25,7 @@ static int sm_count() {
     *hh = &ttng##KK::hel_h[0][0];                                                                              \
   }                                                                                                            \
   template <class T> static int me_rec_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out,  \
-                                                    double* hel_out, cudaStream_t st) {                           \
+                                                    double* hel_out, int* err, cudaStream_t st) {                 \
     const void* fn = (const void*)me_rec_kernel<KK, T>;                                                        \
     int bytes = rec_smem_bytes<KK, T>();                                                                       \
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                              \
@@ -35,16 +35,16 @@ static int sm_count() {
     int64_t g = (int64_t)sm_count() * per * 8;                                                                 \
     if (g > N) g = N;                                                                                          \
     if (g < 1) g = 1;                                                                                          \
-    me_rec_kernel<KK, T><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out);                       \
+    me_rec_kernel<KK, T><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out, err);                  \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }                                                                                                            \
   int64_t mf_prep_bytes_k##KK(int prec) {                                                                      \
     return prec == 0 ? (int64_t)sizeof(PrepRec<double, KK>) : (int64_t)sizeof(PrepRec<float, KK>);           \
   }                                                                                                            \
   int mf_launch_me_k##KK(int prec, const int4* prep, int64_t N, const double* skip, double* out,               \
-                         double* hel_out, cudaStream_t st) {                                                   \
-    return prec == 0 ? me_rec_launch_k##KK<double>(prep, N, skip, out, hel_out, st)                           \
-                     : me_rec_launch_k##KK<float>(prep, N, skip, out, hel_out, st);                           \
+                         double* hel_out, int* err, cudaStream_t st) {                                         \
+    return prec == 0 ? me_rec_launch_k##KK<double>(prep, N, skip, out, hel_out, err, st)                      \
+                     : me_rec_launch_k##KK<float>(prep, N, skip, out, hel_out, err, st);                      \
   }                                                                                                            \
   int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,    \
                            int64_t cstride, int4* prep, cudaStream_t st) {                                     \

@@ -360,3 +360,29 @@ def test_stage_timing(cuda):
     assert set(ms) == {"seed", "phase_space", "matrix_element", "accumulate"}
     assert all(v >= 0.0 for v in ms.values()) and ms["matrix_element"] > 0.0
     assert torch.equal(f0, f1)
+
+
+def test_colour_tensor_core_vs_simt(cuda, oracle):
+    """g g > t t~ g g in FP32: the colour sum on the tensor cores (TF32 split,
+    the total) against the FP32 SIMT colour sum of the same amplitudes (the
+    per-helicity outputs) and against the FP64 oracle; no tensor-core wait
+    ran out."""
+    import ctypes
+
+    from madflow_gb300 import _lib
+    from madflow_gb300.matrix import PROCESSES
+
+    rng = np.random.default_rng(77)
+    x = rng.uniform(size=(4099, 18))
+    p, *_ = oracle.ramboflow(x, 6, 13000.0, [MT, MT, 0.0, 0.0])
+    m = PROCESSES[4](precision=1)
+    tot, hel = m.smatrix_per_helicity(p, MT, WT, GC10, GC11, GC12)
+    tot, hel = _np(tot), _np(hel)
+    simt = hel.sum(axis=0) / 512.0
+    assert rel_err(tot, simt) < 1e-5
+    T = oracle.TTNG(4)
+    ref = T.smatrix(p[:257], T.params(MT, WT, GC10, GC11, GC12))
+    assert rel_err(tot[:257], ref) < 1e-4
+    flags = ctypes.c_int(-1)
+    _lib.call("mf_process_error_flags", m.handle, ctypes.byref(flags), 1)
+    assert flags.value == 0

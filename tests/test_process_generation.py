@@ -82,3 +82,22 @@ def test_generated_per_helicity_vs_oracle(host_lib, oracle, k):
     host_lib.me_host_helicities(k, _dp(np.ascontiguousarray(p[0])), _dp(coup), ctypes.c_double(MT),
                                 ctypes.c_double(WT), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     np.testing.assert_allclose(out, ref[:, 0], rtol=1e-11, atol=1e-14 * np.abs(ref).max())
+
+
+def test_colour_tc_operand_layout():
+    """The tensor-core B operand holds C^T in the canonical K-major layout
+    (8-row x 16-byte core matrices, LBO 128 bytes, SBO NPERM/4 x 128 bytes),
+    every element once, padding rows zero."""
+    num, _ = codegen.colour_matrix(4)
+    npad, flat = codegen.colour_tc_operand(4)
+    n = len(num)
+    assert npad == 32 and len(flat) == npad * n
+    sbo, lbo = (n // 4) * 32, 32
+    seen = set()
+    for r in range(npad):
+        for c in range(n):
+            off = (r // 8) * sbo + (c // 4) * lbo + (r % 8) * 4 + (c % 4)
+            assert off not in seen
+            seen.add(off)
+            assert flat[off] == (num[c][r] if r < n else 0.0)
+    assert len(seen) == len(flat)
