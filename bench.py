@@ -193,6 +193,8 @@ def run_gpu(args):
     per_launch = [REC_FLOPS[4] * int(n) for n in npass.tolist()]
     achieved = sum(per_launch) / (sum(me_ms) / 1000.0) / 1e12
     stages = {k: statistics.mean(d[k] for d in stage_ms) for k in stage_ms[0]}
+    # the autotuner ran on the first (warm-up) iteration
+    tune = integ.tuning()
 
     # end to end: the integrand contract f(x) with host buffers, copies timed
     e2e_n = min(N, args.e2e_events)
@@ -237,12 +239,13 @@ def run_gpu(args):
         # per step: set-int, phase-space first pass, phase space, matrix element, accumulate, reduce, refine
         "gpu_launches": 7 * args.steps,
         "stage_ms": stages,
+        "autotune": dict(tune, variants="index colour*4 + log2(waves); colour 0 SIMT, 1 tensor cores (tcgen05 TF32)"),
         "e2e": {"value": e2e_rate, "unit": "|M|^2 evals/s", "h2d_bytes_per_step": int(x_host.numel() * 8),
                 "d2h_bytes_per_step": int(f_host.numel() * 8), "api": "FusedIntegrand(x) -> f, host buffers",
                 "events_per_step": e2e_n},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
                      "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": None,
-                     "kernel": "me_rec_kernel<4,float>",
+                     "kernel": "me_rec_kernel<4,float,%d>" % tune["colour"],
                      "peak_source": "nominal FP32 SIMT (152 SMs x 128 lanes x 2 x 2.07 GHz); "
                                     "MEASURED_PEAKS.json holds no FP32 figure",
                      "flops_per_event": REC_FLOPS[4],

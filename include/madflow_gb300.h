@@ -159,6 +159,24 @@ int mf_vegas_iteration(const mf_process* proc, const mf_integrand_config* cfg, c
 #define MF_STAGES 4
 int mf_process_set_timing(mf_process* proc, int enable);
 
+/* Autotuner of the matrix-element launch (no counterpart in the reference).
+ * On the first call of mf_smatrix / mf_integrand / mf_vegas_iteration with at
+ * least 262144 events that is not being captured into a CUDA graph, the
+ * matrix-element kernel is timed with CUDA events on that call's own events
+ * (up to 2^20) in MF_TUNE_VARIANTS variants -- colour sum on the SIMT lanes
+ * (colour 0) or on the tensor cores (colour 1, FP32 processes with 24 colour
+ * flows) x a grid of 1, 2, 4 or 8 waves of resident blocks -- and the fastest
+ * is kept by the handle.  MF_AUTOTUNE=0 in the environment keeps the default
+ * (colour 1 where available, 8 waves).  mf_process_tuning reports the
+ * configuration, whether it was tuned, and (ms, optional, MF_TUNE_VARIANTS
+ * floats) the time of each variant in milliseconds, index colour*4 +
+ * log2(waves), -1 for variants that do not exist; mf_process_set_tuning
+ * fixes a configuration (MF_ERR_UNSUPPORTED for tensor cores where there is
+ * no such variant). */
+#define MF_TUNE_VARIANTS 8
+int mf_process_tuning(const mf_process* proc, int* colour, int* waves, int* tuned, float* ms);
+int mf_process_set_tuning(mf_process* proc, int colour, int waves);
+
 /* Device error flags the handle's kernels raised (no counterpart in the
  * reference): bit 0 = a bounded wait on the tensor cores ran out (the
  * affected events got NaN).  Synchronous device-to-host read; clear != 0

@@ -19,6 +19,7 @@ c_dp = ctypes.c_void_p  # device pointers are passed as integers
 
 MF_OK, MF_ERR_ARG, MF_ERR_CUDA, MF_ERR_UNSUPPORTED, MF_ERR_CAPACITY, MF_ERR_NONFINITE, MF_ERR_STATE = range(7)
 MF_STAGES = 4
+MF_TUNE_VARIANTS = 8
 MF_PREC_FP64, MF_PREC_MIXED = 0, 1
 MF_NEWTON_BATCH, MF_NEWTON_PER_EVENT = 0, 1
 
@@ -79,6 +80,9 @@ _SIGS = {
     "mf_vegas_accumulate": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
     "mf_process_set_timing": (c_int, [c_void_p, c_int]),
     "mf_process_error_flags": (c_int, [c_void_p, ctypes.POINTER(c_int), c_int]),
+    "mf_process_tuning": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                  ctypes.POINTER(ctypes.c_float)]),
+    "mf_process_set_tuning": (c_int, [c_void_p, c_int, c_int]),
     "mf_process_stage_ms": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float)]),
     "mf_vegas_accumulate_noalloc": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
     "mf_vegas_refine": (c_int, [c_dp, c_dp, c_int, c_int, c_double, c_void_p]),

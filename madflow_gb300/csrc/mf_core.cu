@@ -3,6 +3,7 @@
 // integrand/iteration drivers.  Per-process matrix-element kernels live in
 // mf_proc_k<K>.cu.
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -429,6 +430,10 @@ struct mf_process {
   unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
   int64_t event_cap = 0;
   int* d_err = nullptr;     // device error flags of the kernels (bit 0: a tensor-core wait ran out)
+  // matrix-element launch configuration and the autotuner's record
+  MeTune tune = {1, 8};
+  bool tuned = false;
+  float tune_ms[MF_TUNE_VARIANTS] = {};
   // optional stage timing of the fused iteration (events on the caller's stream)
   int timing = 0;
   bool timed_last = false;
@@ -439,6 +444,8 @@ static const int kDiagrams[6] = {0, 0, 3, 16, 123, 1240};
 
 extern "C" {
 static int ensure_events(mf_process* p, int64_t N);
+static bool autotune_wanted(const mf_process* p, int64_t N, void* stream);
+static int autotune_me(mf_process* p, const int4* prep, int64_t N, const double* skip, double* out, void* stream);
 
 const char* mf_version(void) { return "madflow_gb300 0.1 (sm_103a)"; }
 
@@ -527,7 +534,11 @@ int mf_smatrix(const mf_process* p, const double* ps, int64_t N, double mt, doub
   int st = ensure_events(pm, N);
   if (st) return st;
   if (mf_launch_prep(p->k, p->prec, ps, N, mt, wt, coup, cstride, pm->d_prep, S(stream))) return last_launch();
-  st = mf_launch_me(p->k, p->prec, pm->d_prep, N, nullptr, out, hel_out, pm->d_err, S(stream));
+  if (autotune_wanted(pm, N, stream)) {
+    st = autotune_me(pm, pm->d_prep, N, nullptr, out, stream);
+    if (st) return st;
+  }
+  st = mf_launch_me(p->k, p->prec, pm->d_prep, N, nullptr, out, hel_out, pm->d_err, pm->tune, S(stream));
   if (st == 3) return MF_ERR_UNSUPPORTED;
   return st ? last_launch() : MF_OK;
 }
@@ -695,6 +706,65 @@ static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, Ite
   return pdf_device_table(A.pdf);
 }
 
+// ---- autotuner of the matrix-element launch ----------------------------------
+// On the first uncaptured call with at least kTuneMinEvents events the
+// matrix-element kernel is timed (CUDA events, the caller's stream, the
+// call's own records, up to kTuneEvents of them) in every variant: colour sum
+// on the SIMT lanes or the tensor cores x grid of 1, 2, 4 or 8 waves of
+// resident blocks; the fastest becomes the handle's configuration.
+// MF_AUTOTUNE=0 in the environment keeps the defaults (tensor cores, 8 waves).
+static const int kTuneWaves[4] = {1, 2, 4, 8};
+static const int64_t kTuneMinEvents = 262144, kTuneEvents = 1 << 20;
+
+static bool autotune_wanted(const mf_process* p, int64_t N, void* stream) {
+  if (p->tuned || N < kTuneMinEvents) return false;
+  const char* env = getenv("MF_AUTOTUNE");
+  if (env && env[0] == '0') return false;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(S(stream), &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return false;
+  return true;
+}
+
+static int autotune_me(mf_process* p, const int4* prep, int64_t N, const double* skip, double* out, void* stream) {
+  int64_t n = N < kTuneEvents ? N : kTuneEvents;
+  cudaEvent_t a = nullptr, b = nullptr;
+  int st = cuda_status(cudaEventCreate(&a));
+  if (!st) st = cuda_status(cudaEventCreate(&b));
+  float best = 0.0f;
+  MeTune pick = p->tune;
+  bool have = false;
+  for (int c = 0; c < 2 && !st; ++c) {
+    if (c == 1 && (p->prec == MF_PREC_FP64 || !mf_colour_tc(p->k))) {
+      for (int w = 0; w < 4; ++w) p->tune_ms[4 * c + w] = -1.0f;
+      continue;
+    }
+    for (int w = 0; w < 4 && !st; ++w) {
+      MeTune t = {c, kTuneWaves[w]};
+      float ms = 0.0f;
+      for (int rep = 0; rep < 2 && !st; ++rep) {  // the first launch of a variant is a warm-up
+        st = cuda_status(cudaEventRecord(a, S(stream)));
+        if (!st && mf_launch_me(p->k, p->prec, prep, n, skip, out, nullptr, p->d_err, t, S(stream))) st = last_launch();
+        if (!st) st = cuda_status(cudaEventRecord(b, S(stream)));
+        if (!st) st = cuda_status(cudaEventSynchronize(b));
+        if (!st) st = cuda_status(cudaEventElapsedTime(&ms, a, b));
+      }
+      if (st) break;
+      p->tune_ms[4 * c + w] = ms;
+      if (!have || ms < best) {
+        best = ms;
+        pick = t;
+        have = true;
+      }
+    }
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (st) return st;
+  p->tune = pick;
+  p->tuned = true;
+  return MF_OK;
+}
+
 static int ensure_events(mf_process* p, int64_t N) {
   if (!p->d_err) {
     int st = cuda_status(cudaMalloc(&p->d_err, sizeof(int)));
@@ -770,7 +840,12 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   mark(1);
   if (mf_launch_ps(p->k, p->prec, A, S(stream))) return last_launch();
   mark(2);
-  if (mf_launch_me(p->k, p->prec, A.prep, A.N, A.pref, A.me, nullptr, p->d_err, S(stream))) return last_launch();
+  if (autotune_wanted(p, A.N, stream)) {
+    st = autotune_me(p, A.prep, A.N, A.pref, A.me, stream);
+    if (st) return st;
+  }
+  if (mf_launch_me(p->k, p->prec, A.prep, A.N, A.pref, A.me, nullptr, p->d_err, p->tune, S(stream)))
+    return last_launch();
   mark(3);
   size_t shm = (size_t)(A.ndim * A.nb + 2 * 256) * sizeof(double);
   cudaFuncSetAttribute(accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
@@ -780,6 +855,24 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
     reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(p->d_partials, accum_grid, width, results);
   mark(4);
   return last_launch();
+}
+
+int mf_process_tuning(const mf_process* p, int* colour, int* waves, int* tuned, float* ms) {
+  if (!p) return MF_ERR_ARG;
+  if (colour) *colour = p->tune.colour;
+  if (waves) *waves = p->tune.waves;
+  if (tuned) *tuned = p->tuned ? 1 : 0;
+  if (ms)
+    for (int i = 0; i < MF_TUNE_VARIANTS; ++i) ms[i] = p->tune_ms[i];
+  return MF_OK;
+}
+
+int mf_process_set_tuning(mf_process* p, int colour, int waves) {
+  if (!p || (colour != 0 && colour != 1) || (waves != 1 && waves != 2 && waves != 4 && waves != 8)) return MF_ERR_ARG;
+  if (colour == 1 && (p->prec == MF_PREC_FP64 || !mf_colour_tc(p->k))) return MF_ERR_UNSUPPORTED;
+  p->tune = {colour, waves};
+  p->tuned = true;
+  return MF_OK;
 }
 
 int mf_process_error_flags(mf_process* p, int* flags, int clear) {

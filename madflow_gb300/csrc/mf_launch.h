@@ -4,12 +4,20 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 struct IterArgs;
+// Launch configuration of the matrix-element kernel (chosen by the
+// autotuner): colour sum on the SIMT lanes (0) or the tensor cores (1), and
+// the grid as `waves` x (SMs x resident blocks per SM).
+struct MeTune {
+  int colour;
+  int waves;
+};
 #define MF_DECLARE_PROCESS(KK)                                                                              \
   void mf_host_tables_k##KK(int* nperm, int* ncomb, double* den, double* cden, const float** cn,             \
                             const signed char** hh);                                                        \
   int64_t mf_prep_bytes_k##KK(int prec);                                                                     \
   int mf_launch_me_k##KK(int prec, const int4* prep, int64_t N, const double* skip, double* out,             \
-                         double* hel_out, int* err, cudaStream_t st);                                       \
+                         double* hel_out, int* err, MeTune t, cudaStream_t st);                             \
+  bool mf_colour_tc_k##KK();                                                                                 \
   int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,  \
                            int64_t cstride, int4* prep, cudaStream_t st);                                   \
   int mf_launch_ps_k##KK(int prec, const IterArgs& A, cudaStream_t st);                                     \
@@ -35,13 +43,21 @@ inline int64_t mf_prep_bytes(int k, int prec) {
   }
 }
 inline int mf_launch_me(int k, int prec, const int4* prep, int64_t N, const double* skip, double* out,
-                        double* hel_out, int* err, cudaStream_t st) {
+                        double* hel_out, int* err, MeTune t, cudaStream_t st) {
   switch (k) {
-    case 2: return mf_launch_me_k2(prec, prep, N, skip, out, hel_out, err, st);
-    case 3: return mf_launch_me_k3(prec, prep, N, skip, out, hel_out, err, st);
-    case 4: return mf_launch_me_k4(prec, prep, N, skip, out, hel_out, err, st);
+    case 2: return mf_launch_me_k2(prec, prep, N, skip, out, hel_out, err, t, st);
+    case 3: return mf_launch_me_k3(prec, prep, N, skip, out, hel_out, err, t, st);
+    case 4: return mf_launch_me_k4(prec, prep, N, skip, out, hel_out, err, t, st);
   }
   return 3;
+}
+// whether the process has a tensor-core colour variant (FP32)
+inline bool mf_colour_tc(int k) {
+  switch (k) {
+    case 2: return mf_colour_tc_k2();
+    case 3: return mf_colour_tc_k3();
+    default: return mf_colour_tc_k4();
+  }
 }
 inline int mf_launch_prep(int k, int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,
                           int64_t cstride, int4* prep, cudaStream_t st) {

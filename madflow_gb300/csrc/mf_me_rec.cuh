@@ -364,19 +364,20 @@ __global__ void __launch_bounds__(128) prep_kernel(const double* __restrict__ ps
 // Block-per-event |M|^2 from the per-event records prep [N][prep_words];
 // skip (optional) [N]: events with skip[e] == 0 get out[e] = 0 without work;
 // out [N]; hel_out (optional) [ncomb][N] in MadGraph helicity order.
-// FP32 processes with a tensor-core colour operand take the colour sum on
-// the tensor cores (mf_colour_tc.cuh); err (optional) gets bit 0 set, and the
-// remaining events of the block NaN, if a wait on the tensor cores ran out.
+// COLOUR = 1: FP32 processes with a tensor-core colour operand take the
+// colour sum on the tensor cores (mf_colour_tc.cuh); err (optional) gets bit
+// 0 set, and the remaining events of the block NaN, if a wait on the tensor
+// cores ran out.  COLOUR = 0: the register-tiled SIMT colour sum.
 template <class T, int K> constexpr bool use_colour_tc() {
   return MF_TCGEN05 && TcTraits<K>::enabled && sizeof(T) == 4 && (2 << (K + 2)) == 128 &&
          MF_REC_NT >= 128;
 }
-template <int K, class T>
+template <int K, class T, int COLOUR>
 __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     me_rec_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
                   double* __restrict__ out, double* __restrict__ hel_out, int* __restrict__ err) {
   using R = RecTraits<K>;
-  constexpr bool TC = use_colour_tc<T, K>();
+  constexpr bool TC = COLOUR == 1 && use_colour_tc<T, K>();
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   RecSmem<T, K>& S = *reinterpret_cast<RecSmem<T, K>*>(smem_raw);
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -400,17 +401,25 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     tc_fence_after();
   }
 #endif
-  for (int64_t e = blockIdx.x; e < N; e += gridDim.x) {
-    if (skip && skip[e] == 0.0) {
+  // the next event of this block that needs work (events with skip == 0
+  // get out = 0 on the way), and the loading of its record + external slots
+  auto next_event = [&](int64_t e) {
+    while (e < N && skip && skip[e] == 0.0) {
       if (tid == 0) out[e] = 0.0;
-      continue;
+      e += gridDim.x;
     }
-    __syncthreads();
+    return e;
+  };
+  auto load_ext = [&](int64_t e) {
     int4* dst = reinterpret_cast<int4*>(&S.pr);
     const int4* src = prep + e * NW;
     for (int w = tid; w < NW; w += nt) dst[w] = src[w];
     __syncthreads();
     rec_st_ext<T, K>(S.ws, S.pr, tid, nt);
+  };
+  int64_t e = next_event(blockIdx.x);
+  if (e < N) load_ext(e);
+  while (e < N) {
     __syncthreads();
     for (int st = 1; st < K; ++st) {
       rec_stage<T, K>(S.ws, S.pr.ev, st, tid, nt);
@@ -418,6 +427,8 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     }
     rec_st_A<T, K>(S.ws, tid, nt);
     __syncthreads();
+    const double sc = S.pr.scale;
+    const int64_t en = next_event(e + gridDim.x);
     double part = 0.0;
     bool bad = false;
 #if MF_TCGEN05
@@ -440,6 +451,10 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
           tc_mma_tf32(S.tmem, tc_smem_desc(lo + 256 * s, L, SB), tc_smem_desc(b + 256 * s, L, SB), idesc, 1);
         tc_commit(&S.mbar);
       }
+      // while the tensor cores work: the next event's record and external
+      // slots (its record, the gluon slots of J and the quark spinors; none
+      // of them is an MMA operand or read by this event's epilogue)
+      if (en < N) load_ext(en);
       if (tid < 2 * NC) {
         // bounded, warp-uniform wait (the accumulator loads are warp-collective)
         bool done = false;
@@ -476,7 +491,6 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     }
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((tid & 31) == 0) S.red[tid >> 5] = part;
-    const double sc = S.pr.scale;
     if (hel_out)
       for (int c = tid; c < (1 << (K + 2)); c += nt)
         hel_out[(int64_t)R::cfg_to_mg(c) * N + e] = rec_colour_one<T, K>(S.ws, c) * sc * R::DENOMINATOR;
@@ -489,6 +503,9 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
       if (bad && err) atomicOr(err, 1);
     }
     if (bad) break;
+    if constexpr (!TC)
+      if (en < N) load_ext(en);
+    e = en;
   }
 #if MF_TCGEN05
   if constexpr (TC) {

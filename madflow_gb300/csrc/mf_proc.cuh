@@ -24,27 +24,36 @@ static int sm_count() {
     *cn = ttng##KK::colour_num_h;                                                                              \
     *hh = &ttng##KK::hel_h[0][0];                                                                              \
   }                                                                                                            \
-  template <class T> static int me_rec_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out,  \
-                                                    double* hel_out, int* err, cudaStream_t st) {                 \
-    const void* fn = (const void*)me_rec_kernel<KK, T>;                                                        \
+  template <class T, int COLOUR>                                                                               \
+  static int me_rec_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out, double* hel_out, \
+                                 int* err, int waves, cudaStream_t st) {                                       \
+    const void* fn = (const void*)me_rec_kernel<KK, T, COLOUR>;                                                \
+    const void* fn0 = (const void*)me_rec_kernel<KK, T, 0>;                                                    \
     int bytes = rec_smem_bytes<KK, T>();                                                                       \
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                              \
+    cudaFuncSetAttribute(fn0, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                             \
+    /* resident blocks per SM from the SIMT variant: the same registers and  */                                \
+    /* shared memory (the occupancy query reports 1 for kernels that         */                                \
+    /* allocate tensor memory, although 4 blocks x 32 columns fit)           */                                \
     int per = 0;                                                                                               \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, MF_REC_NT, bytes);                                 \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn0, MF_REC_NT, bytes);                                \
     if (per < 1) per = 1;                                                                                      \
-    int64_t g = (int64_t)sm_count() * per * 8;                                                                 \
+    int64_t g = (int64_t)sm_count() * per * (waves > 0 ? waves : 1);                                           \
     if (g > N) g = N;                                                                                          \
     if (g < 1) g = 1;                                                                                          \
-    me_rec_kernel<KK, T><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out, err);                  \
+    me_rec_kernel<KK, T, COLOUR><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out, err);          \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }                                                                                                            \
   int64_t mf_prep_bytes_k##KK(int prec) {                                                                      \
     return prec == 0 ? (int64_t)sizeof(PrepRec<double, KK>) : (int64_t)sizeof(PrepRec<float, KK>);           \
   }                                                                                                            \
+  bool mf_colour_tc_k##KK() { return TcTraits<KK>::enabled; }                                                  \
   int mf_launch_me_k##KK(int prec, const int4* prep, int64_t N, const double* skip, double* out,               \
-                         double* hel_out, int* err, cudaStream_t st) {                                         \
-    return prec == 0 ? me_rec_launch_k##KK<double>(prep, N, skip, out, hel_out, err, st)                      \
-                     : me_rec_launch_k##KK<float>(prep, N, skip, out, hel_out, err, st);                      \
+                         double* hel_out, int* err, MeTune t, cudaStream_t st) {                               \
+    if (prec == 0) return me_rec_launch_k##KK<double, 0>(prep, N, skip, out, hel_out, err, t.waves, st);      \
+    if constexpr (TcTraits<KK>::enabled)                                                                       \
+      if (t.colour == 1) return me_rec_launch_k##KK<float, 1>(prep, N, skip, out, hel_out, err, t.waves, st); \
+    return me_rec_launch_k##KK<float, 0>(prep, N, skip, out, hel_out, err, t.waves, st);                      \
   }                                                                                                            \
   int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,    \
                            int64_t cstride, int4* prep, cudaStream_t st) {                                     \

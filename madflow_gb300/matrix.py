@@ -108,6 +108,18 @@ class MatrixTTNG:
                   out.data_ptr(), hel.data_ptr() if with_hel else None, stream_ptr())
         return out, hel
 
+    def tuning(self):
+        """Launch configuration of the matrix-element kernel (see
+        mf_process_tuning): dict(colour, waves, tuned, variant_ms)."""
+        c, w, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ms = (ctypes.c_float * _lib.MF_TUNE_VARIANTS)()
+        _lib.call("mf_process_tuning", self.handle, ctypes.byref(c), ctypes.byref(w), ctypes.byref(t), ms)
+        return dict(colour=c.value, waves=w.value, tuned=bool(t.value), variant_ms=[float(v) for v in ms])
+
+    def set_tuning(self, colour, waves):
+        """Fix the launch configuration (colour 0 SIMT / 1 tensor cores; waves 1, 2, 4, 8)."""
+        _lib.call("mf_process_set_tuning", self.handle, int(colour), int(waves))
+
     def smatrix(self, all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12=None):
         """|M|^2 averaged over initial and summed over final helicities and colours."""
         return self._run(all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12, False)[0]

@@ -75,6 +75,13 @@ class FusedIntegrand:
                   results.data_ptr(), f_out.data_ptr() if f_out is not None else None,
                   u_out.data_ptr() if u_out is not None else None, stream_ptr())
 
+    def tuning(self):
+        """The matrix-element launch configuration of the handle: colour sum
+        on the SIMT lanes (0) or tensor cores (1), grid waves, whether the
+        autotuner chose it, and the autotuner's time per variant in ms
+        (index colour*4 + log2(waves); -1 where a variant does not exist)."""
+        return self.matrix.tuning()
+
     def set_timing(self, enable=True):
         """Record CUDA events between the pipeline stages of later calls."""
         _lib.call("mf_process_set_timing", self.matrix.handle, int(bool(enable)))

@@ -386,3 +386,33 @@ def test_colour_tensor_core_vs_simt(cuda, oracle):
     flags = ctypes.c_int(-1)
     _lib.call("mf_process_error_flags", m.handle, ctypes.byref(flags), 1)
     assert flags.value == 0
+
+
+def test_autotuner(cuda):
+    """The first large enough call times every launch variant and keeps the
+    fastest; a fixed configuration is honoured and unsupported ones are
+    refused; results do not depend on the configuration."""
+    import torch
+
+    from madflow_gb300 import _lib
+    from madflow_gb300.vegas import FusedIntegrand
+
+    integ = FusedIntegrand(4, kind=1, sqrts=13000.0, ptmin=60.0, etamax=2.5, drmin=0.4, precision=1)
+    assert not integ.tuning()["tuned"]
+    x = torch.rand((300_000, integ.n_dim), dtype=torch.float64, device="cuda",
+                   generator=torch.Generator(device="cuda").manual_seed(9))
+    f_auto = integ(x)
+    t = integ.tuning()
+    assert t["tuned"]
+    ms = t["variant_ms"]
+    assert len(ms) == 8 and all(v > 0 for v in ms)
+    best = min(range(8), key=lambda i: ms[i])
+    assert (t["colour"], t["waves"]) == (best // 4, 1 << (best % 4))
+    for colour in (0, 1):
+        integ.matrix.set_tuning(colour, 2)
+        f = integ(x)
+        assert torch.allclose(f, f_auto, rtol=2e-5, atol=0.0)
+    fp64 = FusedIntegrand(2, kind=0, sqrts=1000.0, precision=0)
+    with pytest.raises(_lib.MadflowError):
+        fp64.matrix.set_tuning(1, 8)
+    assert fp64.tuning()["variant_ms"][4:] == [0.0] * 4 or not fp64.tuning()["tuned"]
