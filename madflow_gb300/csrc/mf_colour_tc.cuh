@@ -87,14 +87,16 @@ MF_DO void tc_mbar_init(unsigned long long* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem_u32(bar)), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-MF_DO bool tc_mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+// Waits for the phase of the given parity to complete, suspending the thread
+// for up to about `ns` nanoseconds (woken early when the phase completes).
+MF_DO bool tc_mbar_try_wait(unsigned long long* bar, uint32_t parity, uint32_t ns) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.b32 %0, 1, 0, p;\n\t}\n"
       : "=r"(ok)
-      : "r"(tc_smem_u32(bar)), "r"(parity)
+      : "r"(tc_smem_u32(bar)), "r"(parity), "r"(ns)
       : "memory");
   return ok != 0;
 }

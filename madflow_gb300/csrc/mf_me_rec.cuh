@@ -293,11 +293,11 @@ template <class T, int K, int PART, bool LAST = (PART == colour_parts<K>() - 1)>
 template <class T, int K, int PART> struct ColourDispatch<T, K, PART, true> {
   MF_D static T run(const RecWS<T, K>& ws, int c, int) { return colour_rows<T, K, PART>(ws, c); }
 };
-template <class T, int K> MF_D double rec_st_colour(const RecWS<T, K>& ws, int tid, int nt) {
+template <class T, int K> MF_D T rec_st_colour(const RecWS<T, K>& ws, int tid, int nt) {
   constexpr int NC = 1 << (K + 2), P = colour_parts<K>();
   T acc = T(0);
   for (int it = tid; it < NC * P; it += nt) acc += ColourDispatch<T, K, 0>::run(ws, it % NC, it / NC);
-  return (double)acc;
+  return acc;
 }
 
 // colour sum of one helicity combination c (per-helicity outputs)
@@ -322,7 +322,7 @@ template <class T, int K> struct RecHostRun {
       for (int t = 0; t < nt; ++t) rec_stage<T, K>(ws, pr.ev, st, t, nt);
     for (int t = 0; t < nt; ++t) rec_st_A<T, K>(ws, t, nt);
     double tot = 0.0;
-    for (int t = 0; t < nt; ++t) tot += rec_st_colour<T, K>(ws, t, nt);
+    for (int t = 0; t < nt; ++t) tot += (double)rec_st_colour<T, K>(ws, t, nt);
     return tot;
   }
 };
@@ -332,7 +332,7 @@ constexpr int MF_REC_NT = 192;  // threads per event block
 template <class T, int K> struct RecSmem {
   RecWS<T, K> ws;
   PrepRec<T, K> pr;
-  double red[MF_REC_NT / 32];
+  T red[MF_REC_NT / 32];
   unsigned long long mbar;  // tensor-core colour stage: MMA completion
   uint32_t tmem;            // its tensor-memory accumulator
   int tc_err;               // a bounded wait ran out
@@ -403,8 +403,9 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
 #endif
   // the next event of this block that needs work (events with skip == 0
   // get out = 0 on the way), and the loading of its record + external slots
+  // (the skip test on the bits: +-0.0, without the FP64 pipe)
   auto next_event = [&](int64_t e) {
-    while (e < N && skip && skip[e] == 0.0) {
+    while (e < N && skip && (__double_as_longlong(skip[e]) << 1) == 0) {
       if (tid == 0) out[e] = 0.0;
       e += gridDim.x;
     }
@@ -429,7 +430,7 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     __syncthreads();
     const double sc = S.pr.scale;
     const int64_t en = next_event(e + gridDim.x);
-    double part = 0.0;
+    T part = T(0);
     bool bad = false;
 #if MF_TCGEN05
     if constexpr (TC) {
@@ -457,9 +458,10 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
       if (en < N) load_ext(en);
       if (tid < 2 * NC) {
         // bounded, warp-uniform wait (the accumulator loads are warp-collective)
+        // (each try suspends for up to 1 ms; 1000 tries bound the wait to ~1 s)
         bool done = false;
-        for (uint32_t spin = 0; spin < (1u << 22); ++spin) {
-          done = tc_mbar_try_wait(&S.mbar, phase);
+        for (uint32_t spin = 0; spin < 1000u; ++spin) {
+          done = tc_mbar_try_wait(&S.mbar, phase, 1000000u);
           if (__all_sync(0xffffffffu, done)) break;
         }
         done = __all_sync(0xffffffffu, done);
@@ -477,7 +479,7 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
             const cx<float> a = S.ws.A[t * NC + c];
             acc += d[t] * (im ? a.im : a.re);
           }
-          part = (double)acc;
+          part = acc;
         } else {
           S.tc_err = 1;
         }
@@ -497,9 +499,9 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     __syncthreads();
     if constexpr (TC) bad = S.tc_err != 0;
     if (tid == 0) {
-      double tot = 0.0;
+      T tot = T(0);
       for (int w = 0; w < nt / 32; ++w) tot += S.red[w];
-      out[e] = bad ? __longlong_as_double(0x7ff8000000000000ll) : tot * sc;
+      out[e] = bad ? __longlong_as_double(0x7ff8000000000000ll) : (double)tot * sc;
       if (bad && err) atomicOr(err, 1);
     }
     if (bad) break;
@@ -513,7 +515,7 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     if (S.tc_err) {
       // let an unfinished MMA drain (bounded) before its accumulator is freed
       bool done = false;
-      for (uint32_t spin = 0; spin < (1u << 22) && !done; ++spin) done = tc_mbar_try_wait(&S.mbar, phase ^ 1u);
+      for (uint32_t spin = 0; spin < 1000u && !done; ++spin) done = tc_mbar_try_wait(&S.mbar, phase ^ 1u, 1000000u);
     }
     if (tid < 32) {
       tc_fence_after();
