@@ -147,6 +147,26 @@ int mf_vegas_iteration(const mf_process* proc, const mf_integrand_config* cfg, c
                        uint64_t seed, uint32_t stream_id, const int* iteration, int64_t n_events, double* results,
                        double* f_out, float* u_out, void* stream);
 
+/* Event output (device-side events for an LHE writer; replaces the
+ * per-iteration dump of lhe_writer.py:139-196, called from
+ * madflow_exec.py:460-464).  One iteration of the fused pipeline at
+ * `iteration` of the frozen grid, with, per event, f_out [N] = jac * f (0 for
+ * events failing the cuts, as in mf_vegas_iteration) and ps_out
+ * [N][nexternal][4] the lab-frame momenta (E, px, py, pz) madflow passes to
+ * its writer (PhaseSpaceGenerator(com_output=False)); zero rows for events
+ * failing the cuts.  The VEGAS event weight is f_out / N. */
+int mf_vegas_events(const mf_process* proc, const mf_integrand_config* cfg, const double* grid, int nbins,
+                    uint64_t seed, uint32_t stream_id, int iteration, int64_t n_events, double* f_out,
+                    double* ps_out, void* stream);
+
+/* Hit-or-miss unweighting on the device (replaces the MG5 lhe_parser
+ * unweight call of lhe_writer.py:316-358): keep[e] = 1 when u_e * w_max <
+ * |w_e|, u_e a Philox4x32-10 uniform of (seed, stream_id, event e), else 0.
+ * w [N] device, keep [N] device bytes.  Kept events with |w| > w_max are
+ * overweight (their relative weight is |w| / w_max). */
+int mf_unweight(const double* w, int64_t n_events, double w_max, uint64_t seed, uint32_t stream_id,
+                unsigned char* keep, void* stream);
+
 /* Stage timing of the fused pipeline behind mf_integrand / mf_vegas_iteration
  * (no counterpart in the reference).  With timing enabled, each call records
  * CUDA events on its stream between its stages; mf_process_stage_ms then

@@ -77,6 +77,9 @@ _SIGS = {
     "mf_integrand": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int64, c_dp, c_void_p]),
     "mf_vegas_iteration": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int, c_uint64, c_uint32, c_dp,
                                    c_int64, c_dp, c_dp, c_dp, c_void_p]),
+    "mf_vegas_events": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int, c_uint64, c_uint32, c_int,
+                                c_int64, c_dp, c_dp, c_void_p]),
+    "mf_unweight": (c_int, [c_dp, c_int64, c_double, c_uint64, c_uint32, c_void_p, c_void_p]),
     "mf_vegas_accumulate": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
     "mf_process_set_timing": (c_int, [c_void_p, c_int]),
     "mf_process_error_flags": (c_int, [c_void_p, ctypes.POINTER(c_int), c_int]),

@@ -423,6 +423,7 @@ struct mf_process {
   double* d_partials = nullptr;
   size_t partial_cap = 0;
   int* d_zero_iter = nullptr;
+  int* d_event_iter = nullptr;  // iteration index of mf_vegas_events
   int4* d_prep = nullptr;   // [cap] per-event matrix-element records
   double* d_state = nullptr; // [state words][cap] first-pass phase-space state
   double* d_pref = nullptr; // [cap]
@@ -492,6 +493,7 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_kmin) cudaFree(p->d_kmin);
   if (p->d_partials) cudaFree(p->d_partials);
   if (p->d_zero_iter) cudaFree(p->d_zero_iter);
+  if (p->d_event_iter) cudaFree(p->d_event_iter);
   if (p->d_prep) cudaFree(p->d_prep);
   if (p->d_state) cudaFree(p->d_state);
   if (p->d_pref) cudaFree(p->d_pref);
@@ -949,6 +951,55 @@ int mf_vegas_iteration(const mf_process* pc, const mf_integrand_config* c, const
   A.inv_n = 1.0 / (double)N;
   A.u_out = u_out;
   return run_fused(p, A, c, results, f_out, stream);
+}
+
+int mf_vegas_events(const mf_process* pc, const mf_integrand_config* c, const double* grid, int nb, uint64_t seed,
+                    uint32_t stream_id, int iteration, int64_t N, double* f_out, double* ps_out, void* stream) {
+  mf_process* p = const_cast<mf_process*>(pc);
+  int ndim = 0;
+  if (!p || !c || !grid || !f_out || !ps_out || N <= 0 || nb < 2 || nb > 255 || iteration < 0) return MF_ERR_ARG;
+  int st = mf_integrand_ndim(p, c, &ndim);
+  if (st) return st;
+  if (ndim > MF_MAX_DIM) return MF_ERR_CAPACITY;
+  IterArgs A;
+  st = fill_iter_args(p, c, A);
+  if (st) return st;
+  if (!p->d_event_iter) {
+    st = cuda_status(cudaMalloc(&p->d_event_iter, sizeof(int)));
+    if (st) return st;
+  }
+  set_int_kernel<<<1, 1, 0, S(stream)>>>(p->d_event_iter, iteration);
+  A.div = grid;
+  A.ndim = ndim;
+  A.nb = nb;
+  A.seed = seed;
+  A.stream = stream_id;
+  A.iteration = p->d_event_iter;
+  A.N = N;
+  A.inv_n = 1.0 / (double)N;
+  A.ps_out = ps_out;
+  return run_fused(p, A, c, nullptr, f_out, stream);
+}
+
+// Unweighting (hit or miss): event e is kept when u_e * w_max < |w_e|, u_e a
+// Philox uniform of (seed, stream, event).
+__global__ void unweight_kernel(const double* __restrict__ w, int64_t N, double wmax, uint64_t seed, uint32_t stream,
+                                unsigned char* __restrict__ keep) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double u0, u1;
+    philox_pair(seed, stream, 0xFFFFFFFFu, (uint64_t)e, 0, u0, u1);
+    keep[e] = (u0 * wmax < fabs(w[e])) ? 1 : 0;
+  }
+}
+
+int mf_unweight(const double* w, int64_t N, double w_max, uint64_t seed, uint32_t stream_id, unsigned char* keep,
+                void* stream) {
+  if (N < 0 || (N > 0 && (!w || !keep)) || !(w_max > 0.0)) return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  int64_t blocks = (N + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  unweight_kernel<<<(int)blocks, 256, 0, S(stream)>>>(w, N, w_max, seed, stream_id, keep);
+  return last_launch();
 }
 
 int mf_vegas_accumulate(const double* f, const double* jac, const int32_t* bins, int64_t N, int ndim, int nb,

@@ -41,6 +41,7 @@ struct IterArgs {
   int f32q;
   const double* x_in;  // optional [ndim][N] points (integrand API): no Philox / VEGAS map, jac = 1
   float* u_out;        // optional [ndim][N] uniforms
+  double* ps_out;      // optional [N][K+2][4] lab-frame momenta of the passing events (event output)
   // pipeline buffers (scratch)
   double* state;            // [4(K)+6][N] first-pass state (ps_state_words)
   int4* prep;              // [N] per-event records (PrepRec), passing events only
@@ -241,6 +242,15 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
     const double x2 = st[(int64_t)(4 * K + 4) * N], jac = st[(int64_t)(4 * K + 5) * N];
     bool ok = event_finish<T>(A, NPART, niter, p, logw, shat, wgt, x1, x2, v, pw, wl);
     A.pref[e] = ok ? jac * wl : 0.0;
+    if (A.ps_out) {
+      // madflow's all_ps (com_output=False): lab frame, FP64
+      double* q = A.ps_out + (int64_t)e * NPART * 4;
+      for (int i = 0; i < NPART; ++i) {
+        double t[4] = {p[i][0], p[i][1], p[i][2], p[i][3]};
+        if (A.kind != 0) boost_lab<double>(t, x1, x2);
+        for (int c = 0; c < 4; ++c) q[4 * i + c] = ok ? t[c] : 0.0;
+      }
+    }
     if (ok) {
       PrepRec<T, K> r;
       prep_event<T, K>(r, p, A.mt, A.wt, A.gc10, A.gc11, A.gc12);

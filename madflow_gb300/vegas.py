@@ -95,6 +95,34 @@ class FusedIntegrand:
         return dict(zip(("seed", "phase_space", "matrix_element", "accumulate"), list(ms)))
 
 
+def reduce_results(results, group=None):
+    """Sum an iteration's results vector [2 + ndim*nbins] (sum of w, of w^2,
+    per-bin w^2) over the ranks of a torch.distributed group, in place: the
+    one exchange of a sharded integration.  The vector stays on its device
+    for NCCL and goes through host memory for gloo."""
+    import torch.distributed as dist
+
+    if group is None and not dist.is_initialized():
+        return results
+    if dist.get_backend(group) == "nccl" or results.device.type == "cpu":
+        dist.all_reduce(results, op=dist.ReduceOp.SUM, group=group)
+        return results
+    host = results.cpu()
+    dist.all_reduce(host, op=dist.ReduceOp.SUM, group=group)
+    results.copy_(host)
+    return results
+
+
+def iteration_estimate(s1, s2, n_per_rank, world=1):
+    """(estimate, sigma) of one iteration from the summed w = f jac / n and
+    w^2 over world ranks of n events each: the mean of f jac over all
+    M = world*n events and the error of that mean."""
+    n, m = float(n_per_rank), float(n_per_rank) * world
+    res = s1 / world
+    var = n * n * (s2 - s1 * s1 / m) / (m * (m - 1.0))
+    return res, math.sqrt(max(var, 0.0))
+
+
 class VegasFlow:
     """VEGAS integrator (the vegasflow interface madflow calls).
 
@@ -104,12 +132,22 @@ class VegasFlow:
     """
 
     def __init__(self, n_dim, n_events, events_limit=None, seed=4, nbins=BINS_MAX, alpha=ALPHA, stream_id=0,
-                 verbose=False, use_graph=True):
+                 verbose=False, use_graph=True, process_group=None):
+        """process_group (torch.distributed, optional): shard every iteration
+        over the group's ranks, n_events on each (Philox stream
+        stream_id * world + rank), with one all-reduce of the results vector
+        per iteration; every rank then refines the same grid."""
         self.n_dim = int(n_dim)
         self.n_events = int(n_events)
         self.events_per_run = int(events_limit or n_events)
         self.seed = int(seed)
-        self.stream_id = int(stream_id)
+        self.group = process_group
+        self.world, self.rank = 1, 0
+        if process_group is not None:
+            import torch.distributed as dist
+
+            self.world, self.rank = dist.get_world_size(process_group), dist.get_rank(process_group)
+        self.stream_id = int(stream_id) * self.world + self.rank
         self.nbins = int(nbins)
         self.alpha = float(alpha)
         self.verbose = verbose
@@ -171,11 +209,27 @@ class VegasFlow:
                       stream_ptr())
         self.iteration += 1
 
+    def _refine(self):
+        _lib.call("mf_vegas_refine", self.grid.data_ptr(), self.results[2:].data_ptr(), self.n_dim, self.nbins,
+                  self.alpha, stream_ptr())
+
     def _iteration_fused_body(self):
         self.integrand.iteration(self.grid, self.seed, self.stream_id, self.iteration, self.n_events, self.results)
         if self.train:
-            _lib.call("mf_vegas_refine", self.grid.data_ptr(), self.results[2:].data_ptr(), self.n_dim, self.nbins,
-                      self.alpha, stream_ptr())
+            self._refine()
+        self.iteration += 1
+
+    def _iteration_sharded(self):
+        if isinstance(self.integrand, FusedIntegrand):
+            self.integrand.iteration(self.grid, self.seed, self.stream_id, self.iteration, self.n_events, self.results)
+        else:
+            train, self.train = self.train, False
+            self._iteration_python()
+            self.train = train
+            self.iteration -= 1
+        reduce_results(self.results, self.group)
+        if self.train:
+            self._refine()
         self.iteration += 1
 
     def _iteration_fused(self):
@@ -198,6 +252,10 @@ class VegasFlow:
         self._graph.replay()
 
     def run_event(self):
+        if self.group is not None:
+            self._iteration_sharded()
+            r = self.results[:2].double().cpu().numpy()
+            return iteration_estimate(float(r[0]), float(r[1]), self.n_events, self.world)
         if isinstance(self.integrand, FusedIntegrand):
             self._iteration_fused()
         else:
