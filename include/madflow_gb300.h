@@ -147,7 +147,18 @@ int mf_vegas_iteration(const mf_process* proc, const mf_integrand_config* cfg, c
                        uint64_t seed, uint32_t stream_id, const int* iteration, int64_t n_events, double* results,
                        double* f_out, float* u_out, void* stream);
 
-/* Event output (SURVEY 8f: device-side events for an LHE writer; replaces the
+/* Several processes in one persistent launch (no counterpart in the reference,
+ * which loops over its processes in Python, madflow_exec.py:444-455).
+ * procs [nproc] distinct handles of one precision, nproc <= 4; batch j:
+ * ps[j] [nexternal_j][4][n[j]] momenta (as mf_smatrix), out[j] [n[j]]
+ * |M|^2.  Couplings coup [6] (GC_10, GC_11, GC_12 as re, im) and the top
+ * mass and width are shared.  The events of all batches form one work list,
+ * the process with the most colour flows first; blocks take events from a
+ * global counter.  The colour sums run on the SIMT lanes. */
+int mf_smatrix_multi(mf_process* const* procs, int nproc, const double* const* ps, const int64_t* n, double mt,
+                     double wt, const double* coup, double* const* out, void* stream);
+
+/* Event output (device-side events for an LHE writer; replaces the
  * per-iteration dump of lhe_writer.py:139-196, called from
  * madflow_exec.py:460-464).  One iteration of the fused pipeline at
  * `iteration` of the frozen grid, with, per event, f_out [N] = jac * f (0 for

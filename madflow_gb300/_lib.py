@@ -77,6 +77,8 @@ _SIGS = {
     "mf_integrand": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int64, c_dp, c_void_p]),
     "mf_vegas_iteration": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int, c_uint64, c_uint32, c_dp,
                                    c_int64, c_dp, c_dp, c_dp, c_void_p]),
+    "mf_smatrix_multi": (c_int, [ctypes.POINTER(c_void_p), c_int, ctypes.POINTER(c_void_p),
+                                 ctypes.POINTER(c_int64), c_double, c_double, c_dp, ctypes.POINTER(c_void_p), c_void_p]),
     "mf_vegas_events": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int, c_uint64, c_uint32, c_int,
                                 c_int64, c_dp, c_dp, c_void_p]),
     "mf_unweight": (c_int, [c_dp, c_int64, c_double, c_uint64, c_uint32, c_void_p, c_void_p]),

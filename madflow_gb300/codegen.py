@@ -274,11 +274,11 @@ def emit_process_header(k):
     L.append(f"constexpr int NEXT = {k + 2};")
     L.append(f"constexpr double DENOMINATOR = {float(denominator(k))!r};")
     L.append(f"constexpr double COLOUR_DEN = {float(den)!r};")
-    L.append(f"__constant__ float colour_num[{n * n}] = {{")
+    L.append(f"static __constant__ float colour_num[{n * n}] = {{")
     for r in num:
         L.append("  " + ", ".join(f"{float(v)!r}f" for v in r) + ",")
     L.append("};")
-    L.append(f"__constant__ signed char hel[{len(hels)}][{k + 2}] = {{")
+    L.append(f"static __constant__ signed char hel[{len(hels)}][{k + 2}] = {{")
     for h in hels:
         L.append("  {" + ", ".join(str(int(v)) for v in h) + "},")
     L.append("};")

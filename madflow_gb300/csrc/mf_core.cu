@@ -2,6 +2,7 @@
 // handles, phase space, wavefunctions, ALOHA routines, VEGAS and the fused
 // integrand/iteration drivers.  Per-process matrix-element kernels live in
 // mf_proc_k<K>.cu.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
@@ -424,6 +425,7 @@ struct mf_process {
   size_t partial_cap = 0;
   int* d_zero_iter = nullptr;
   int* d_event_iter = nullptr;  // iteration index of mf_vegas_events
+  unsigned long long* d_counter = nullptr;  // work counter of multi-process launches
   int4* d_prep = nullptr;   // [cap] per-event matrix-element records
   double* d_state = nullptr; // [state words][cap] first-pass phase-space state
   double* d_pref = nullptr; // [cap]
@@ -494,6 +496,7 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_partials) cudaFree(p->d_partials);
   if (p->d_zero_iter) cudaFree(p->d_zero_iter);
   if (p->d_event_iter) cudaFree(p->d_event_iter);
+  if (p->d_counter) cudaFree(p->d_counter);
   if (p->d_prep) cudaFree(p->d_prep);
   if (p->d_state) cudaFree(p->d_state);
   if (p->d_pref) cudaFree(p->d_pref);
@@ -543,6 +546,54 @@ int mf_smatrix(const mf_process* p, const double* ps, int64_t N, double mt, doub
   st = mf_launch_me(p->k, p->prec, pm->d_prep, N, nullptr, out, hel_out, pm->d_err, pm->tune, S(stream));
   if (st == 3) return MF_ERR_UNSUPPORTED;
   return st ? last_launch() : MF_OK;
+}
+
+int mf_smatrix_multi(mf_process* const* procs, int nproc, const double* const* ps, const int64_t* n, double mt,
+                     double wt, const double* coup, double* const* out, void* stream) {
+  if (!procs || nproc < 1 || nproc > MF_MULTI_MAX || !ps || !n || !coup || !out) return MF_ERR_ARG;
+  int prec = -1;
+  for (int j = 0; j < nproc; ++j) {
+    if (!procs[j] || n[j] < 0 || (n[j] > 0 && (!ps[j] || !out[j]))) return MF_ERR_ARG;
+    if (prec >= 0 && procs[j]->prec != prec) return MF_ERR_ARG;
+    prec = procs[j]->prec;
+    for (int i = 0; i < j; ++i)
+      if (procs[i] == procs[j]) return MF_ERR_ARG;  // each handle holds one batch of records
+  }
+  // records of every batch (one thread per event each)
+  for (int j = 0; j < nproc; ++j) {
+    if (n[j] == 0) continue;
+    int st = ensure_events(procs[j], n[j]);
+    if (st) return st;
+    if (mf_launch_prep(procs[j]->k, prec, ps[j], n[j], mt, wt, coup, 0, procs[j]->d_prep, S(stream)))
+      return last_launch();
+  }
+  // the work list, most colour flows first
+  int order[MF_MULTI_MAX];
+  for (int j = 0; j < nproc; ++j) order[j] = j;
+  for (int a = 0; a < nproc; ++a)
+    for (int b = a + 1; b < nproc; ++b)
+      if (procs[order[b]]->k > procs[order[a]]->k) std::swap(order[a], order[b]);
+  MultiMe M;
+  std::memset(&M, 0, sizeof(M));
+  M.n = 0;
+  M.off[0] = 0;
+  for (int a = 0; a < nproc; ++a) {
+    int j = order[a];
+    if (n[j] == 0) continue;
+    M.k[M.n] = procs[j]->k;
+    M.prep[M.n] = procs[j]->d_prep;
+    M.out[M.n] = out[j];
+    M.off[M.n + 1] = M.off[M.n] + n[j];
+    ++M.n;
+  }
+  if (M.n == 0) return MF_OK;
+  mf_process* p0 = procs[order[0]];
+  if (!p0->d_counter) {
+    int st = cuda_status(cudaMalloc(&p0->d_counter, sizeof(unsigned long long)));
+    if (st) return st;
+  }
+  if (mf_launch_me_multi(prec, M, p0->d_counter, S(stream))) return last_launch();
+  return MF_OK;
 }
 
 // ---- phase space --------------------------------------------------------------

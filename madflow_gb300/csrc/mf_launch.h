@@ -11,6 +11,18 @@ struct MeTune {
   int colour;
   int waves;
 };
+// Work list of one multi-process launch: n processes, process j with k[j]
+// gluons, records prep[j], its events at list positions [off[j], off[j+1]),
+// results out[j].
+constexpr int MF_MULTI_MAX = 4;
+struct MultiMe {
+  int n;
+  int k[MF_MULTI_MAX];
+  const int4* prep[MF_MULTI_MAX];
+  int64_t off[MF_MULTI_MAX + 1];
+  double* out[MF_MULTI_MAX];
+};
+int mf_launch_me_multi(int prec, const MultiMe& M, unsigned long long* counter, cudaStream_t st);
 #define MF_DECLARE_PROCESS(KK)                                                                              \
   void mf_host_tables_k##KK(int* nperm, int* ncomb, double* den, double* cden, const float** cn,             \
                             const signed char** hh);                                                        \

@@ -361,6 +361,35 @@ __global__ void __launch_bounds__(128) prep_kernel(const double* __restrict__ ps
   }
 }
 
+// One event by the whole block with the SIMT colour sum (launches that mix
+// processes): record load, stages, amplitudes, colour sum, block reduction.
+// Returns |M|^2 in thread 0.
+template <class T, int K> MF_DO double me_rec_event(RecSmem<T, K>& S, const int4* __restrict__ rec, int tid, int nt) {
+  constexpr int NW = prep_words<T, K>();
+  int4* dst = reinterpret_cast<int4*>(&S.pr);
+  for (int w = tid; w < NW; w += nt) dst[w] = rec[w];
+  __syncthreads();
+  rec_st_ext<T, K>(S.ws, S.pr, tid, nt);
+  __syncthreads();
+  for (int st = 1; st < K; ++st) {
+    rec_stage<T, K>(S.ws, S.pr.ev, st, tid, nt);
+    __syncthreads();
+  }
+  rec_st_A<T, K>(S.ws, tid, nt);
+  __syncthreads();
+  T part = rec_st_colour<T, K>(S.ws, tid, nt);
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((tid & 31) == 0) S.red[tid >> 5] = part;
+  __syncthreads();
+  double r = 0.0;
+  if (tid == 0) {
+    T tot = T(0);
+    for (int w = 0; w < nt / 32; ++w) tot += S.red[w];
+    r = (double)tot * S.pr.scale;
+  }
+  return r;
+}
+
 // Block-per-event |M|^2 from the per-event records prep [N][prep_words];
 // skip (optional) [N]: events with skip[e] == 0 get out[e] = 0 without work;
 // out [N]; hel_out (optional) [ncomb][N] in MadGraph helicity order.

@@ -161,3 +161,35 @@ class Matrix_1_gg_ttxgg(MatrixTTNG):
 
 
 PROCESSES = {2: Matrix_1_gg_ttx, 3: Matrix_1_gg_ttxg, 4: Matrix_1_gg_ttxgg}
+
+
+def smatrix_multi(batches, mdl_MT, mdl_WT, GC_10, GC_11, GC_12=None):
+    """|M|^2 of several processes in one persistent launch (C ABI
+    ``mf_smatrix_multi``): batches is a list of (matrix, all_ps) with distinct
+    matrix objects of one precision; scalar couplings shared by all.  Returns
+    the list of results, one per batch."""
+    if not batches or len(batches) > 4:
+        raise ValueError("one to four batches")
+    handles, ptrs, ns, outs, keep = [], [], [], [], []
+    coup = None
+    for m, all_ps in batches:
+        ps = to_device(all_ps)
+        if ps.dim() != 3 or ps.shape[1] != m._proc.nexternal or ps.shape[2] != 4:
+            raise ValueError(f"all_ps must have shape (N, {m._proc.nexternal}, 4), got {tuple(ps.shape)}")
+        n = ps.shape[0]
+        soa = ps.permute(1, 2, 0).contiguous()
+        out = torch.empty(n, dtype=DTYPE, device=device())
+        c, stride = m._couplings(n, GC_10, GC_11, GC_12)
+        if stride != 0:
+            raise ValueError("smatrix_multi takes scalar couplings")
+        coup = c
+        keep += [soa, out]
+        handles.append(m.handle)
+        ptrs.append(soa.data_ptr())
+        ns.append(n)
+        outs.append(out)
+    k = len(batches)
+    _lib.call("mf_smatrix_multi", (ctypes.c_void_p * k)(*handles), k, (ctypes.c_void_p * k)(*ptrs),
+              (ctypes.c_int64 * k)(*ns), float(mdl_MT), float(mdl_WT), coup.data_ptr(),
+              (ctypes.c_void_p * k)(*[o.data_ptr() for o in outs]), stream_ptr())
+    return outs

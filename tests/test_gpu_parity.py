@@ -416,3 +416,26 @@ def test_autotuner(cuda):
     with pytest.raises(_lib.MadflowError):
         fp64.matrix.set_tuning(1, 8)
     assert fp64.tuning()["variant_ms"][4:] == [0.0] * 4 or not fp64.tuning()["tuned"]
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_smatrix_multi_process_launch(cuda, oracle, prec):
+    """g g > t t~, t t~ g and t t~ g g batches of uneven sizes in one
+    persistent launch give the single-process results (FP64: the same bits;
+    mixed: within 1e-5, the single-process g g > t t~ g g colour sum runs on
+    the tensor cores)."""
+    from madflow_gb300.matrix import PROCESSES, smatrix_multi
+
+    rng = np.random.default_rng(90)
+    batches, singles = [], []
+    for k, n in ((2, 1001), (3, 517), (4, 333)):
+        x = rng.uniform(size=(n, 4 * k + 2))
+        p, *_ = oracle.ramboflow(x, k + 2, 13000.0, [MT, MT] + [0.0] * (k - 2))
+        batches.append((PROCESSES[k](precision=prec), p))
+        singles.append(_np(PROCESSES[k](precision=prec).smatrix(p, MT, WT, GC10, GC11, GC12)))
+    outs = [_np(o) for o in smatrix_multi(batches, MT, WT, GC10, GC11, GC12)]
+    for o, s in zip(outs, singles):
+        if prec == 0:
+            assert np.array_equal(o, s)
+        else:
+            assert rel_err(o, s) < 1e-5
