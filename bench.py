@@ -355,7 +355,8 @@ def time_to_target(args, target=1e-3):
     def flow_run(flow, grid, prior, target_, max_batches, train_batches):
         return adaptive_flow_integration(flow, integ, target_rel_error=target_, batch_size=args.flow_batch,
                                          max_batches=max_batches, lr=args.flow_lr, train_batches=train_batches,
-                                         minibatch=args.flow_minibatch, grid=grid, prior=prior)
+                                         minibatch=args.flow_minibatch, grid=grid, prior=prior,
+                                         resample=args.flow_resample)
 
     # untimed warm-up of the flow's kernels and GEMM shapes
     flow_run(make_flow(), None, None, 0.0, 2, 1)
@@ -378,7 +379,8 @@ def time_to_target(args, target=1e-3):
                          "result_pb": res, "error_pb": err, "rel_error": err / abs(res) if res else None,
                          "reached": bool(res and err / abs(res) <= target),
                          "flow": f"{args.flow_layers} piecewise-quadratic coupling layers, 16 bins, "
-                                 f"MLP 2x{args.flow_hidden} (bf16 cuBLAS), lr {args.flow_lr}, on a frozen VEGAS grid",
+                                 f"MLP 2x{args.flow_hidden} (bf16 cuBLAS), lr {args.flow_lr}, on a frozen VEGAS grid, "
+                                 f"trained on {args.flow_resample} events per batch resampled with probability w^2",
                          "last_std_over_mean": info["last_rel_std"]}
     return out
 
@@ -463,9 +465,10 @@ def main():
     ap.add_argument("--flow-layers", type=int, default=6)
     ap.add_argument("--flow-hidden", type=int, default=64)
     ap.add_argument("--flow-batch", type=int, default=2_000_000)
-    ap.add_argument("--flow-minibatch", type=int, default=500_000)
-    ap.add_argument("--flow-lr", type=float, default=2e-3)
-    ap.add_argument("--flow-train-batches", type=int, default=10)
+    ap.add_argument("--flow-minibatch", type=int, default=50_000)
+    ap.add_argument("--flow-resample", type=int, default=200_000)
+    ap.add_argument("--flow-lr", type=float, default=5e-3)
+    ap.add_argument("--flow-train-batches", type=int, default=20)
     ap.add_argument("--flow-vegas-iters", type=int, default=5)
     ap.add_argument("--flow-vegas-events", type=int, default=4_000_000)
     ap.add_argument("--precision-points", type=int, default=1_000_000)

@@ -142,8 +142,30 @@ def _clamp_open(x, eps=1e-7):
     return x.clamp(eps, 1.0 - eps)
 
 
-def _train_step(flow, opt, x, w, minibatch):
-    """Variance-loss updates on one batch (x, w = f/q) drawn from the flow."""
+def _train_step(flow, opt, x, w, minibatch, resample=0):
+    """Variance-loss updates on one batch (x, w = f/q) drawn from the flow.
+
+    The gradient of Var(f/q) is -E_q[w^2 d log q] (score function).  With
+    resample > 0 it is estimated from `resample` events drawn with
+    probability w^2 / sum w^2 (systematic resampling), as
+    -(sum w^2) mean(d log q) over them: unbiased, and only the resampled
+    events go through the flow's log-density and its backward pass."""
+    if resample > 0:
+        w2 = (w * w).double()
+        total = float(w2.sum())
+        if total <= 0.0:
+            return
+        cdf = torch.cumsum(w2, 0) / total
+        u = (torch.arange(resample, device=w.device, dtype=torch.float64) + torch.rand(1, device=w.device,
+                                                                                      dtype=torch.float64)) / resample
+        idx = torch.clamp(torch.searchsorted(cdf, u), max=w.numel() - 1)
+        xs = x[idx]
+        for s in range(0, resample, minibatch):
+            loss = -flow.log_prob(xs[s: s + minibatch]).mean()
+            opt.zero_grad(set_to_none=True)
+            loss.backward()
+            opt.step()
+        return
     mean_w = w.mean()
     scale = (mean_w * mean_w).clamp_min(1e-300)
     n = x.shape[0]
@@ -187,7 +209,8 @@ def _vegas_map(grid, z):
 
 
 def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size=1_000_000, max_batches=200,
-                              train_batches=30, minibatch=100_000, lr=2e-3, seed=99, grid=None, prior=None):
+                              train_batches=30, minibatch=100_000, lr=2e-3, seed=99, grid=None, prior=None,
+                              resample=0):
     """Integrate while training: every batch is drawn from the current (frozen)
     flow, so mean(f/q) over it is an unbiased estimate with variance
     var(f/q)/n; the estimates of all batches are combined with
@@ -199,7 +222,8 @@ def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size
     the density of the grid's input variables, x = G(z), and the weights are
     f(G(z)) |dG/dz| / q(z).  prior (optional): (wsum, wres) of earlier
     unbiased estimates (e.g. the VEGAS iterations that adapted the grid), in
-    the same inverse-variance form.
+    the same inverse-variance form.  resample > 0: train on that many events
+    resampled with probability w^2 (see _train_step).
 
     Returns (result, error, info)."""
     opt = torch.optim.Adam(flow.parameters(), lr=lr)
@@ -224,7 +248,7 @@ def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size
             if cur != 0 and (1.0 / math.sqrt(wsum)) / abs(cur) <= target_rel_error:
                 break
         if b < train_batches:
-            _train_step(flow, opt, z, w, minibatch)
+            _train_step(flow, opt, z, w, minibatch, resample)
     info = {"batches": b + 1, "trained": min(b + 1, int(train_batches)), "last_rel_std": rel_std}
     if wsum == 0:
         return 0.0, 0.0, info
