@@ -110,10 +110,12 @@ def test_flow_training_reduces_variance(cuda):
     assert hist[-1] < 0.5 * hist[0]
 
 
-def test_adaptive_flow_integration(cuda):
+@pytest.mark.parametrize("resample", [0, 20_000])
+def test_adaptive_flow_integration(cuda, resample):
     """Training batches double as estimates: the combined result of a
     normalised bump agrees with its integral within the quoted error, and the
-    quoted error reaches the target."""
+    quoted error reaches the target (training on all events, or on events
+    resampled with probability w^2)."""
     import math
 
     import torch
@@ -128,7 +130,8 @@ def test_adaptive_flow_integration(cuda):
 
     flow = NormalizingFlow(3, n_layers=4, bins=16, hidden=32, seed=2)
     res, err, info = adaptive_flow_integration(flow, bump, target_rel_error=3e-3, batch_size=50_000,
-                                               max_batches=60, train_batches=20, minibatch=25_000, lr=5e-3)
+                                               max_batches=60, train_batches=20, minibatch=10_000 if resample else 25_000,
+                                               lr=5e-3, resample=resample)
     assert err / res <= 3e-3
     assert abs(res - 1.0) < 4 * err
     assert info["batches"] <= 60
