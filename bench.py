@@ -32,11 +32,11 @@ CUTS = dict(ptmin=60.0, etamax=2.5, drmin=0.4)
 # (all helicities, no sharing across helicities; complex mul 6, add 2,
 # div/sqrt/log 1), counted by the oracle's counting scalar
 # (tests/test_flop_counts.py keeps these in step with it).
-ALG_FLOPS = {2: 23601.0, 3: 356161.0, 4: 5744961.0}
+ALG_FLOPS = {2: 23601.0, 3: 356161.0, 4: 5744961.0, 5: 102333185.0}
 # Flops per phase-space point the helicity-recycling kernel executes (same
 # counting convention), counted by running its stage functions with the
 # counting scalar (tests/test_flop_counts.py).
-REC_FLOPS = {2: 5817.0, 3: 58190.0, 4: 745707.0}
+REC_FLOPS = {2: 5817.0, 3: 58190.0, 4: 745707.0, 5: 13242912.0}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max clock
 
 

@@ -474,7 +474,7 @@ def emit_program(k):
     return "\n".join(L)
 
 
-def write_generated(outdir, ks=(2, 3, 4)):
+def write_generated(outdir, ks=(2, 3, 4, 5)):
     import os
 
     os.makedirs(outdir, exist_ok=True)

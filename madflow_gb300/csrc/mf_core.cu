@@ -426,6 +426,7 @@ struct mf_process {
   int* d_zero_iter = nullptr;
   int* d_event_iter = nullptr;  // iteration index of mf_vegas_events
   unsigned long long* d_counter = nullptr;  // work counter of multi-process launches
+  void* d_ws = nullptr;     // global matrix-element workspace (processes too large for shared memory)
   int4* d_prep = nullptr;   // [cap] per-event matrix-element records
   double* d_state = nullptr; // [state words][cap] first-pass phase-space state
   double* d_pref = nullptr; // [cap]
@@ -470,7 +471,7 @@ const char* mf_last_cuda_error(void) { return g_cuda_err.c_str(); }
 int mf_process_create(int n_gluons, int precision, mf_process** out) {
   if (!out) return MF_ERR_ARG;
   *out = nullptr;
-  if (n_gluons < 2 || n_gluons > 4) return MF_ERR_UNSUPPORTED;
+  if (n_gluons < 2 || n_gluons > 5) return MF_ERR_UNSUPPORTED;
   if (precision != MF_PREC_FP64 && precision != MF_PREC_MIXED) return MF_ERR_ARG;
   auto* p = new mf_process();
   p->k = n_gluons;
@@ -497,6 +498,7 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_zero_iter) cudaFree(p->d_zero_iter);
   if (p->d_event_iter) cudaFree(p->d_event_iter);
   if (p->d_counter) cudaFree(p->d_counter);
+  if (p->d_ws) cudaFree(p->d_ws);
   if (p->d_prep) cudaFree(p->d_prep);
   if (p->d_state) cudaFree(p->d_state);
   if (p->d_pref) cudaFree(p->d_pref);
@@ -543,7 +545,7 @@ int mf_smatrix(const mf_process* p, const double* ps, int64_t N, double mt, doub
     st = autotune_me(pm, pm->d_prep, N, nullptr, out, stream);
     if (st) return st;
   }
-  st = mf_launch_me(p->k, p->prec, pm->d_prep, N, nullptr, out, hel_out, pm->d_err, pm->tune, S(stream));
+  st = mf_launch_me(p->k, p->prec, pm->d_prep, N, nullptr, out, hel_out, pm->d_err, pm->tune, pm->d_ws, S(stream));
   if (st == 3) return MF_ERR_UNSUPPORTED;
   return st ? last_launch() : MF_OK;
 }
@@ -554,6 +556,7 @@ int mf_smatrix_multi(mf_process* const* procs, int nproc, const double* const* p
   int prec = -1;
   for (int j = 0; j < nproc; ++j) {
     if (!procs[j] || n[j] < 0 || (n[j] > 0 && (!ps[j] || !out[j]))) return MF_ERR_ARG;
+    if (procs[j]->k > 4) return MF_ERR_UNSUPPORTED;  // the shared-memory evaluation only
     if (prec >= 0 && procs[j]->prec != prec) return MF_ERR_ARG;
     prec = procs[j]->prec;
     for (int i = 0; i < j; ++i)
@@ -771,6 +774,7 @@ static const int64_t kTuneMinEvents = 262144, kTuneEvents = 1 << 20;
 
 static bool autotune_wanted(const mf_process* p, int64_t N, void* stream) {
   if (p->tuned || N < kTuneMinEvents) return false;
+  if (mf_ws_bytes(p->k, p->prec) > 0) return false;  // one launch form only
   const char* env = getenv("MF_AUTOTUNE");
   if (env && env[0] == '0') return false;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -796,7 +800,8 @@ static int autotune_me(mf_process* p, const int4* prep, int64_t N, const double*
       float ms = 0.0f;
       for (int rep = 0; rep < 2 && !st; ++rep) {  // the first launch of a variant is a warm-up
         st = cuda_status(cudaEventRecord(a, S(stream)));
-        if (!st && mf_launch_me(p->k, p->prec, prep, n, skip, out, nullptr, p->d_err, t, S(stream))) st = last_launch();
+        if (!st && mf_launch_me(p->k, p->prec, prep, n, skip, out, nullptr, p->d_err, t, p->d_ws, S(stream)))
+          st = last_launch();
         if (!st) st = cuda_status(cudaEventRecord(b, S(stream)));
         if (!st) st = cuda_status(cudaEventSynchronize(b));
         if (!st) st = cuda_status(cudaEventElapsedTime(&ms, a, b));
@@ -822,6 +827,11 @@ static int ensure_events(mf_process* p, int64_t N) {
   if (!p->d_err) {
     int st = cuda_status(cudaMalloc(&p->d_err, sizeof(int)));
     if (!st) st = cuda_status(cudaMemset(p->d_err, 0, sizeof(int)));
+    if (st) return st;
+  }
+  const int64_t wsb = mf_ws_bytes(p->k, p->prec);
+  if (wsb > 0 && !p->d_ws) {
+    int st = cuda_status(cudaMalloc(&p->d_ws, (size_t)wsb));
     if (st) return st;
   }
   if (p->event_cap >= N) return MF_OK;
@@ -897,7 +907,7 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
     st = autotune_me(p, A.prep, A.N, A.pref, A.me, stream);
     if (st) return st;
   }
-  if (mf_launch_me(p->k, p->prec, A.prep, A.N, A.pref, A.me, nullptr, p->d_err, p->tune, S(stream)))
+  if (mf_launch_me(p->k, p->prec, A.prep, A.N, A.pref, A.me, nullptr, p->d_err, p->tune, p->d_ws, S(stream)))
     return last_launch();
   mark(3);
   size_t shm = (size_t)(A.ndim * A.nb + 2 * 256) * sizeof(double);

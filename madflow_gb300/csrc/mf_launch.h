@@ -28,7 +28,8 @@ int mf_launch_me_multi(int prec, const MultiMe& M, unsigned long long* counter, 
                             const signed char** hh);                                                        \
   int64_t mf_prep_bytes_k##KK(int prec);                                                                     \
   int mf_launch_me_k##KK(int prec, const int4* prep, int64_t N, const double* skip, double* out,             \
-                         double* hel_out, int* err, MeTune t, cudaStream_t st);                             \
+                         double* hel_out, int* err, MeTune t, void* ws, cudaStream_t st);                   \
+  int64_t mf_ws_bytes_k##KK(int prec);                                                                       \
   bool mf_colour_tc_k##KK();                                                                                 \
   int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,  \
                            int64_t cstride, int4* prep, cudaStream_t st);                                   \
@@ -38,37 +39,51 @@ int mf_launch_me_multi(int prec, const MultiMe& M, unsigned long long* counter, 
 MF_DECLARE_PROCESS(2)
 MF_DECLARE_PROCESS(3)
 MF_DECLARE_PROCESS(4)
+MF_DECLARE_PROCESS(5)
 
 inline void mf_host_tables(int k, int* nperm, int* ncomb, double* den, double* cden, const float** cn,
                            const signed char** hh) {
   switch (k) {
     case 2: mf_host_tables_k2(nperm, ncomb, den, cden, cn, hh); break;
     case 3: mf_host_tables_k3(nperm, ncomb, den, cden, cn, hh); break;
-    default: mf_host_tables_k4(nperm, ncomb, den, cden, cn, hh); break;
+    case 4: mf_host_tables_k4(nperm, ncomb, den, cden, cn, hh); break;
+    default: mf_host_tables_k5(nperm, ncomb, den, cden, cn, hh); break;
   }
 }
 inline int64_t mf_prep_bytes(int k, int prec) {
   switch (k) {
     case 2: return mf_prep_bytes_k2(prec);
     case 3: return mf_prep_bytes_k3(prec);
-    default: return mf_prep_bytes_k4(prec);
+    case 4: return mf_prep_bytes_k4(prec);
+    default: return mf_prep_bytes_k5(prec);
   }
 }
 inline int mf_launch_me(int k, int prec, const int4* prep, int64_t N, const double* skip, double* out,
-                        double* hel_out, int* err, MeTune t, cudaStream_t st) {
+                        double* hel_out, int* err, MeTune t, void* ws, cudaStream_t st) {
   switch (k) {
-    case 2: return mf_launch_me_k2(prec, prep, N, skip, out, hel_out, err, t, st);
-    case 3: return mf_launch_me_k3(prec, prep, N, skip, out, hel_out, err, t, st);
-    case 4: return mf_launch_me_k4(prec, prep, N, skip, out, hel_out, err, t, st);
+    case 2: return mf_launch_me_k2(prec, prep, N, skip, out, hel_out, err, t, ws, st);
+    case 3: return mf_launch_me_k3(prec, prep, N, skip, out, hel_out, err, t, ws, st);
+    case 4: return mf_launch_me_k4(prec, prep, N, skip, out, hel_out, err, t, ws, st);
+    case 5: return mf_launch_me_k5(prec, prep, N, skip, out, hel_out, err, t, ws, st);
   }
   return 3;
+}
+// bytes of global workspace the matrix-element launch of a process needs (0: shared memory only)
+inline int64_t mf_ws_bytes(int k, int prec) {
+  switch (k) {
+    case 2: return mf_ws_bytes_k2(prec);
+    case 3: return mf_ws_bytes_k3(prec);
+    case 4: return mf_ws_bytes_k4(prec);
+    default: return mf_ws_bytes_k5(prec);
+  }
 }
 // whether the process has a tensor-core colour variant (FP32)
 inline bool mf_colour_tc(int k) {
   switch (k) {
     case 2: return mf_colour_tc_k2();
     case 3: return mf_colour_tc_k3();
-    default: return mf_colour_tc_k4();
+    case 4: return mf_colour_tc_k4();
+    default: return mf_colour_tc_k5();
   }
 }
 inline int mf_launch_prep(int k, int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,
@@ -77,6 +92,7 @@ inline int mf_launch_prep(int k, int prec, const double* ps, int64_t N, double m
     case 2: return mf_launch_prep_k2(prec, ps, N, mt, wt, coup, cstride, prep, st);
     case 3: return mf_launch_prep_k3(prec, ps, N, mt, wt, coup, cstride, prep, st);
     case 4: return mf_launch_prep_k4(prec, ps, N, mt, wt, coup, cstride, prep, st);
+    case 5: return mf_launch_prep_k5(prec, ps, N, mt, wt, coup, cstride, prep, st);
   }
   return 3;
 }
@@ -85,6 +101,7 @@ inline int mf_launch_ps(int k, int prec, const IterArgs& A, cudaStream_t st) {
     case 2: return mf_launch_ps_k2(prec, A, st);
     case 3: return mf_launch_ps_k3(prec, A, st);
     case 4: return mf_launch_ps_k4(prec, A, st);
+    case 5: return mf_launch_ps_k5(prec, A, st);
   }
   return 3;
 }
@@ -92,7 +109,8 @@ inline int64_t mf_state_words(int k) {
   switch (k) {
     case 2: return mf_state_words_k2();
     case 3: return mf_state_words_k3();
-    default: return mf_state_words_k4();
+    case 4: return mf_state_words_k4();
+    default: return mf_state_words_k5();
   }
 }
 inline int mf_launch_seed(int k, int prec, const IterArgs& A, int* kmin, int batch_rule, cudaStream_t st) {
@@ -100,6 +118,7 @@ inline int mf_launch_seed(int k, int prec, const IterArgs& A, int* kmin, int bat
     case 2: return mf_launch_seed_k2(prec, A, kmin, batch_rule, st);
     case 3: return mf_launch_seed_k3(prec, A, kmin, batch_rule, st);
     case 4: return mf_launch_seed_k4(prec, A, kmin, batch_rule, st);
+    case 5: return mf_launch_seed_k5(prec, A, kmin, batch_rule, st);
   }
   return 3;
 }

@@ -293,11 +293,31 @@ template <class T, int K, int PART, bool LAST = (PART == colour_parts<K>() - 1)>
 template <class T, int K, int PART> struct ColourDispatch<T, K, PART, true> {
   MF_D static T run(const RecWS<T, K>& ws, int c, int) { return colour_rows<T, K, PART>(ws, c); }
 };
-template <class T, int K> MF_D T rec_st_colour(const RecWS<T, K>& ws, int tid, int nt) {
-  constexpr int NC = 1 << (K + 2), P = colour_parts<K>();
+// Colour sum for many flows (120 for five gluons): an item is one row a and
+// one helicity combination c, z = sum_{b>a} C_ab A_b(c); neighbouring threads
+// take neighbouring c, so C_ab is the same across a warp.
+template <class T, int K> MF_D T rec_st_colour_rows(const RecWS<T, K>& ws, int tid, int nt) {
+  using R = RecTraits<K>;
+  constexpr int NP = R::NPERM, NC = 1 << (K + 2);
   T acc = T(0);
-  for (int it = tid; it < NC * P; it += nt) acc += ColourDispatch<T, K, 0>::run(ws, it % NC, it / NC);
+  for (int it = tid; it < NC * NP; it += nt) {
+    const int a = it / NC, c = it % NC;
+    cx<T> z = {T(0), T(0)};
+    for (int b = a + 1; b < NP; ++b) z += (T)R::colour(a * NP + b) * ws.A[b * NC + c];
+    const cx<T> Aa = ws.A[it];
+    acc += (T)R::colour(a * NP + a) * (Aa.re * Aa.re + Aa.im * Aa.im) + T(2) * (Aa.re * z.re + Aa.im * z.im);
+  }
   return acc;
+}
+template <class T, int K> MF_D T rec_st_colour(const RecWS<T, K>& ws, int tid, int nt) {
+  if constexpr (RecTraits<K>::NPERM > 24) {
+    return rec_st_colour_rows<T, K>(ws, tid, nt);
+  } else {
+    constexpr int NC = 1 << (K + 2), P = colour_parts<K>();
+    T acc = T(0);
+    for (int it = tid; it < NC * P; it += nt) acc += ColourDispatch<T, K, 0>::run(ws, it % NC, it / NC);
+    return acc;
+  }
 }
 
 // colour sum of one helicity combination c (per-helicity outputs)
@@ -388,6 +408,58 @@ template <class T, int K> MF_DO double me_rec_event(RecSmem<T, K>& S, const int4
     r = (double)tot * S.pr.scale;
   }
   return r;
+}
+
+// Processes whose workspace does not fit in shared memory (five gluons: 523
+// KB in FP32) keep it in global memory, one per block (ws [gridDim]); the
+// record and the reduction stay in shared memory.  Same stages, SIMT colour
+// sum, same outputs as me_rec_kernel.
+template <class T, int K> struct RecSmemG {
+  PrepRec<T, K> pr;
+  T red[MF_REC_NT / 32];
+};
+template <int K, class T>
+__global__ void __launch_bounds__(MF_REC_NT)
+    me_gws_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
+                  double* __restrict__ out, double* __restrict__ hel_out, RecWS<T, K>* __restrict__ ws_all) {
+  using R = RecTraits<K>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  RecSmemG<T, K>& S = *reinterpret_cast<RecSmemG<T, K>*>(smem_raw);
+  RecWS<T, K>& ws = ws_all[blockIdx.x];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  constexpr int NW = prep_words<T, K>();
+  for (int64_t e = blockIdx.x; e < N; e += gridDim.x) {
+    if (skip && (__double_as_longlong(skip[e]) << 1) == 0) {
+      if (tid == 0) out[e] = 0.0;
+      continue;
+    }
+    __syncthreads();
+    int4* dst = reinterpret_cast<int4*>(&S.pr);
+    const int4* src = prep + e * NW;
+    for (int w = tid; w < NW; w += nt) dst[w] = src[w];
+    __syncthreads();
+    rec_st_ext<T, K>(ws, S.pr, tid, nt);
+    __syncthreads();
+    for (int st = 1; st < K; ++st) {
+      rec_stage<T, K>(ws, S.pr.ev, st, tid, nt);
+      __syncthreads();
+    }
+    rec_st_A<T, K>(ws, tid, nt);
+    __syncthreads();
+    T part = rec_st_colour<T, K>(ws, tid, nt);
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((tid & 31) == 0) S.red[tid >> 5] = part;
+    const double sc = S.pr.scale;
+    if (hel_out)
+      for (int c = tid; c < (1 << (K + 2)); c += nt)
+        hel_out[(int64_t)R::cfg_to_mg(c) * N + e] = rec_colour_one<T, K>(ws, c) * sc * R::DENOMINATOR;
+    __syncthreads();
+    if (tid == 0) {
+      T tot = T(0);
+      for (int w = 0; w < nt / 32; ++w) tot += S.red[w];
+      out[e] = (double)tot * sc;
+    }
+  }
 }
 
 // Block-per-event |M|^2 from the per-event records prep [N][prep_words];

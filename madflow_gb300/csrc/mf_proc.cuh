@@ -5,6 +5,10 @@
 #include "mf_me.cuh"
 
 template <int K, class T> static int rec_smem_bytes() { return (int)sizeof(RecSmem<T, K>); }
+// whether the block-per-event workspace of a process fits in shared memory
+template <int K, class T> constexpr bool rec_in_smem() { return sizeof(RecSmem<T, K>) <= 200 * 1024; }
+// blocks of the global-workspace kernel per SM (its workspaces are allocated per block)
+constexpr int MF_GWS_PER_SM = 2;
 
 static int sm_count() {
   int dev = 0, sms = 0;
@@ -48,12 +52,35 @@ static int sm_count() {
     return prec == 0 ? (int64_t)sizeof(PrepRec<double, KK>) : (int64_t)sizeof(PrepRec<float, KK>);           \
   }                                                                                                            \
   bool mf_colour_tc_k##KK() { return TcTraits<KK>::enabled; }                                                  \
+  template <class T>                                                                                           \
+  static int me_gws_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out, double* hel_out,  \
+                                 void* ws, cudaStream_t st) {                                                  \
+    if (!ws) return 3;                                                                                         \
+    int bytes = (int)sizeof(RecSmemG<T, KK>);                                                                  \
+    int64_t g = (int64_t)sm_count() * MF_GWS_PER_SM;                                                           \
+    me_gws_kernel<KK, T><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out,                        \
+                                                           reinterpret_cast<RecWS<T, KK>*>(ws));               \
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
+  }                                                                                                            \
+  int64_t mf_ws_bytes_k##KK(int prec) {                                                                        \
+    if (prec == 0) return rec_in_smem<KK, double>() ? 0 : (int64_t)sizeof(RecWS<double, KK>) * sm_count() * MF_GWS_PER_SM; \
+    return rec_in_smem<KK, float>() ? 0 : (int64_t)sizeof(RecWS<float, KK>) * sm_count() * MF_GWS_PER_SM;      \
+  }                                                                                                            \
   int mf_launch_me_k##KK(int prec, const int4* prep, int64_t N, const double* skip, double* out,               \
-                         double* hel_out, int* err, MeTune t, cudaStream_t st) {                               \
-    if (prec == 0) return me_rec_launch_k##KK<double, 0>(prep, N, skip, out, hel_out, err, t.waves, st);      \
-    if constexpr (TcTraits<KK>::enabled)                                                                       \
-      if (t.colour == 1) return me_rec_launch_k##KK<float, 1>(prep, N, skip, out, hel_out, err, t.waves, st); \
-    return me_rec_launch_k##KK<float, 0>(prep, N, skip, out, hel_out, err, t.waves, st);                      \
+                         double* hel_out, int* err, MeTune t, void* ws, cudaStream_t st) {                     \
+    if (prec == 0) {                                                                                           \
+      if constexpr (rec_in_smem<KK, double>())                                                                 \
+        return me_rec_launch_k##KK<double, 0>(prep, N, skip, out, hel_out, err, t.waves, st);                 \
+      else                                                                                                     \
+        return me_gws_launch_k##KK<double>(prep, N, skip, out, hel_out, ws, st);                               \
+    }                                                                                                          \
+    if constexpr (!rec_in_smem<KK, float>()) {                                                                 \
+      return me_gws_launch_k##KK<float>(prep, N, skip, out, hel_out, ws, st);                                  \
+    } else {                                                                                                   \
+      if constexpr (TcTraits<KK>::enabled)                                                                     \
+        if (t.colour == 1) return me_rec_launch_k##KK<float, 1>(prep, N, skip, out, hel_out, err, t.waves, st); \
+      return me_rec_launch_k##KK<float, 0>(prep, N, skip, out, hel_out, err, t.waves, st);                    \
+    }                                                                                                          \
   }                                                                                                            \
   int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,    \
                            int64_t cstride, int4* prep, cudaStream_t st) {                                     \

@@ -160,7 +160,14 @@ class Matrix_1_gg_ttxgg(MatrixTTNG):
     process_string = "1_gg_ttxgg"
 
 
-PROCESSES = {2: Matrix_1_gg_ttx, 3: Matrix_1_gg_ttxg, 4: Matrix_1_gg_ttxgg}
+class Matrix_1_gg_ttxggg(MatrixTTNG):
+    """g g > t t~ g g g (1240 diagrams, 120 colour flows, 128 helicities)."""
+
+    n_gluons = 5
+    process_string = "1_gg_ttxggg"
+
+
+PROCESSES = {2: Matrix_1_gg_ttx, 3: Matrix_1_gg_ttxg, 4: Matrix_1_gg_ttxgg, 5: Matrix_1_gg_ttxggg}
 
 
 def smatrix_multi(batches, mdl_MT, mdl_WT, GC_10, GC_11, GC_12=None):

@@ -10,10 +10,12 @@
 #include "../../madflow_gb300/csrc/generated/ttng2.cuh"
 #include "../../madflow_gb300/csrc/generated/ttng3.cuh"
 #include "../../madflow_gb300/csrc/generated/ttng4.cuh"
+#include "../../madflow_gb300/csrc/generated/ttng5.cuh"
 
 MF_DEFINE_REC(2)
 MF_DEFINE_REC(3)
 MF_DEFINE_REC(4)
+MF_DEFINE_REC(5)
 
 // |M|^2 of one event; hel_out (optional) [ncomb] in MadGraph helicity order.
 template <int K, class T>
@@ -42,6 +44,7 @@ extern "C" int me_host_smatrix(int k, int prec, const double* p, int64_t N, cons
     if (k == 2) out[e] = prec ? smatrix_one<2, float>(pe, coup, mt, wt, nullptr) : smatrix_one<2, double>(pe, coup, mt, wt, nullptr);
     else if (k == 3) out[e] = prec ? smatrix_one<3, float>(pe, coup, mt, wt, nullptr) : smatrix_one<3, double>(pe, coup, mt, wt, nullptr);
     else if (k == 4) out[e] = prec ? smatrix_one<4, float>(pe, coup, mt, wt, nullptr) : smatrix_one<4, double>(pe, coup, mt, wt, nullptr);
+    else if (k == 5) out[e] = prec ? smatrix_one<5, float>(pe, coup, mt, wt, nullptr) : smatrix_one<5, double>(pe, coup, mt, wt, nullptr);
     else return 1;
   }
   return 0;
@@ -81,6 +84,7 @@ extern "C" double me_host_flops(int k, const double* p, const double* coup, doub
   if (k == 2) out = smatrix_one<2, CountF>(p, coup, mt, wt, nullptr);
   else if (k == 3) out = smatrix_one<3, CountF>(p, coup, mt, wt, nullptr);
   else if (k == 4) out = smatrix_one<4, CountF>(p, coup, mt, wt, nullptr);
+  else if (k == 5) out = smatrix_one<5, CountF>(p, coup, mt, wt, nullptr);
   (void)out;
   return (double)CountF::n;
 }
@@ -89,6 +93,7 @@ extern "C" int me_host_helicities(int k, const double* p, const double* coup, do
   if (k == 2) smatrix_one<2, double>(p, coup, mt, wt, hel_out);
   else if (k == 3) smatrix_one<3, double>(p, coup, mt, wt, hel_out);
   else if (k == 4) smatrix_one<4, double>(p, coup, mt, wt, hel_out);
+  else if (k == 5) smatrix_one<5, double>(p, coup, mt, wt, hel_out);
   else return 1;
   return 0;
 }

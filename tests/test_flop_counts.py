@@ -10,7 +10,7 @@ import bench
 from conftest import GC10, GC11, GC12, MT, WT
 
 
-@pytest.mark.parametrize("k", [2, 3, 4])
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
 def test_alg_flops(oracle, k):
     T = oracle.TTNG(k)
     x = np.random.default_rng(0).uniform(size=(1, 4 * k + 2))
@@ -18,7 +18,7 @@ def test_alg_flops(oracle, k):
     assert T.flops(p[0], T.params(MT, WT, GC10, GC11, GC12)) == bench.ALG_FLOPS[k]
 
 
-@pytest.mark.parametrize("k", [2, 3, 4])
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
 def test_recycled_flops(host_lib, oracle, k):
     x = np.random.default_rng(1).uniform(size=(1, 4 * k + 2))
     p, *_ = oracle.ramboflow(x, k + 2, 13000.0, [MT, MT] + [0.0] * (k - 2))

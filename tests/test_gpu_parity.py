@@ -114,7 +114,7 @@ def test_smatrix_ggttx_golden(cuda, golden):
     assert rel_err(me2, golden["me_flow_ggttx_smatrix"]) < 1e-12
 
 
-@pytest.mark.parametrize("k", [2, 3, 4])
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
 def test_smatrix_vs_oracle(cuda, oracle, k):
     from madflow_gb300.matrix import PROCESSES
 

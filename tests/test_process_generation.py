@@ -51,7 +51,7 @@ def _dp(a):
     return np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-@pytest.mark.parametrize("k", [2, 3, 4])
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
 def test_generated_recursion_vs_oracle(host_lib, oracle, k):
     """FP64 generated code within 1e-12 of the oracle; FP32 (mixed) within 5e-5."""
     T = oracle.TTNG(k)
@@ -69,7 +69,7 @@ def test_generated_recursion_vs_oracle(host_lib, oracle, k):
         assert np.max(np.abs(out / me0 - 1)) < tol, (k, prec)
 
 
-@pytest.mark.parametrize("k", [2, 3, 4])
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
 def test_generated_per_helicity_vs_oracle(host_lib, oracle, k):
     """Per-helicity values (Matrix_<proc>.matrix) in MadGraph's helicity order."""
     T = oracle.TTNG(k)
