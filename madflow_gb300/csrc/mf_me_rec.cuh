@@ -625,4 +625,72 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
   }
 #endif
 }
+// Processes with few helicities and colour flows (two or three gluons) run
+// EPB events per block, TPE = MF_REC_NT / EPB threads each (a multiple of a
+// warp), every event in its own RecSmem; the block keeps the events in step
+// (stage barriers are block-wide).  Thread 0 gathers the next EPB events of
+// the block's sequence that need work; a sub-group left without one only
+// takes part in the barriers.
+template <int K> constexpr int events_per_block() { return K == 2 ? 6 : (K == 3 ? 3 : 1); }
+template <int K, class T>
+__global__ void __launch_bounds__(MF_REC_NT, 4)
+    me_rec_multi_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
+                        double* __restrict__ out, double* __restrict__ hel_out) {
+  using R = RecTraits<K>;
+  constexpr int EPB = events_per_block<K>(), TPE = MF_REC_NT / EPB, NW = prep_words<T, K>();
+  static_assert(TPE % 32 == 0, "whole warps per event");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  RecSmem<T, K>* Sall = reinterpret_cast<RecSmem<T, K>*>(smem_raw);
+  __shared__ int64_t ev[EPB];
+  __shared__ int64_t cursor;
+  const int tid = threadIdx.x, sub = tid / TPE, lt = tid % TPE;
+  RecSmem<T, K>& S = Sall[sub];
+  if (tid == 0) cursor = blockIdx.x;
+  __syncthreads();
+  for (;;) {
+    if (tid == 0) {
+      int64_t c = cursor;
+      for (int j = 0; j < EPB; ++j) {
+        while (c < N && skip && (__double_as_longlong(skip[c]) << 1) == 0) {
+          out[c] = 0.0;
+          c += gridDim.x;
+        }
+        ev[j] = c < N ? c : -1;
+        if (c < N) c += gridDim.x;
+      }
+      cursor = c;
+    }
+    __syncthreads();
+    if (ev[0] < 0) break;
+    const int64_t e = ev[sub];
+    const bool on = e >= 0;
+    if (on) {
+      int4* dst = reinterpret_cast<int4*>(&S.pr);
+      const int4* src = prep + e * NW;
+      for (int w = lt; w < NW; w += TPE) dst[w] = src[w];
+    }
+    __syncthreads();
+    if (on) rec_st_ext<T, K>(S.ws, S.pr, lt, TPE);
+    __syncthreads();
+    for (int st = 1; st < K; ++st) {
+      if (on) rec_stage<T, K>(S.ws, S.pr.ev, st, lt, TPE);
+      __syncthreads();
+    }
+    if (on) rec_st_A<T, K>(S.ws, lt, TPE);
+    __syncthreads();
+    T part = on ? rec_st_colour<T, K>(S.ws, lt, TPE) : T(0);
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((tid & 31) == 0) S.red[lt >> 5] = part;
+    const double sc = S.pr.scale;
+    if (on && hel_out)
+      for (int c = lt; c < (1 << (K + 2)); c += TPE)
+        hel_out[(int64_t)R::cfg_to_mg(c) * N + e] = rec_colour_one<T, K>(S.ws, c) * sc * R::DENOMINATOR;
+    __syncthreads();
+    if (on && lt == 0) {
+      T tot = T(0);
+      for (int w = 0; w < TPE / 32; ++w) tot += S.red[w];
+      out[e] = (double)tot * sc;
+    }
+  }
+}
 #endif

@@ -31,22 +31,38 @@ static int sm_count() {
   template <class T, int COLOUR>                                                                               \
   static int me_rec_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out, double* hel_out, \
                                  int* err, int waves, cudaStream_t st) {                                       \
-    const void* fn = (const void*)me_rec_kernel<KK, T, COLOUR>;                                                \
-    const void* fn0 = (const void*)me_rec_kernel<KK, T, 0>;                                                    \
-    int bytes = rec_smem_bytes<KK, T>();                                                                       \
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                              \
-    cudaFuncSetAttribute(fn0, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                             \
-    /* resident blocks per SM from the SIMT variant: the same registers and  */                                \
-    /* shared memory (the occupancy query reports 1 for kernels that         */                                \
-    /* allocate tensor memory, although 4 blocks x 32 columns fit)           */                                \
-    int per = 0;                                                                                               \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn0, MF_REC_NT, bytes);                                \
-    if (per < 1) per = 1;                                                                                      \
-    int64_t g = (int64_t)sm_count() * per * (waves > 0 ? waves : 1);                                           \
-    if (g > N) g = N;                                                                                          \
-    if (g < 1) g = 1;                                                                                          \
-    me_rec_kernel<KK, T, COLOUR><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out, err);          \
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
+    if constexpr (events_per_block<KK>() > 1) {                                                                \
+      /* several events per block (few helicities and colour flows) */                                        \
+      const void* fm = (const void*)me_rec_multi_kernel<KK, T>;                                                \
+      int mb = (int)sizeof(RecSmem<T, KK>) * events_per_block<KK>();                                           \
+      cudaFuncSetAttribute(fm, cudaFuncAttributeMaxDynamicSharedMemorySize, mb);                               \
+      int pm = 0;                                                                                              \
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pm, fm, MF_REC_NT, mb);                                   \
+      if (pm < 1) pm = 1;                                                                                      \
+      int64_t gm = (int64_t)sm_count() * pm * (waves > 0 ? waves : 1);                                         \
+      int64_t need = (N + events_per_block<KK>() - 1) / events_per_block<KK>();                                \
+      if (gm > need) gm = need;                                                                                \
+      if (gm < 1) gm = 1;                                                                                      \
+      me_rec_multi_kernel<KK, T><<<(int)gm, MF_REC_NT, mb, st>>>(prep, N, skip, out, hel_out);                \
+      return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                     \
+    } else {                                                                                                   \
+      const void* fn = (const void*)me_rec_kernel<KK, T, COLOUR>;                                              \
+      const void* fn0 = (const void*)me_rec_kernel<KK, T, 0>;                                                  \
+      int bytes = rec_smem_bytes<KK, T>();                                                                     \
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                            \
+      cudaFuncSetAttribute(fn0, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                           \
+      /* resident blocks per SM from the SIMT variant: the same registers and  */                              \
+      /* shared memory (the occupancy query reports 1 for kernels that         */                              \
+      /* allocate tensor memory, although 4 blocks x 32 columns fit)           */                              \
+      int per = 0;                                                                                             \
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn0, MF_REC_NT, bytes);                              \
+      if (per < 1) per = 1;                                                                                    \
+      int64_t g = (int64_t)sm_count() * per * (waves > 0 ? waves : 1);                                         \
+      if (g > N) g = N;                                                                                        \
+      if (g < 1) g = 1;                                                                                        \
+      me_rec_kernel<KK, T, COLOUR><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out, err);        \
+      return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                     \
+    }                                                                                                          \
   }                                                                                                            \
   int64_t mf_prep_bytes_k##KK(int prec) {                                                                      \
     return prec == 0 ? (int64_t)sizeof(PrepRec<double, KK>) : (int64_t)sizeof(PrepRec<float, KK>);           \

@@ -421,9 +421,10 @@ def test_autotuner(cuda):
 @pytest.mark.parametrize("prec", [0, 1])
 def test_smatrix_multi_process_launch(cuda, oracle, prec):
     """g g > t t~, t t~ g and t t~ g g batches of uneven sizes in one
-    persistent launch give the single-process results (FP64: the same bits;
-    mixed: within 1e-5, the single-process g g > t t~ g g colour sum runs on
-    the tensor cores)."""
+    persistent launch give the single-process results (FP64: to rounding,
+    the single-process launches of the small processes split an event over
+    fewer threads and sum in another order; mixed: within 1e-5, the
+    single-process g g > t t~ g g colour sum runs on the tensor cores)."""
     from madflow_gb300.matrix import PROCESSES, smatrix_multi
 
     rng = np.random.default_rng(90)
@@ -436,6 +437,6 @@ def test_smatrix_multi_process_launch(cuda, oracle, prec):
     outs = [_np(o) for o in smatrix_multi(batches, MT, WT, GC10, GC11, GC12)]
     for o, s in zip(outs, singles):
         if prec == 0:
-            assert np.array_equal(o, s)
+            assert rel_err(o, s) < 1e-13
         else:
             assert rel_err(o, s) < 1e-5
