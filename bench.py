@@ -353,8 +353,8 @@ def time_to_target(args, target=1e-3):
     out["vegas_fp64"]["pass_fraction"] = float((integ(x) != 0).double().mean())
 
     def make_flow():
-        return NormalizingFlow(integ.n_dim, n_layers=args.flow_layers, bins=16, hidden=args.flow_hidden, n_hidden=2,
-                               seed=0, bf16=True)
+        return NormalizingFlow(integ.n_dim, n_layers=args.flow_layers, bins=args.flow_bins, hidden=args.flow_hidden,
+                               n_hidden=2, seed=0, bf16=args.flow_bf16)
 
     def flow_run(flow, grid, prior, target_, max_batches, train_batches):
         return adaptive_flow_integration(flow, integ, target_rel_error=target_, batch_size=args.flow_batch,
@@ -382,8 +382,9 @@ def time_to_target(args, target=1e-3):
                          "events": info["batches"] * args.flow_batch + args.flow_vegas_iters * args.flow_vegas_events,
                          "result_pb": res, "error_pb": err, "rel_error": err / abs(res) if res else None,
                          "reached": bool(res and err / abs(res) <= target),
-                         "flow": f"{args.flow_layers} piecewise-quadratic coupling layers, 16 bins, "
-                                 f"MLP 2x{args.flow_hidden} (bf16 cuBLAS), lr {args.flow_lr}, on a frozen VEGAS grid, "
+                         "flow": f"{args.flow_layers} piecewise-quadratic coupling layers, {args.flow_bins} bins, "
+                                 f"MLP 2x{args.flow_hidden} ({'bf16' if args.flow_bf16 else 'TF32'} cuBLAS), "
+                                 f"lr {args.flow_lr}, on a frozen VEGAS grid, "
                                  f"trained on {args.flow_resample} events per batch resampled with probability w^2",
                          "last_std_over_mean": info["last_rel_std"]}
     return out
@@ -466,10 +467,12 @@ def main():
     ap.add_argument("--no-time-to-target", dest="time_to_target", action="store_false")
     ap.add_argument("--target-events", type=int, default=4_000_000)
     ap.add_argument("--max-iter", type=int, default=40)
-    ap.add_argument("--flow-layers", type=int, default=6)
+    ap.add_argument("--flow-layers", type=int, default=4)
+    ap.add_argument("--flow-bins", type=int, default=8)
+    ap.add_argument("--flow-bf16", action="store_true", help="bf16 MLP GEMMs (default TF32)")
     ap.add_argument("--flow-hidden", type=int, default=64)
     ap.add_argument("--flow-batch", type=int, default=2_000_000)
-    ap.add_argument("--flow-minibatch", type=int, default=50_000)
+    ap.add_argument("--flow-minibatch", type=int, default=200_000)
     ap.add_argument("--flow-resample", type=int, default=200_000)
     ap.add_argument("--flow-lr", type=float, default=5e-3)
     ap.add_argument("--flow-train-batches", type=int, default=20)

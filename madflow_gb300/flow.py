@@ -104,8 +104,17 @@ class NormalizingFlow(torch.nn.Module):
                      for m in self.masks]
 
     def _params(self, l, x_a):
-        with torch.autocast("cuda", dtype=torch.bfloat16, enabled=self.bf16):
-            out = self.nets[l](2.0 * x_a - 1.0)
+        if self.bf16:
+            with torch.autocast("cuda", dtype=torch.bfloat16):
+                out = self.nets[l](2.0 * x_a - 1.0)
+        else:
+            # FP32 weights and activations, TF32 tensor-core GEMMs
+            prev = torch.backends.cuda.matmul.allow_tf32
+            torch.backends.cuda.matmul.allow_tf32 = True
+            try:
+                out = self.nets[l](2.0 * x_a - 1.0)
+            finally:
+                torch.backends.cuda.matmul.allow_tf32 = prev
         nb = int(self.masks[l].sum())
         return out.float().reshape(-1, nb, 2 * self.K + 1)
 
