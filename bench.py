@@ -354,7 +354,7 @@ def time_to_target(args, target=1e-3):
 
     def make_flow():
         return NormalizingFlow(integ.n_dim, n_layers=args.flow_layers, bins=args.flow_bins, hidden=args.flow_hidden,
-                               n_hidden=2, seed=0, bf16=args.flow_bf16)
+                               n_hidden=2, seed=0, bf16=args.flow_bf16, tf32=not args.flow_bf16)
 
     def flow_run(flow, grid, prior, target_, max_batches, train_batches):
         return adaptive_flow_integration(flow, integ, target_rel_error=target_, batch_size=args.flow_batch,

@@ -771,10 +771,13 @@ static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, Ite
 // MF_AUTOTUNE=0 in the environment keeps the defaults (tensor cores, 8 waves).
 static const int kTuneWaves[4] = {1, 2, 4, 8};
 static const int64_t kTuneMinEvents = 262144, kTuneEvents = 1 << 20;
+// processes with a global workspace (five gluons): 2^14 events, 16 times the cost each
+static const int64_t kTuneMinEventsGws = 16384, kTuneEventsGws = 1 << 14;
 
 static bool autotune_wanted(const mf_process* p, int64_t N, void* stream) {
-  if (p->tuned || N < kTuneMinEvents) return false;
-  if (mf_ws_bytes(p->k, p->prec) > 0) return false;  // one launch form only
+  const bool gws = mf_ws_bytes(p->k, p->prec) > 0;  // fixed grid: only the colour method is tuned
+  if (p->tuned || N < (gws ? kTuneMinEventsGws : kTuneMinEvents)) return false;
+  if (gws && (p->prec == MF_PREC_FP64 || !mf_colour_tc(p->k))) return false;
   const char* env = getenv("MF_AUTOTUNE");
   if (env && env[0] == '0') return false;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -783,7 +786,9 @@ static bool autotune_wanted(const mf_process* p, int64_t N, void* stream) {
 }
 
 static int autotune_me(mf_process* p, const int4* prep, int64_t N, const double* skip, double* out, void* stream) {
-  int64_t n = N < kTuneEvents ? N : kTuneEvents;
+  const bool gws = mf_ws_bytes(p->k, p->prec) > 0;
+  const int64_t cap = gws ? kTuneEventsGws : kTuneEvents;
+  int64_t n = N < cap ? N : cap;
   cudaEvent_t a = nullptr, b = nullptr;
   int st = cuda_status(cudaEventCreate(&a));
   if (!st) st = cuda_status(cudaEventCreate(&b));
@@ -796,6 +801,10 @@ static int autotune_me(mf_process* p, const int4* prep, int64_t N, const double*
       continue;
     }
     for (int w = 0; w < 4 && !st; ++w) {
+      if (gws && w != 3) {  // the grid does not depend on the waves
+        p->tune_ms[4 * c + w] = -1.0f;
+        continue;
+      }
       MeTune t = {c, kTuneWaves[w]};
       float ms = 0.0f;
       for (int rep = 0; rep < 2 && !st; ++rep) {  // the first launch of a variant is a warm-up

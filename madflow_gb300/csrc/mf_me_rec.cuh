@@ -412,22 +412,66 @@ template <class T, int K> MF_DO double me_rec_event(RecSmem<T, K>& S, const int4
 
 // Processes whose workspace does not fit in shared memory (five gluons: 523
 // KB in FP32) keep it in global memory, one per block (ws [gridDim]); the
-// record and the reduction stay in shared memory.  Same stages, SIMT colour
-// sum, same outputs as me_rec_kernel.
+// record and the reduction stay in shared memory.  Same stages and outputs
+// as me_rec_kernel.  COLOUR = 1 (FP32, 128 helicity combinations, flows a
+// multiple of 40): the colour sum on the tensor cores, one 128-row half of
+// the amplitude matrix (Re, then Im) at a time, K in chunks of 40 flows
+// (5 MMA K-steps each, A_hi and A_lo), C^T resident in shared memory, the
+// accumulator (128 columns) in tensor memory; else the row-loop SIMT sum.
 template <class T, int K> struct RecSmemG {
   PrepRec<T, K> pr;
   T red[MF_REC_NT / 32];
+  unsigned long long mbar;
+  uint32_t tmem;
+  int tc_err;
 };
-template <int K, class T>
+constexpr int MF_GWS_KC = 40;  // flows per K chunk of the tensor-core colour sum
+template <class T, int K> constexpr bool use_colour_tc_gws() {
+  return MF_TCGEN05 && TcTraits<K>::enabled && sizeof(T) == 4 && (1 << (K + 2)) == 128 &&
+         RecTraits<K>::NPERM % MF_GWS_KC == 0 && MF_REC_NT >= 128;
+}
+// shared-memory bytes of the tensor-core colour operands: B (all flows),
+// A_hi and A_lo of one 128-row half and one K chunk
+template <int K> constexpr int gws_tc_bytes() {
+  return TcTraits<K>::enabled ? (TcTraits<K>::N * RecTraits<K>::NPERM + 2 * 128 * MF_GWS_KC) * 4 : 0;
+}
+template <class T, int K> constexpr int gws_smem_bytes(int colour) {
+  return colour == 1 && TcTraits<K>::enabled ? (int)((sizeof(RecSmemG<T, K>) + 1023) / 1024 * 1024) + gws_tc_bytes<K>()
+                                             : (int)sizeof(RecSmemG<T, K>);
+}
+template <int K, class T, int COLOUR>
 __global__ void __launch_bounds__(MF_REC_NT)
     me_gws_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
-                  double* __restrict__ out, double* __restrict__ hel_out, RecWS<T, K>* __restrict__ ws_all) {
+                  double* __restrict__ out, double* __restrict__ hel_out, RecWS<T, K>* __restrict__ ws_all,
+                  int* __restrict__ err) {
   using R = RecTraits<K>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr bool TC = COLOUR == 1 && use_colour_tc_gws<T, K>();
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
   RecSmemG<T, K>& S = *reinterpret_cast<RecSmemG<T, K>*>(smem_raw);
   RecWS<T, K>& ws = ws_all[blockIdx.x];
   const int tid = threadIdx.x, nt = blockDim.x;
   constexpr int NW = prep_words<T, K>();
+#if MF_TCGEN05
+  float* tcB = nullptr;
+  uint32_t phase = 0;
+  if constexpr (TC) {
+    constexpr int NP = R::NPERM;
+    tcB = reinterpret_cast<float*>(smem_raw + (sizeof(RecSmemG<T, K>) + 1023) / 1024 * 1024);
+    // C^T for every K chunk, resident for the whole launch
+    const int4* src = reinterpret_cast<const int4*>(TcTraits<K>::b());
+    int4* dB = reinterpret_cast<int4*>(tcB);
+    for (int i = tid; i < TcTraits<K>::N * NP / 4; i += nt) dB[i] = src[i];
+    if (tid < 32) tc_tmem_alloc(&S.tmem, 128);
+    if (tid == 0) {
+      tc_mbar_init(&S.mbar, 1);
+      S.tc_err = 0;
+    }
+    tc_fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+  }
+#endif
   for (int64_t e = blockIdx.x; e < N; e += gridDim.x) {
     if (skip && (__double_as_longlong(skip[e]) << 1) == 0) {
       if (tid == 0) out[e] = 0.0;
@@ -446,7 +490,84 @@ __global__ void __launch_bounds__(MF_REC_NT)
     }
     rec_st_A<T, K>(ws, tid, nt);
     __syncthreads();
-    T part = rec_st_colour<T, K>(ws, tid, nt);
+    T part = T(0);
+    bool bad = false;
+#if MF_TCGEN05
+    if constexpr (TC) {
+      constexpr int NP = R::NPERM, NC = 1 << (K + 2), KC = MF_GWS_KC, NCH = NP / KC;
+      constexpr uint32_t SBA = (KC / 4) * 128;  // A chunk: 8-row groups
+      constexpr uint32_t idesc = tc_idesc_tf32(128, TcTraits<K>::N);
+      float* hi = tcB + TcTraits<K>::N * NP;
+      float* lo = hi + 128 * KC;
+      const uint32_t bB = tc_smem_u32(tcB), bh = tc_smem_u32(hi), bl = tc_smem_u32(lo);
+      for (int h = 0; h < 2; ++h) {  // 0: Re rows, 1: Im rows
+        for (int q = 0; q < NCH; ++q) {
+          // A_hi, A_lo of rows c, flows [q KC, (q+1) KC), canonical K-major layout
+          for (int it = tid; it < NC * (KC / 4); it += nt) {
+            const int c = it % NC, k4 = it / NC;
+            float vh[4], vl[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const cx<float> a = ws.A[(q * KC + 4 * k4 + j) * NC + c];
+              const float v = h ? a.im : a.re;
+              vh[j] = tc_hi(v);
+              vl[j] = v - vh[j];
+            }
+            const int o = (c / 8) * (KC / 4) * 32 + k4 * 32 + (c % 8) * 4;
+            *reinterpret_cast<float4*>(hi + o) = make_float4(vh[0], vh[1], vh[2], vh[3]);
+            *reinterpret_cast<float4*>(lo + o) = make_float4(vl[0], vl[1], vl[2], vl[3]);
+          }
+          tc_fence_proxy_async();
+          __syncthreads();
+          if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int s = 0; s < KC / 8; ++s) {
+              const uint64_t db = tc_smem_desc(bB + 256 * (q * (KC / 8) + s), TcTraits<K>::LBO, TcTraits<K>::SBO);
+              tc_mma_tf32(S.tmem, tc_smem_desc(bh + 256 * s, 128, SBA), db, idesc, (q > 0 || s > 0) ? 1u : 0u);
+              tc_mma_tf32(S.tmem, tc_smem_desc(bl + 256 * s, 128, SBA), db, idesc, 1u);
+            }
+            tc_commit(&S.mbar);
+          }
+          // every thread waits: the next chunk overwrites the operands
+          bool done = false;
+          for (uint32_t spin = 0; spin < 1000u; ++spin) {
+            done = tc_mbar_try_wait(&S.mbar, phase, 1000000u);
+            if (__all_sync(0xffffffffu, done)) break;
+          }
+          done = __all_sync(0xffffffffu, done);
+          if (!done) S.tc_err = 1;
+          phase ^= 1u;
+          __syncthreads();
+          if (S.tc_err) break;
+        }
+        if (S.tc_err) break;
+        if (tid < 128) {
+          tc_fence_after();
+          const uint32_t ta = S.tmem + ((uint32_t)(32 * (tid >> 5)) << 16);
+          float acc = 0.0f;
+#pragma unroll
+          for (int cb = 0; cb < NP; cb += 8) {
+            float d[8];
+            tc_ld_x8(ta + cb, d);
+            tc_wait_ld();
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+              const cx<float> a = ws.A[(cb + t) * NC + tid];
+              acc += d[t] * (h ? a.im : a.re);
+            }
+          }
+          part += acc;
+          tc_fence_before();
+        }
+        __syncthreads();  // the accumulator is read before the next half overwrites it
+      }
+      bad = S.tc_err != 0;
+    } else
+#endif
+    {
+      part = rec_st_colour<T, K>(ws, tid, nt);
+    }
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((tid & 31) == 0) S.red[tid >> 5] = part;
     const double sc = S.pr.scale;
@@ -457,9 +578,24 @@ __global__ void __launch_bounds__(MF_REC_NT)
     if (tid == 0) {
       T tot = T(0);
       for (int w = 0; w < nt / 32; ++w) tot += S.red[w];
-      out[e] = (double)tot * sc;
+      out[e] = bad ? __longlong_as_double(0x7ff8000000000000ll) : (double)tot * sc;
+      if (bad && err) atomicOr(err, 1);
+    }
+    if (bad) break;
+  }
+#if MF_TCGEN05
+  if constexpr (TC) {
+    __syncthreads();
+    if (S.tc_err) {
+      bool done = false;
+      for (uint32_t spin = 0; spin < 1000u && !done; ++spin) done = tc_mbar_try_wait(&S.mbar, phase ^ 1u, 1000000u);
+    }
+    if (tid < 32) {
+      tc_fence_after();
+      tc_tmem_dealloc(S.tmem, 128);
     }
   }
+#endif
 }
 
 // Block-per-event |M|^2 from the per-event records prep [N][prep_words];

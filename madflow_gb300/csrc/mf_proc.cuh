@@ -68,14 +68,16 @@ static int sm_count() {
     return prec == 0 ? (int64_t)sizeof(PrepRec<double, KK>) : (int64_t)sizeof(PrepRec<float, KK>);           \
   }                                                                                                            \
   bool mf_colour_tc_k##KK() { return TcTraits<KK>::enabled; }                                                  \
-  template <class T>                                                                                           \
+  template <class T, int COLOUR>                                                                               \
   static int me_gws_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out, double* hel_out,  \
-                                 void* ws, cudaStream_t st) {                                                  \
+                                 int* err, void* ws, cudaStream_t st) {                                        \
     if (!ws) return 3;                                                                                         \
-    int bytes = (int)sizeof(RecSmemG<T, KK>);                                                                  \
+    const void* fn = (const void*)me_gws_kernel<KK, T, COLOUR>;                                                \
+    int bytes = gws_smem_bytes<T, KK>(COLOUR);                                                                 \
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                              \
     int64_t g = (int64_t)sm_count() * MF_GWS_PER_SM;                                                           \
-    me_gws_kernel<KK, T><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out,                        \
-                                                           reinterpret_cast<RecWS<T, KK>*>(ws));               \
+    me_gws_kernel<KK, T, COLOUR><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out,                \
+                                                                   reinterpret_cast<RecWS<T, KK>*>(ws), err);  \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }                                                                                                            \
   int64_t mf_ws_bytes_k##KK(int prec) {                                                                        \
@@ -88,10 +90,12 @@ static int sm_count() {
       if constexpr (rec_in_smem<KK, double>())                                                                 \
         return me_rec_launch_k##KK<double, 0>(prep, N, skip, out, hel_out, err, t.waves, st);                 \
       else                                                                                                     \
-        return me_gws_launch_k##KK<double>(prep, N, skip, out, hel_out, ws, st);                               \
+        return me_gws_launch_k##KK<double, 0>(prep, N, skip, out, hel_out, err, ws, st);                       \
     }                                                                                                          \
     if constexpr (!rec_in_smem<KK, float>()) {                                                                 \
-      return me_gws_launch_k##KK<float>(prep, N, skip, out, hel_out, ws, st);                                  \
+      if constexpr (TcTraits<KK>::enabled)                                                                     \
+        if (t.colour == 1) return me_gws_launch_k##KK<float, 1>(prep, N, skip, out, hel_out, err, ws, st);     \
+      return me_gws_launch_k##KK<float, 0>(prep, N, skip, out, hel_out, err, ws, st);                          \
     } else {                                                                                                   \
       if constexpr (TcTraits<KK>::enabled)                                                                     \
         if (t.colour == 1) return me_rec_launch_k##KK<float, 1>(prep, N, skip, out, hel_out, err, t.waves, st); \

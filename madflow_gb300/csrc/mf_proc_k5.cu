@@ -3,4 +3,5 @@
 #include "mf_me.cuh"
 #include "generated/ttng5.cuh"
 #include "mf_proc.cuh"
+MF_DEFINE_TC(5)
 MF_DEFINE_PROCESS(5)

@@ -83,9 +83,13 @@ def _masks(dim, n_layers, seed):
 
 
 class NormalizingFlow(torch.nn.Module):
-    def __init__(self, dim, n_layers=6, bins=16, hidden=64, n_hidden=2, seed=0, bf16=True):
+    def __init__(self, dim, n_layers=6, bins=16, hidden=64, n_hidden=2, seed=0, bf16=True, tf32=False):
+        """bf16: conditioner GEMMs in BF16 (autocast); else FP32, with TF32
+        tensor-core GEMMs when tf32 is set.  Reduced-precision GEMMs leave
+        the estimates unbiased (the sampled log-density is the exact density
+        of the map as evaluated); they perturb the training gradients."""
         super().__init__()
-        self.dim, self.K, self.bf16 = dim, bins, bf16
+        self.dim, self.K, self.bf16, self.tf32 = dim, bins, bf16, tf32
         self.masks = _masks(dim, n_layers, seed)
         self.nets = torch.nn.ModuleList()
         torch.manual_seed(seed)
@@ -108,9 +112,9 @@ class NormalizingFlow(torch.nn.Module):
             with torch.autocast("cuda", dtype=torch.bfloat16):
                 out = self.nets[l](2.0 * x_a - 1.0)
         else:
-            # FP32 weights and activations, TF32 tensor-core GEMMs
+            # FP32 weights and activations; TF32 tensor-core GEMMs if asked
             prev = torch.backends.cuda.matmul.allow_tf32
-            torch.backends.cuda.matmul.allow_tf32 = True
+            torch.backends.cuda.matmul.allow_tf32 = bool(self.tf32)
             try:
                 out = self.nets[l](2.0 * x_a - 1.0)
             finally:

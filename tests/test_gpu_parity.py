@@ -440,3 +440,29 @@ def test_smatrix_multi_process_launch(cuda, oracle, prec):
             assert rel_err(o, s) < 1e-13
         else:
             assert rel_err(o, s) < 1e-5
+
+
+def test_colour_tensor_core_120_flows(cuda, oracle):
+    """g g > t t~ g g g in FP32: the 120-flow colour sum on the tensor cores
+    (two 128-row halves, K in chunks of 40 flows) against the SIMT row loop
+    on the same amplitudes and against the FP64 oracle."""
+    import ctypes
+
+    from madflow_gb300 import _lib
+    from madflow_gb300.matrix import PROCESSES
+
+    rng = np.random.default_rng(55)
+    x = rng.uniform(size=(300, 22))
+    p, *_ = oracle.ramboflow(x, 7, 13000.0, [MT, MT, 0.0, 0.0, 0.0])
+    m = PROCESSES[5](precision=1)
+    m.set_tuning(0, 8)
+    simt = _np(m.smatrix(p, MT, WT, GC10, GC11, GC12))
+    m.set_tuning(1, 8)
+    tc = _np(m.smatrix(p, MT, WT, GC10, GC11, GC12))
+    assert rel_err(tc, simt) < 1e-5
+    T = oracle.TTNG(5)
+    ref = T.smatrix(p[:40], T.params(MT, WT, GC10, GC11, GC12))
+    assert rel_err(tc[:40], ref) < 1e-4
+    flags = ctypes.c_int(-1)
+    _lib.call("mf_process_error_flags", m.handle, ctypes.byref(flags), 1)
+    assert flags.value == 0
