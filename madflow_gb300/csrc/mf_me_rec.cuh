@@ -418,9 +418,10 @@ template <class T, int K> MF_DO double me_rec_event(RecSmem<T, K>& S, const int4
 // the amplitude matrix (Re, then Im) at a time, K in chunks of 40 flows
 // (5 MMA K-steps each, A_hi and A_lo), C^T resident in shared memory, the
 // accumulator (128 columns) in tensor memory; else the row-loop SIMT sum.
+constexpr int MF_GWS_NT = 384;  // threads per block of the global-workspace kernel
 template <class T, int K> struct RecSmemG {
   PrepRec<T, K> pr;
-  T red[MF_REC_NT / 32];
+  T red[MF_GWS_NT / 32];
   unsigned long long mbar;
   uint32_t tmem;
   int tc_err;
@@ -428,7 +429,7 @@ template <class T, int K> struct RecSmemG {
 constexpr int MF_GWS_KC = 40;  // flows per K chunk of the tensor-core colour sum
 template <class T, int K> constexpr bool use_colour_tc_gws() {
   return MF_TCGEN05 && TcTraits<K>::enabled && sizeof(T) == 4 && (1 << (K + 2)) == 128 &&
-         RecTraits<K>::NPERM % MF_GWS_KC == 0 && MF_REC_NT >= 128;
+         RecTraits<K>::NPERM % MF_GWS_KC == 0 && MF_GWS_NT >= 128;
 }
 // shared-memory bytes of the tensor-core colour operands: B (all flows),
 // A_hi and A_lo of one 128-row half and one K chunk
@@ -440,7 +441,7 @@ template <class T, int K> constexpr int gws_smem_bytes(int colour) {
                                              : (int)sizeof(RecSmemG<T, K>);
 }
 template <int K, class T, int COLOUR>
-__global__ void __launch_bounds__(MF_REC_NT)
+__global__ void __launch_bounds__(MF_GWS_NT)
     me_gws_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
                   double* __restrict__ out, double* __restrict__ hel_out, RecWS<T, K>* __restrict__ ws_all,
                   int* __restrict__ err) {

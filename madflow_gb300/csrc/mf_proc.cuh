@@ -8,7 +8,7 @@ template <int K, class T> static int rec_smem_bytes() { return (int)sizeof(RecSm
 // whether the block-per-event workspace of a process fits in shared memory
 template <int K, class T> constexpr bool rec_in_smem() { return sizeof(RecSmem<T, K>) <= 200 * 1024; }
 // blocks of the global-workspace kernel per SM (its workspaces are allocated per block)
-constexpr int MF_GWS_PER_SM = 2;
+constexpr int MF_GWS_PER_SM = 1;
 
 static int sm_count() {
   int dev = 0, sms = 0;
@@ -76,7 +76,7 @@ static int sm_count() {
     int bytes = gws_smem_bytes<T, KK>(COLOUR);                                                                 \
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                              \
     int64_t g = (int64_t)sm_count() * MF_GWS_PER_SM;                                                           \
-    me_gws_kernel<KK, T, COLOUR><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out,                \
+    me_gws_kernel<KK, T, COLOUR><<<(int)g, MF_GWS_NT, bytes, st>>>(prep, N, skip, out, hel_out,                \
                                                                    reinterpret_cast<RecWS<T, KK>*>(ws), err);  \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }                                                                                                            \
