@@ -1,6 +1,6 @@
-// CPU oracle for the madflow hot path.  TEST INFRASTRUCTURE ONLY: it is the
-// checker the CUDA library is compared against (tests, smoke check, and the
-// CPU-baseline leg of the benchmark).  Nothing in the product links it.
+// CPU oracle for the madflow hot path.  TEST INFRASTRUCTURE ONLY: the CUDA
+// library is compared against it (tests, smoke check, and the CPU-baseline
+// leg of the benchmark).  Nothing in the product links it.
 //
 // Every routine restates madflow's algorithm in plain C++ (double precision
 // unless a counting scalar is substituted for R), citing the reference file and

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (``mf_oracle.cpp``).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, by ``__graft_entry__.smoke``
-as the checker, and by the CPU-baseline leg of ``bench.py``.  The product
+to compare against, and by the CPU-baseline leg of ``bench.py``.  The product
 package never imports it.
 
 Each wrapper mirrors the madflow function it restates (same argument meaning,
