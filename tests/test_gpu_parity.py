@@ -466,3 +466,44 @@ def test_colour_tensor_core_120_flows(cuda, oracle):
     flags = ctypes.c_int(-1)
     _lib.call("mf_process_error_flags", m.handle, ctypes.byref(flags), 1)
     assert flags.value == 0
+
+
+def test_edge_cases_of_the_newer_entry_points(cuda):
+    """Empty batches give empty results; invalid arguments give status codes,
+    not faults: unweighting of nothing, a multi-process launch with an empty
+    batch and repeated handles, event output with a bad iteration index, a
+    tuning outside the variants, the integrand of no points."""
+    import ctypes
+
+    import torch
+
+    from madflow_gb300 import _lib, lhe
+    from madflow_gb300.config import stream_ptr
+    from madflow_gb300.matrix import PROCESSES, smatrix_multi
+    from madflow_gb300.vegas import FusedIntegrand, VegasFlow
+
+    idx, rel = lhe.unweight(torch.empty(0, dtype=torch.float64, device="cuda"), 1.0)
+    assert idx.numel() == 0 and rel.numel() == 0
+    with pytest.raises(_lib.MadflowError):
+        lhe.unweight(torch.ones(4, dtype=torch.float64, device="cuda"), 0.0)
+    m3, m4 = PROCESSES[3](precision=1), PROCESSES[4](precision=1)
+    rng = np.random.default_rng(2)
+    x = rng.uniform(size=(50, 18))
+    from madflow_gb300.phasespace import ramboflow
+
+    p4, *_ = ramboflow(x, 6, 13000.0, [MT, MT, 0.0, 0.0])
+    outs = smatrix_multi([(m3, np.zeros((0, 5, 4))), (m4, p4)], MT, WT, GC10, GC11, GC12)
+    assert outs[0].numel() == 0 and outs[1].numel() == 50
+    assert torch.allclose(outs[1], m4.smatrix(p4, MT, WT, GC10, GC11, GC12), rtol=2e-5)
+    with pytest.raises(_lib.MadflowError):
+        smatrix_multi([(m4, p4), (m4, p4)], MT, WT, GC10, GC11, GC12)
+    with pytest.raises(_lib.MadflowError):
+        m4.set_tuning(1, 3)
+    integ = FusedIntegrand(2, kind=0, sqrts=1000.0, precision=1)
+    assert integ(torch.empty((0, 8), dtype=torch.float64, device="cuda")).numel() == 0
+    v = VegasFlow(8, 1000, use_graph=False)
+    f = torch.empty(10, dtype=torch.float64, device="cuda")
+    ps = torch.empty((10, 4, 4), dtype=torch.float64, device="cuda")
+    st = _lib.load().mf_vegas_events(integ.matrix.handle, ctypes.byref(integ._cs), v.grid.data_ptr(), v.nbins, 1, 0,
+                                     -1, 10, f.data_ptr(), ps.data_ptr(), stream_ptr())
+    assert st == _lib.MF_ERR_ARG
