@@ -919,7 +919,7 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   if (mf_launch_me(p->k, p->prec, A.prep, A.N, A.pref, A.me, nullptr, p->d_err, p->tune, p->d_ws, S(stream)))
     return last_launch();
   mark(3);
-  size_t shm = (size_t)(A.ndim * A.nb + 2 * 256) * sizeof(double);
+  size_t shm = (size_t)(A.ndim * A.nb + 3 * 256) * sizeof(double);
   cudaFuncSetAttribute(accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   accum_kernel<<<accum_grid, 256, shm, S(stream)>>>(A.pref, A.me, A.bins, A.N, A.ndim, A.nb, A.inv_n, f_out,
                                                      results ? p->d_partials : nullptr);

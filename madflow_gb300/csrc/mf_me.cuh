@@ -267,7 +267,7 @@ static __global__ void __launch_bounds__(256) accum_kernel(const double* __restr
                                                     const unsigned char* __restrict__ bins, int64_t N, int ndim,
                                                     int nb, double inv_n, double* __restrict__ f_out,
                                                     double* __restrict__ partials) {
-  extern __shared__ double sh[];  // [ndim*nb] + [2*blockDim]
+  extern __shared__ double sh[];  // [ndim*nb] + [2*blockDim] + [blockDim]
   double* hist = sh;
   double* red = sh + ndim * nb;
   const int width = 2 + ndim * nb;
@@ -292,12 +292,26 @@ static __global__ void __launch_bounds__(256) accum_kernel(const double* __restr
     }
     __syncthreads();
   }
-  if (bins)
-    for (int d = threadIdx.x; d < ndim; d += blockDim.x)
-      for (int64_t e = e0; e < e1; ++e) {
-        double w = pref[e] * me[e] * inv_n;
-        hist[d * nb + bins[(int64_t)d * N + e]] += w * w;
+  if (bins) {
+    // per-bin sums of w^2 in event order, one thread per dimension; w^2 of a
+    // chunk of blockDim events is formed once by all threads
+    double* w2 = red + 2 * blockDim.x;
+    for (int64_t c0 = e0; c0 < e1; c0 += blockDim.x) {
+      const int64_t e = c0 + threadIdx.x;
+      if (e < e1) {
+        const double w = pref[e] * me[e] * inv_n;
+        w2[threadIdx.x] = w * w;
       }
+      __syncthreads();
+      const int cn = (int)min((int64_t)blockDim.x, e1 - c0);
+      for (int d = threadIdx.x; d < ndim; d += blockDim.x) {
+        const unsigned char* bd = bins + (int64_t)d * N + c0;
+        double* hd = hist + d * nb;
+        for (int j = 0; j < cn; ++j) hd[bd[j]] += w2[j];
+      }
+      __syncthreads();
+    }
+  }
   __syncthreads();
   if (partials) {
     double* out = partials + (int64_t)blockIdx.x * width;
