@@ -360,7 +360,7 @@ __global__ void reduce_partials_kernel(const double* __restrict__ partials, int 
 __global__ void vegas_accum_kernel(const double* __restrict__ f, const double* __restrict__ jac,
                                    const int32_t* __restrict__ bins, int64_t N, int ndim, int nb, double inv_n,
                                    double* __restrict__ partials) {
-  extern __shared__ double sh[];  // [ndim*nb] + [2*blockDim]
+  extern __shared__ double sh[];  // [ndim*nb] + [2*blockDim] + [blockDim]
   double* hist = sh;
   double* red = sh + ndim * nb;
   int width = 2 + ndim * nb;
@@ -383,12 +383,24 @@ __global__ void vegas_accum_kernel(const double* __restrict__ f, const double* _
     }
     __syncthreads();
   }
-  for (int d = threadIdx.x; d < ndim; d += blockDim.x)
-    for (int64_t e = e0; e < e1; ++e) {
-      double w = f[e] * jac[e] * inv_n;
-      hist[d * nb + bins[(int64_t)d * N + e]] += w * w;
+  // per-bin sums of w^2 in event order, one thread per dimension; w^2 of a
+  // chunk of blockDim events is formed once by all threads
+  double* w2 = red + 2 * blockDim.x;
+  for (int64_t c0 = e0; c0 < e1; c0 += blockDim.x) {
+    const int64_t e = c0 + threadIdx.x;
+    if (e < e1) {
+      const double w = f[e] * jac[e] * inv_n;
+      w2[threadIdx.x] = w * w;
     }
-  __syncthreads();
+    __syncthreads();
+    const int cn = (int)min((int64_t)blockDim.x, e1 - c0);
+    for (int d = threadIdx.x; d < ndim; d += blockDim.x) {
+      const int32_t* bd = bins + (int64_t)d * N + c0;
+      double* hd = hist + d * nb;
+      for (int j = 0; j < cn; ++j) hd[bd[j]] += w2[j];
+    }
+    __syncthreads();
+  }
   double* out = partials + (int64_t)blockIdx.x * width;
   if (threadIdx.x == 0) { out[0] = red[0]; out[1] = red[blockDim.x]; }
   for (int i = threadIdx.x; i < ndim * nb; i += blockDim.x) out[2 + i] = hist[i];
@@ -1091,7 +1103,7 @@ int mf_vegas_accumulate(const double* f, const double* jac, const int32_t* bins,
     if (st) return st;
     cap[dev] = need;
   }
-  size_t shm = (size_t)(ndim * nb + 2 * 256) * sizeof(double);
+  size_t shm = (size_t)(ndim * nb + 3 * 256) * sizeof(double);
   cudaFuncSetAttribute(vegas_accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   vegas_accum_kernel<<<blocks, 256, shm, S(stream)>>>(f, jac, bins, N, ndim, nb, inv_n, part[dev]);
   reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(part[dev], blocks, width, results);
@@ -1147,7 +1159,7 @@ int mf_vegas_accumulate_noalloc(const double* f, const double* jac, const int32_
   const int width = 2 + ndim * nb;
   // every block writes all `width` entries of its row, so the partials left
   // by an earlier call never need clearing
-  size_t shm = (size_t)(ndim * nb + 2 * 256) * sizeof(double);
+  size_t shm = (size_t)(ndim * nb + 3 * 256) * sizeof(double);
   cudaFuncSetAttribute(vegas_accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   vegas_accum_kernel<<<blocks, 256, shm, S(stream)>>>(f, jac, bins, N, ndim, nb, inv_n, part);
   reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(part, blocks, width, results);
