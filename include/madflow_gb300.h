@@ -197,7 +197,10 @@ int mf_process_set_timing(mf_process* proc, int enable);
  * (up to 2^20) in MF_TUNE_VARIANTS variants -- colour sum on the SIMT lanes
  * (colour 0) or on the tensor cores (colour 1, FP32 processes with 24 colour
  * flows) x a grid of 1, 2, 4 or 8 waves of resident blocks -- and the fastest
- * is kept by the handle.  MF_AUTOTUNE=0 in the environment keeps the default
+ * is kept by the handle (that one call waits on the host for the timings).
+ * Five-gluon processes (global workspace, fixed grid) tune only the colour
+ * method, on 2^14 events, from 16384 events up.  MF_AUTOTUNE=0 in the
+ * environment keeps the default
  * (colour 1 where available, 8 waves).  mf_process_tuning reports the
  * configuration, whether it was tuned, and (ms, optional, MF_TUNE_VARIANTS
  * floats) the time of each variant in milliseconds, index colour*4 +
