@@ -195,7 +195,7 @@ int mf_process_set_timing(mf_process* proc, int enable);
  * least 262144 events that is not being captured into a CUDA graph, the
  * matrix-element kernel is timed with CUDA events on that call's own events
  * (up to 2^20) in MF_TUNE_VARIANTS variants -- colour sum on the SIMT lanes
- * (colour 0) or on the tensor cores (colour 1, FP32 processes with 24 colour
+ * (colour 0) or on the tensor cores (colour 1, FP32 processes with 24 or 120 colour
  * flows) x a grid of 1, 2, 4 or 8 waves of resident blocks -- and the fastest
  * is kept by the handle (that one call waits on the host for the timings).
  * Five-gluon processes (global workspace, fixed grid) tune only the colour
