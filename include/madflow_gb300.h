@@ -274,6 +274,14 @@ int mf_pq_inverse(const float* u, const float* params, int64_t n, int nb, int K,
                   void* stream);
 int mf_pq_backward(const float* x, const float* params, const float* gy, const float* glogdet, int64_t n, int nb,
                    int K, float* gx, float* gparams, void* stream);
+/* The same three kernels under the flow-sampler names of the boundary:
+ * forward (density), inverse (sampling), gradient. */
+int mf_flow_fwd(const float* x, const float* params, int64_t n, int nb, int K, float* y, float* logdet,
+                void* stream);
+int mf_flow_inv(const float* u, const float* params, int64_t n, int nb, int K, float* x, float* logdet,
+                void* stream);
+int mf_flow_grad(const float* x, const float* params, const float* gy, const float* glogdet, int64_t n, int nb, int K,
+                 float* gx, float* gparams, void* stream);
 
 #ifdef __cplusplus
 }

@@ -175,4 +175,17 @@ int mf_pq_backward(const float* x, const float* params, const float* gy, const f
   return launch_check();
 }
 
+int mf_flow_fwd(const float* x, const float* params, int64_t n, int nb, int K, float* y, float* logdet,
+                void* stream) {
+  return mf_pq_forward(x, params, n, nb, K, y, logdet, stream);
+}
+int mf_flow_inv(const float* u, const float* params, int64_t n, int nb, int K, float* x, float* logdet,
+                void* stream) {
+  return mf_pq_inverse(u, params, n, nb, K, x, logdet, stream);
+}
+int mf_flow_grad(const float* x, const float* params, const float* gy, const float* glogdet, int64_t n, int nb, int K,
+                 float* gx, float* gparams, void* stream) {
+  return mf_pq_backward(x, params, gy, glogdet, n, nb, K, gx, gparams, stream);
+}
+
 }  // extern "C"
