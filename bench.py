@@ -124,7 +124,7 @@ def run_gpu(args):
     import torch
 
     from madflow_gb300 import _lib
-    from madflow_gb300.vegas import VegasFlow
+    from madflow_gb300.vegas import VegasFlow, reduce_results
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -138,7 +138,8 @@ def run_gpu(args):
     prec = _lib.MF_PREC_MIXED if args.precision == "mixed" else _lib.MF_PREC_FP64
     integ = make_integrand(prec)
     N = args.events
-    # replicas: each rank integrates its own Philox stream (stream id = rank)
+    # each rank draws its own Philox stream (stream id = rank); with several
+    # ranks the iteration sums are all-reduced, so every rank refines one grid
     vegas = VegasFlow(integ.n_dim, N, seed=args.seed, stream_id=rank, use_graph=True)
     vegas.compile(integ)
     f_out = torch.empty(N, dtype=torch.float64, device="cuda")
@@ -147,6 +148,9 @@ def run_gpu(args):
 
     def step():
         integ.iteration(vegas.grid, vegas.seed, vegas.stream_id, vegas.iteration, N, vegas.results, f_out=f_out)
+        if dist:
+            # one grid over all ranks: the iteration sums are summed (NCCL) before the refinement
+            reduce_results(vegas.results)
         _lib.call("mf_vegas_refine", vegas.grid.data_ptr(), vegas.results[2:].data_ptr(), vegas.n_dim, vegas.nbins,
                   vegas.alpha, torch.cuda.current_stream().cuda_stream)
         vegas.iteration += 1
@@ -232,7 +236,9 @@ def run_gpu(args):
         "dtype": "f32 (mixed: FP64 momenta, propagators, sums)" if prec == 1 else "f64",
         "data": "synthetic (Philox4x32-10 uniforms, seed %d)" % args.seed,
         "config": dict(workload(N), precision=args.precision, l2="flushed (256 MB write) before every step",
-                       parallelism="replicas" if world > 1 else "single GPU"),
+                       parallelism=(f"sharded over {world} GPUs: own Philox stream and {N} points per rank, "
+                                    "one NCCL all-reduce of the iteration sums per step, one grid")
+                       if world > 1 else "single GPU"),
         "pass_fraction": pass_frac,
         "phase_space_points_per_s": N * args.steps * world / step_s,
         "wall_s": wall,
