@@ -18,6 +18,7 @@
 // The stage functions are host-callable so the CPU test suite can run them
 // one thread at a time against the oracle.
 #pragma once
+#include <type_traits>
 #include "mf_helas.cuh"
 #include "mf_phasespace.cuh"
 #include "mf_vertex.cuh"
@@ -100,7 +101,10 @@ template <class T, int K>
 MF_D void prep_event(PrepRec<T, K>& r, const double (*p)[4], double mt, double wt, cx<double> c10, cx<double> c11,
                      cx<double> c12) {
   using R = RecTraits<K>;
-  for (int s = 0; s < (1 << K); ++s) evdata_subset<T, K>(r.ev, s, p, mt, wt, c10, c11, c12);
+  if constexpr (std::is_same<T, float>::value)
+    evdata_all_ff<K>(r.ev, p, mt, wt, c10, c11, c12);
+  else
+    for (int s = 0; s < (1 << K); ++s) evdata_subset<T, K>(r.ev, s, p, mt, wt, c10, c11, c12);
   for (int i = 0; i < K + 2; ++i)
     for (int c = 0; c < 4; ++c) r.ev.pext[i][c] = (T)p[i][c];
   r.ev.mt = (T)mt;

@@ -5,7 +5,8 @@
 //
 // The momentum flow of a current is kept per subset of external legs (the
 // "slot" momentum Q: +p for outgoing, -p for incoming), so the propagator
-// factor of every subset is computed once per event, in FP64, instead of once
+// factor of every subset is computed once per event (the momenta and
+// invariants in FP64, or in double-float for the FP32 path) instead of once
 // per current and helicity.  In the HELAS chiral basis the vertex bilinear is
 // F1^T S(V) F2 with S(a) = [[0, a+], [a-, 0]],
 //   a+ = [[a0+a3, a1+i a2], [a1-i a2, a0-a3]],
@@ -77,7 +78,8 @@ template <class T> MF_D cx<T> sandwich(const W4<T>& F1, const W4<T>& V, const W4
 
 // Per-event data shared by all helicities of one event: slot momenta of every
 // subset of gluons (Qg) and of the top line (Qt = p_t + Qg), and the
-// propagator x coupling factors, evaluated in FP64 and stored in T.
+// propagator x coupling factors, evaluated in FP64 (double-float for T =
+// float) and stored in T.
 template <class T, int K> struct EvData {
   T Qg[1 << K][4];
   T Qt[1 << K][4];
@@ -90,6 +92,96 @@ template <class T, int K> struct EvData {
 
 // Slot sign of gluon label j: incoming gluons (particles 0, 1) carry -p.
 template <int K> MF_D int gluon_particle(int j) { return j < 2 ? j : j + 2; }
+
+// Double-float arithmetic (a value as an unevaluated sum hi + lo of two
+// floats, about 48 significant bits), after Dekker (Numer. Math. 18 (1971)
+// 224) and Knuth (TAOCP vol. 2, 4.2.2): the error-free two_sum and the
+// fma-based two_prod.  GB300 runs FP32 at 64 times its FP64 rate, so the
+// subset invariants of the mixed path are formed this way.
+struct ffl {
+  float hi, lo;
+};
+MF_HD ffl ff_two_sum(float a, float b) {
+  float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+MF_HD ffl ff_quick_two_sum(float a, float b) {
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+MF_HD ffl ff_from(double x) {
+  float h = (float)x;
+  return {h, (float)(x - (double)h)};
+}
+MF_HD ffl ff_add(ffl a, ffl b) {
+  ffl s = ff_two_sum(a.hi, b.hi), t = ff_two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = ff_quick_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return ff_quick_two_sum(s.hi, s.lo);
+}
+MF_HD ffl ff_neg(ffl a) { return {-a.hi, -a.lo}; }
+MF_HD ffl ff_sqr(ffl a) {
+  float p = a.hi * a.hi;
+  float e = fmaf(a.hi, a.hi, -p) + 2.0f * a.hi * a.lo;
+  return ff_quick_two_sum(p, e);
+}
+MF_HD float ff_float(ffl a) { return a.hi + a.lo; }
+// Minkowski square in double-float
+MF_HD ffl ff_msq(const ffl* v) {
+  ffl r = ff_sqr(v[0]);
+  r = ff_add(r, ff_neg(ff_sqr(v[1])));
+  r = ff_add(r, ff_neg(ff_sqr(v[2])));
+  return ff_add(r, ff_neg(ff_sqr(v[3])));
+}
+
+// Every subset of EvData<float> from FP64 external momenta p[K+2][4]: the
+// subset momenta, P^2 and the top line's P^2 - M^2 (where the pole cancels)
+// in double-float, the divisions in FP32.
+template <int K>
+MF_D void evdata_all_ff(EvData<float, K>& ev, const double (*p)[4], double mt, double wt, cx<double> gc10,
+                        cx<double> gc11, cx<double> gc12) {
+  ffl pg[K][4], pt[4];
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    const int part = gluon_particle<K>(j);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) pg[j][c] = ff_from(part < 2 ? -p[part][c] : p[part][c]);
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) pt[c] = ff_from(p[2][c]);
+  const ffl mt2 = ff_from(mt * mt);
+  const float g10r = (float)gc10.re, g10i = (float)gc10.im, g12r = (float)gc12.re, g12i = (float)gc12.im;
+  const cx<float> num = mul_i(ccast<float>(gc11));
+  const float mw = (float)(mt * wt);
+  for (int s = 0; s < (1 << K); ++s) {
+    ffl Q[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}}, Qt[4];
+    int nbits = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      if (s >> j & 1) {
+        ++nbits;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) Q[c] = ff_add(Q[c], pg[j][c]);
+      }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      Qt[c] = ff_add(pt[c], Q[c]);
+      ev.Qg[s][c] = ff_float(Q[c]);
+      ev.Qt[s][c] = ff_float(Qt[c]);
+    }
+    if (nbits >= 2) {
+      const float iq = 1.0f / ff_float(ff_msq(Q));
+      ev.gv3[s] = cx<float>{g10r * iq, g10i * iq};
+      ev.gv4[s] = cx<float>{g12i * iq, -g12r * iq};
+    } else {
+      ev.gv3[s] = cx<float>{0.0f, 0.0f};
+      ev.gv4[s] = cx<float>{0.0f, 0.0f};
+    }
+    const cx<float> den = {ff_float(ff_add(ff_msq(Qt), ff_neg(mt2))), mw};
+    ev.tden[s] = cdiv(num, den);
+  }
+}
 
 // Fill subset `s` of EvData from FP64 external momenta p[K+2][4].
 template <class T, int K>
