@@ -147,7 +147,7 @@ MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (
   MfConsts KC = mf_consts(A.f32q != 0);
   int nout = npart - 2;
   double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
-  logw = rambo_massive(nout, A.masses, p + 2, roots, logw, KC.acc, newton_iters);
+  logw = rambo_massive<P>(nout, A.masses, p + 2, roots, logw, KC.acc, newton_iters);
   double wps = (double)ps_exp((P)logw) / pw;
   double ein = roots / 2.0;
   p[0][0] = ein; p[0][1] = 0.0; p[0][2] = 0.0; p[0][3] = ein;

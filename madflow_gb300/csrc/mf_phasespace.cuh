@@ -127,6 +127,8 @@ MF_HD int newton_conv_iter(int n, const double* masses, const double (*p)[4], do
 // Massive correction of rambo (phasespace.py:194-212) running `iters` Newton
 // iterations (iters <= 0: iterate this event to its own convergence).
 // Rescales p in place and returns the final log-weight.
+// The weight factors run in W (the momenta and the Newton solve stay FP64).
+template <class W = double>
 MF_HD double rambo_massive(int n, const double* masses, double (*p)[4], double sqrts, double logw, double acc,
                            int iters) {
   double m2[MF_MAX_OUT], e2[MF_MAX_OUT], newE[MF_MAX_OUT], tm = 0.0;
@@ -144,17 +146,19 @@ MF_HD double rambo_massive(int n, const double* masses, double (*p)[4], double s
     for (int it = 0; it < 10; ++it)
       if (!newton_step(n, m2, e2, sqrts, acc, xf, newE)) break;
   }
-  double wt2 = 1.0, wt3 = 0.0;
+  W wt2 = W(1), wt3 = W(0);
   for (int i = 0; i < n; ++i) {
     double v = p[i][0] * xf;
-    wt2 = wt2 * (v / newE[i]);
-    wt3 = wt3 + v * v / newE[i];
+    const W vw = (W)v, ew = (W)newE[i];
+    wt2 = wt2 * (vw / ew);
+    wt3 = wt3 + vw * vw / ew;
     p[i][0] = newE[i];
     p[i][1] *= xf;
     p[i][2] *= xf;
     p[i][3] *= xf;
   }
-  return logw + (double)(2 * n - 3) * log(xf) + log(wt2 / wt3 * sqrts);
+  const W a = (W)(2 * n - 3) * ps_log((W)xf), b = ps_log(wt2 / wt3 * (W)sqrts);
+  return logw + (double)a + (double)b;
 }
 
 // _get_x1x2 (phasespace.py:215-233)
