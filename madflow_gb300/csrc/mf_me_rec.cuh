@@ -454,7 +454,8 @@ __global__ void __launch_bounds__(MF_GWS_NT)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   RecSmemG<T, K>& S = *reinterpret_cast<RecSmemG<T, K>*>(smem_raw);
   RecWS<T, K>& ws = ws_all[blockIdx.x];
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x;
+  constexpr int nt = MF_GWS_NT;  // launched with MF_GWS_NT threads
   constexpr int NW = prep_words<T, K>();
 #if MF_TCGEN05
   float* tcB = nullptr;
@@ -622,7 +623,9 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
   constexpr bool TC = COLOUR == 1 && use_colour_tc<T, K>();
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   RecSmem<T, K>& S = *reinterpret_cast<RecSmem<T, K>*>(smem_raw);
-  const int tid = threadIdx.x, nt = blockDim.x;
+  // launched with MF_REC_NT threads: a compile-time stride for every item loop
+  const int tid = threadIdx.x;
+  constexpr int nt = MF_REC_NT;
   constexpr int NW = prep_words<T, K>();
 #if MF_TCGEN05
   // operands in the shared memory of the top-line currents and t~ rows,
