@@ -24,7 +24,8 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     me_multi_kernel(MultiMe M, unsigned long long* __restrict__ counter) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ unsigned long long item;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x;
+  constexpr int nt = MF_REC_NT;  // launched with MF_REC_NT threads
   const unsigned long long total = (unsigned long long)M.off[M.n];
   for (;;) {
     if (tid == 0) item = atomicAdd(counter, 1ull);
