@@ -465,6 +465,9 @@ def emit_program(k):
     w(_arr("prog", "int", prog))
     w(_arr("pdesc", "int", pdesc))
     w(_arr("stage_first", "int", stage_first))
+    # the same two tables as compile-time constants (the stage loops)
+    w(f"constexpr int pdesc_c[{len(pdesc)}] = {{{', '.join(str(int(v)) for v in pdesc)}}};")
+    w(f"constexpr int stage_first_c[{len(stage_first)}] = {{{', '.join(str(int(v)) for v in stage_first)}}};")
     w(_arr("arec", "int", arec))
     w(_arr("hpack", "unsigned char", hpack))
     w(_arr("hunpack", "unsigned char", hunpack))

@@ -46,6 +46,8 @@ template <int K> struct RecTraits;
     MF_D static int jo_ext(int i) { return MF_TBL(rec##KK, jo_ext, i); }                                  \
     MF_D static int cfg_to_mg(int i) { return MF_TBL(rec##KK, cfg_to_mg, i); }                            \
     MF_D static float colour(int i) { return MF_TBL(ttng##KK, colour_num, i); }                           \
+    MF_HD static constexpr int pdesc_c(int i) { return rec##KK::pdesc_c[i]; }                             \
+    MF_HD static constexpr int stage_first_c(int i) { return rec##KK::stage_first_c[i]; }                 \
   };
 
 // Currents in shared memory as 16-byte planes: plane p holds bytes
@@ -223,6 +225,37 @@ MF_D void rec_stage(RecWS<T, K>& ws, const EvData<T, K>& ev, int stage, int tid,
     for (int local = first; local < cnt; local += nt)
       rec_item<T, K>(ws, ev, type, L, rec0 + (local >> lper) * rsz, local & ((1 << lper) - 1));
     base += cnt;
+  }
+}
+
+// The same stage with the part table folded in at compile time (part P of
+// stage STAGE; the item loops keep their run-time node index only).
+template <class T, int K, int P, int PEND, int NT>
+MF_D void rec_stage_parts(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid, int base) {
+  if constexpr (P < PEND) {
+    using R = RecTraits<K>;
+    constexpr int type = R::pdesc_c(5 * P), L = R::pdesc_c(5 * P + 1);
+    constexpr int lper = (type <= 1) ? L : L + 1;
+    constexpr int cnt = R::pdesc_c(5 * P + 2) << lper;
+    constexpr int rec0 = R::pdesc_c(5 * P + 3), rsz = R::pdesc_c(5 * P + 4);
+    int first = (tid - base) % NT;
+    if (first < 0) first += NT;
+    for (int local = first; local < cnt; local += NT)
+      rec_item<T, K>(ws, ev, type, L, rec0 + (local >> lper) * rsz, local & ((1 << lper) - 1));
+    rec_stage_parts<T, K, P + 1, PEND, NT>(ws, ev, tid, base + cnt);
+  }
+}
+template <class T, int K, int STAGE, int NT>
+MF_D void rec_stage_c(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid) {
+  using R = RecTraits<K>;
+  rec_stage_parts<T, K, R::stage_first_c(STAGE - 1), R::stage_first_c(STAGE), NT>(ws, ev, tid, 0);
+}
+template <class T, int K, int STAGE, int NT>
+MF_DO void rec_stages_c(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid) {
+  if constexpr (STAGE < K) {
+    rec_stage_c<T, K, STAGE, NT>(ws, ev, tid);
+    __syncthreads();
+    rec_stages_c<T, K, STAGE + 1, NT>(ws, ev, tid);
   }
 }
 
@@ -667,10 +700,7 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
   if (e < N) load_ext(e);
   while (e < N) {
     __syncthreads();
-    for (int st = 1; st < K; ++st) {
-      rec_stage<T, K>(S.ws, S.pr.ev, st, tid, nt);
-      __syncthreads();
-    }
+    rec_stages_c<T, K, 1, nt>(S.ws, S.pr.ev, tid);
     rec_st_A<T, K>(S.ws, tid, nt);
     __syncthreads();
     const double sc = S.pr.scale;
