@@ -250,12 +250,14 @@ MF_D void rec_stage_c(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid) {
   using R = RecTraits<K>;
   rec_stage_parts<T, K, R::stage_first_c(STAGE - 1), R::stage_first_c(STAGE), NT>(ws, ev, tid, 0);
 }
+// stages STAGE..K-1, each followed by a block barrier; a thread with on =
+// false only takes part in the barriers
 template <class T, int K, int STAGE, int NT>
-MF_DO void rec_stages_c(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid) {
+MF_DO void rec_stages_c(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid, bool on = true) {
   if constexpr (STAGE < K) {
-    rec_stage_c<T, K, STAGE, NT>(ws, ev, tid);
+    if (on) rec_stage_c<T, K, STAGE, NT>(ws, ev, tid);
     __syncthreads();
-    rec_stages_c<T, K, STAGE + 1, NT>(ws, ev, tid);
+    rec_stages_c<T, K, STAGE + 1, NT>(ws, ev, tid, on);
   }
 }
 
@@ -421,17 +423,15 @@ __global__ void __launch_bounds__(128) prep_kernel(const double* __restrict__ ps
 // One event by the whole block with the SIMT colour sum (launches that mix
 // processes): record load, stages, amplitudes, colour sum, block reduction.
 // Returns |M|^2 in thread 0.
-template <class T, int K> MF_DO double me_rec_event(RecSmem<T, K>& S, const int4* __restrict__ rec, int tid, int nt) {
+template <class T, int K, int NT> MF_DO double me_rec_event(RecSmem<T, K>& S, const int4* __restrict__ rec, int tid) {
+  constexpr int nt = NT;
   constexpr int NW = prep_words<T, K>();
   int4* dst = reinterpret_cast<int4*>(&S.pr);
   for (int w = tid; w < NW; w += nt) dst[w] = rec[w];
   __syncthreads();
   rec_st_ext<T, K>(S.ws, S.pr, tid, nt);
   __syncthreads();
-  for (int st = 1; st < K; ++st) {
-    rec_stage<T, K>(S.ws, S.pr.ev, st, tid, nt);
-    __syncthreads();
-  }
+  rec_stages_c<T, K, 1, NT>(S.ws, S.pr.ev, tid);
   rec_st_A<T, K>(S.ws, tid, nt);
   __syncthreads();
   T part = rec_st_colour<T, K>(S.ws, tid, nt);
@@ -523,10 +523,7 @@ __global__ void __launch_bounds__(MF_GWS_NT)
     __syncthreads();
     rec_st_ext<T, K>(ws, S.pr, tid, nt);
     __syncthreads();
-    for (int st = 1; st < K; ++st) {
-      rec_stage<T, K>(ws, S.pr.ev, st, tid, nt);
-      __syncthreads();
-    }
+    rec_stages_c<T, K, 1, nt>(ws, S.pr.ev, tid);
     rec_st_A<T, K>(ws, tid, nt);
     __syncthreads();
     T part = T(0);
@@ -846,10 +843,7 @@ __global__ void __launch_bounds__(MF_REC_NT, 4)
     __syncthreads();
     if (on) rec_st_ext<T, K>(S.ws, S.pr, lt, TPE);
     __syncthreads();
-    for (int st = 1; st < K; ++st) {
-      if (on) rec_stage<T, K>(S.ws, S.pr.ev, st, lt, TPE);
-      __syncthreads();
-    }
+    rec_stages_c<T, K, 1, TPE>(S.ws, S.pr.ev, lt, on);
     if (on) rec_st_A<T, K>(S.ws, lt, TPE);
     __syncthreads();
     T part = on ? rec_st_colour<T, K>(S.ws, lt, TPE) : T(0);

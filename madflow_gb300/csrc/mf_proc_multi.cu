@@ -39,16 +39,13 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     double r = 0.0;
     switch (M.k[j]) {
       case 2:
-        r = me_rec_event<T, 2>(*reinterpret_cast<RecSmem<T, 2>*>(smem_raw), M.prep[j] + e * prep_words<T, 2>(), tid,
-                               nt);
+        r = me_rec_event<T, 2, nt>(*reinterpret_cast<RecSmem<T, 2>*>(smem_raw), M.prep[j] + e * prep_words<T, 2>(), tid);
         break;
       case 3:
-        r = me_rec_event<T, 3>(*reinterpret_cast<RecSmem<T, 3>*>(smem_raw), M.prep[j] + e * prep_words<T, 3>(), tid,
-                               nt);
+        r = me_rec_event<T, 3, nt>(*reinterpret_cast<RecSmem<T, 3>*>(smem_raw), M.prep[j] + e * prep_words<T, 3>(), tid);
         break;
       default:
-        r = me_rec_event<T, 4>(*reinterpret_cast<RecSmem<T, 4>*>(smem_raw), M.prep[j] + e * prep_words<T, 4>(), tid,
-                               nt);
+        r = me_rec_event<T, 4, nt>(*reinterpret_cast<RecSmem<T, 4>*>(smem_raw), M.prep[j] + e * prep_words<T, 4>(), tid);
         break;
     }
     if (tid == 0) M.out[j][e] = r;
