@@ -368,6 +368,10 @@ def emit_program(k):
     prog = []  # flat int records
     parts = []  # per stage: list of (type, L, n_nodes, first_record, record_size)
 
+    # Records are groups of four ints, so that the kernels read each group
+    # with one 16-byte load: a current's header (out, reversed out, sign,
+    # subset), one group per split (J offsets and subsets of both sides), one
+    # per triple of the contact term (three J offsets, padding).
     def cur_record(s, out_off, out_rev, sign):
         L = len(s)
         rec = [out_off, out_rev, sign, _mask(s)]
@@ -376,8 +380,14 @@ def emit_program(k):
             rec += [jo[a], jo[b], _mask(a), _mask(b)]
         for i in range(1, L):
             for j in range(i + 1, L):
-                rec += [jo[s[:i]], jo[s[i:j]], jo[s[j:]]]
+                rec += [jo[s[:i]], jo[s[i:j]], jo[s[j:]], 0]
         return rec
+
+    def pad4(rec):
+        return rec + [0] * (-len(rec) % 4)
+
+    def align_prog():
+        prog.extend([0] * (-len(prog) % 4))
 
     TYPE_J, TYPE_T0, TYPE_O, TYPE_R = 0, 1, 2, 3
     for stage in range(1, k):
@@ -392,6 +402,7 @@ def emit_program(k):
                     continue
                 rev = tuple(reversed(s))
                 recs.append(cur_record(s, jo[s], jo[rev], (-1) ** (L + 1)))
+            align_prog()
             plist.append((TYPE_J, L, len(recs), len(prog), len(recs[0])))
             for r in recs:
                 prog += r
@@ -403,12 +414,14 @@ def emit_program(k):
             for i in range(L):
                 prev = -1 if i == 0 else oo[a[:i]]
                 rec += [prev, jo[a[i:]]]
-            recs.append(rec)
+            recs.append(pad4(rec))
+        align_prog()
         plist.append((TYPE_O, L, len(recs), len(prog), len(recs[0])))
         for r in recs:
             prog += r
         # t~ rows of every sequence of length `stage`
         recs = [[ro[b], jo[b]] for b in itertools.permutations(range(k), L)]
+        align_prog()
         plist.append((TYPE_R, L, len(recs), len(prog), 2))
         for r in recs:
             prog += r
@@ -420,6 +433,7 @@ def emit_program(k):
                     continue
                 rev = tuple(reversed(s))
                 recs.append(cur_record(s, pidx[s], pidx[rev], (-1) ** (k + 1)))
+            align_prog()
             plist.append((TYPE_T0, k, len(recs), len(prog), len(recs[0])))
             # T0 items write their value straight into the amplitude of the
             # helicity combination: hunpack[sigma][pattern] = gluon helicity bits
@@ -462,7 +476,9 @@ def emit_program(k):
     w(f"namespace rec{k} {{")
     w(f"constexpr int J_TOTAL = {J_TOTAL}, O_TOTAL = {O_TOTAL}, R_TOTAL = {R_TOTAL};")
     w(f"constexpr int NSTAGE = {k - 1}, NPART = {len(pdesc) // 5};")
-    w(_arr("prog", "int", prog))
+    body = ", ".join(str(int(v)) for v in prog)
+    w(f"__device__ __align__(16) const int prog[{len(prog)}] = {{{body}}};")
+    w(f"alignas(16) static const int prog_h[{len(prog)}] = {{{body}}};")
     w(_arr("pdesc", "int", pdesc))
     w(_arr("stage_first", "int", stage_first))
     # the same two tables as compile-time constants (the stage loops)

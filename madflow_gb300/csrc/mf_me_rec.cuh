@@ -27,8 +27,10 @@ template <int K> struct RecTraits;
 
 #ifdef __CUDA_ARCH__
 #define MF_TBL(NS, NAME, I) (NS::NAME[(I)])
+#define MF_TBLP(NS, NAME) (NS::NAME)
 #else
 #define MF_TBL(NS, NAME, I) (NS::NAME##_h[(I)])
+#define MF_TBLP(NS, NAME) (NS::NAME##_h)
 #endif
 
 #define MF_DEFINE_REC(KK)                                                                                 \
@@ -38,6 +40,9 @@ template <int K> struct RecTraits;
     static constexpr int NPERM = ttng##KK::NPERM, NCOMB = ttng##KK::NCOMB;                                \
     static constexpr double DENOMINATOR = ttng##KK::DENOMINATOR, COLOUR_DEN = ttng##KK::COLOUR_DEN;       \
     MF_D static int prog(int i) { return MF_TBL(rec##KK, prog, i); }                                      \
+    /* the 4-int group of the program at int index i (a multiple of 4) */                                  \
+    MF_D static int4 prog4(int i) { return reinterpret_cast<const int4*>(MF_TBLP(rec##KK, prog))[i >> 2]; } \
+    MF_D static int2 prog2(int i) { return reinterpret_cast<const int2*>(MF_TBLP(rec##KK, prog))[i >> 1]; } \
     MF_D static int pdesc(int i) { return MF_TBL(rec##KK, pdesc, i); }                                    \
     MF_D static int stage_first(int i) { return MF_TBL(rec##KK, stage_first, i); }                        \
     MF_D static int arec(int i) { return MF_TBL(rec##KK, arec, i); }                                      \
@@ -134,25 +139,28 @@ template <class T, int K> MF_D void rec_st_ext(RecWS<T, K>& ws, const PrepRec<T,
   }
 }
 
-// colour-ordered gluon current from a record (see codegen.emit_program)
+// colour-ordered gluon current from a record (see codegen.emit_program):
+// group i (1..L-1) of the record is split i, then one group per triple of the
+// contact term; m is the subset of the whole sequence
 template <class T, int K>
-MF_D W4<T> rec_current(const RecWS<T, K>& ws, const EvData<T, K>& ev, int r, int L, int hp) {
+MF_D W4<T> rec_current(const RecWS<T, K>& ws, const EvData<T, K>& ev, int r, int L, int m, int hp) {
   using R = RecTraits<K>;
   W4<T> a3 = w4zero<T>(), a4 = w4zero<T>();
-  int q = r + 4;
-  for (int i = 1; i < L; ++i, q += 4) {
-    W4<T> a = ws.J.get(R::prog(q) + (hp & ((1 << i) - 1)));
-    W4<T> b = ws.J.get(R::prog(q + 1) + (hp >> i));
-    vvv_add<T>(a, ev.Qg[R::prog(q + 2)], b, ev.Qg[R::prog(q + 3)], a3);
+  for (int i = 1; i < L; ++i) {
+    const int4 g = R::prog4(r + 4 * i);  // J offsets and subsets of both sides
+    W4<T> a = ws.J.get(g.x + (hp & ((1 << i) - 1)));
+    W4<T> b = ws.J.get(g.y + (hp >> i));
+    vvv_add<T>(a, ev.Qg[g.z], b, ev.Qg[g.w], a3);
   }
+  int q = r + 4 * L;
   for (int i = 1; i < L; ++i)
-    for (int j = i + 1; j < L; ++j, q += 3) {
-      W4<T> a = ws.J.get(R::prog(q) + (hp & ((1 << i) - 1)));
-      W4<T> b = ws.J.get(R::prog(q + 1) + ((hp >> i) & ((1 << (j - i)) - 1)));
-      W4<T> d = ws.J.get(R::prog(q + 2) + (hp >> j));
+    for (int j = i + 1; j < L; ++j, q += 4) {
+      const int4 t = R::prog4(q);
+      W4<T> a = ws.J.get(t.x + (hp & ((1 << i) - 1)));
+      W4<T> b = ws.J.get(t.y + ((hp >> i) & ((1 << (j - i)) - 1)));
+      W4<T> d = ws.J.get(t.z + (hp >> j));
       vvvv_add<T>(a, b, d, a4);
     }
-  int m = R::prog(r + 3);
   return combine<T>(ev.gv3[m], a3, ev.gv4[m], a4);
 }
 
@@ -177,12 +185,14 @@ MF_D void rec_item(RecWS<T, K>& ws, const EvData<T, K>& ev, int type, int L, int
   using R = RecTraits<K>;
   constexpr int NC = 1 << (K + 2);
   if (type == 0) {  // gluon current, written for s and reverse(s)
-    W4<T> v = rec_current<T, K>(ws, ev, r, L, sub);
-    ws.J.put(R::prog(r) + sub, v);
-    ws.J.put(R::prog(r + 1) + bit_reverse(sub, L), R::prog(r + 2) < 0 ? neg(v) : v);
+    const int4 h = R::prog4(r);  // out, reversed out, sign, subset
+    W4<T> v = rec_current<T, K>(ws, ev, r, L, h.w, sub);
+    ws.J.put(h.x + sub, v);
+    ws.J.put(h.y + bit_reverse(sub, L), h.z < 0 ? neg(v) : v);
   } else if (type == 1) {  // full length: bare contractions into the amplitudes
-    W4<T> Jf = rec_current<T, K>(ws, ev, r, K, sub);
-    const int s = R::prog(r), srev = R::prog(r + 1), sg = R::prog(r + 2);
+    const int4 h = R::prog4(r);  // ordering, reversed ordering, sign, subset
+    W4<T> Jf = rec_current<T, K>(ws, ev, r, K, h.w, sub);
+    const int s = h.x, srev = h.y, sg = h.z;
     const int hg = R::hunpack(s * (1 << K) + sub);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -191,20 +201,24 @@ MF_D void rec_item(RecWS<T, K>& ws, const EvData<T, K>& ev, int type, int L, int
       ws.A[s * NC + c] = t;
       ws.A[srev * NC + c] = sg < 0 ? -t : t;
     }
-  } else if (type == 2) {  // top-line current
+  } else if (type == 2) {  // top-line current: out, subset, then (previous, J suffix) per split
     const int ht = sub >> L, hp = sub & ((1 << L) - 1);
+    int4 g[(2 + 2 * (K - 1) + 3) / 4];
+    for (int k = 0; k < (2 + 2 * L + 3) / 4; ++k) g[k] = R::prog4(r + 4 * k);
+    const int* f = reinterpret_cast<const int*>(g);
     W4<T> y = w4zero<T>();
     for (int i = 0; i < L; ++i) {
-      int prev = R::prog(r + 2 + 2 * i), jsuf = R::prog(r + 3 + 2 * i);
+      const int prev = f[2 + 2 * i], jsuf = f[3 + 2 * i];
       W4<T> Jb = ws.J.get(jsuf + (hp >> i));
       if (prev < 0) sv_add<T>(Jb, ws.WT[ht], y);
       else sv_add<T>(Jb, ws.O.get(prev + (ht << i) + (hp & ((1 << i) - 1))), y);
     }
-    int m = R::prog(r + 1);
-    ws.O.put(R::prog(r) + sub, topprop<T>(ev.Qt[m], ev.mt, ev.tden[m], y));
-  } else {  // t~ row
+    const int m = f[1];
+    ws.O.put(f[0] + sub, topprop<T>(ev.Qt[m], ev.mt, ev.tden[m], y));
+  } else {  // t~ row: out, J
     const int htb = sub >> L, hp = sub & ((1 << L) - 1);
-    ws.RW.put(R::prog(r) + sub, sandwich_row(ws.WTB[htb], ws.J.get(R::prog(r + 1) + hp)));
+    const int2 g = R::prog2(r);
+    ws.RW.put(g.x + sub, sandwich_row(ws.WTB[htb], ws.J.get(g.y + hp)));
   }
 }
 
