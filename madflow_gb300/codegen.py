@@ -484,7 +484,9 @@ def emit_program(k):
     # the same two tables as compile-time constants (the stage loops)
     w(f"constexpr int pdesc_c[{len(pdesc)}] = {{{', '.join(str(int(v)) for v in pdesc)}}};")
     w(f"constexpr int stage_first_c[{len(stage_first)}] = {{{', '.join(str(int(v)) for v in stage_first)}}};")
-    w(_arr("arec", "int", arec))
+    body = ", ".join(str(int(v)) for v in arec)
+    w(f"__device__ __align__(8) const int arec[{len(arec)}] = {{{body}}};")
+    w(f"alignas(8) static const int arec_h[{len(arec)}] = {{{body}}};")
     w(_arr("hpack", "unsigned char", hpack))
     w(_arr("hunpack", "unsigned char", hunpack))
     w(_arr("jo_ext", "int", [jo[(q,)] for q in range(k)]))

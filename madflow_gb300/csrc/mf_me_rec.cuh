@@ -18,6 +18,7 @@
 // The stage functions are host-callable so the CPU test suite can run them
 // one thread at a time against the oracle.
 #pragma once
+#include <cstddef>
 #include <type_traits>
 #include "mf_helas.cuh"
 #include "mf_phasespace.cuh"
@@ -46,6 +47,7 @@ template <int K> struct RecTraits;
     MF_D static int pdesc(int i) { return MF_TBL(rec##KK, pdesc, i); }                                    \
     MF_D static int stage_first(int i) { return MF_TBL(rec##KK, stage_first, i); }                        \
     MF_D static int arec(int i) { return MF_TBL(rec##KK, arec, i); }                                      \
+    MF_D static int2 arec2(int i) { return reinterpret_cast<const int2*>(MF_TBLP(rec##KK, arec))[i >> 1]; } \
     MF_D static int hpack(int i) { return MF_TBL(rec##KK, hpack, i); }                                    \
     MF_D static int hunpack(int i) { return MF_TBL(rec##KK, hunpack, i); }                                \
     MF_D static int jo_ext(int i) { return MF_TBL(rec##KK, jo_ext, i); }                                  \
@@ -136,6 +138,36 @@ template <class T, int K> MF_D void rec_st_ext(RecWS<T, K>& ws, const PrepRec<T,
     if (i < 2 * K) ws.J.put(R::jo_ext(i >> 1) + (i & 1), pr.G[i >> 1][i & 1]);
     else if (i < 2 * K + 2) ws.WT[i - 2 * K] = pr.WT[i - 2 * K];
     else ws.WTB[i - 2 * K - 2] = pr.WTB[i - 2 * K - 2];
+  }
+}
+
+// The record of one event straight to where the stages read it: the
+// per-event data to pr, the gluon wavefunctions to their J slots and the
+// quark spinors to ws.WT / ws.WTB (record load and stage 0 in one pass).
+// NT threads, tid in [0, NT).
+template <class T, int K, int NT>
+MF_D void rec_load(RecWS<T, K>& ws, PrepRec<T, K>& pr, const int4* __restrict__ src, int tid) {
+  using R = RecTraits<K>;
+  using P = PrepRec<T, K>;
+  constexpr int NW = (int)(sizeof(P) / 16), NPL = (int)(sizeof(W4<T>) / 16);
+  constexpr int OG = (int)(offsetof(P, G) / 16), OWT = (int)(offsetof(P, WT) / 16);
+  constexpr int OWTB = (int)(offsetof(P, WTB) / 16), OEND = OWTB + 2 * NPL;
+  static_assert(OWT == OG + 2 * K * NPL && OWTB == OWT + 2 * NPL, "record layout");
+  int4* dpr = reinterpret_cast<int4*>(&pr);
+  int4* dwt = reinterpret_cast<int4*>(ws.WT);
+  int4* dwtb = reinterpret_cast<int4*>(ws.WTB);
+  for (int w = tid; w < NW; w += NT) {
+    const int4 v = src[w];
+    if (w < OG || w >= OEND) {
+      dpr[w] = v;
+    } else if (w < OWT) {
+      const int idx = w - OG, wv = idx / NPL;
+      ws.J.pl[idx % NPL][R::jo_ext(wv >> 1) + (wv & 1)] = v;
+    } else if (w < OWTB) {
+      dwt[w - OWT] = v;
+    } else {
+      dwtb[w - OWTB] = v;
+    }
   }
 }
 
@@ -290,7 +322,8 @@ template <class T, int K> MF_D void rec_st_A(RecWS<T, K>& ws, int tid, int nt) {
     for (int q = 0; q < 4; ++q) a[q] = ws.A[s * NC + (hg | ((q & 1) << K) | ((q >> 1) << (K + 1)))];
 #pragma unroll
     for (int i = 1; i < K; ++i) {
-      const int oo = R::arec(s * 2 * (K - 1) + 2 * (i - 1)), ro = R::arec(s * 2 * (K - 1) + 2 * (i - 1) + 1);
+      const int2 orr = R::arec2(s * 2 * (K - 1) + 2 * (i - 1));  // top current, t~ row
+      const int oo = orr.x, ro = orr.y;
       const int lo = hfull & ((1 << i) - 1), hi = hfull >> i;
       W4<T> O0 = ws.O.get(oo + lo), O1 = ws.O.get(oo + (1 << i) + lo);
       W4<T> R0 = ws.RW.get(ro + hi), R1 = ws.RW.get(ro + (1 << (K - i)) + hi);
@@ -439,11 +472,7 @@ __global__ void __launch_bounds__(128) prep_kernel(const double* __restrict__ ps
 // Returns |M|^2 in thread 0.
 template <class T, int K, int NT> MF_DO double me_rec_event(RecSmem<T, K>& S, const int4* __restrict__ rec, int tid) {
   constexpr int nt = NT;
-  constexpr int NW = prep_words<T, K>();
-  int4* dst = reinterpret_cast<int4*>(&S.pr);
-  for (int w = tid; w < NW; w += nt) dst[w] = rec[w];
-  __syncthreads();
-  rec_st_ext<T, K>(S.ws, S.pr, tid, nt);
+  rec_load<T, K, NT>(S.ws, S.pr, rec, tid);
   __syncthreads();
   rec_stages_c<T, K, 1, NT>(S.ws, S.pr.ev, tid);
   rec_st_A<T, K>(S.ws, tid, nt);
@@ -531,11 +560,7 @@ __global__ void __launch_bounds__(MF_GWS_NT)
       continue;
     }
     __syncthreads();
-    int4* dst = reinterpret_cast<int4*>(&S.pr);
-    const int4* src = prep + e * NW;
-    for (int w = tid; w < NW; w += nt) dst[w] = src[w];
-    __syncthreads();
-    rec_st_ext<T, K>(ws, S.pr, tid, nt);
+    rec_load<T, K, nt>(ws, S.pr, prep + e * NW, tid);
     __syncthreads();
     rec_stages_c<T, K, 1, nt>(ws, S.pr.ev, tid);
     rec_st_A<T, K>(ws, tid, nt);
@@ -700,13 +725,7 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     }
     return e;
   };
-  auto load_ext = [&](int64_t e) {
-    int4* dst = reinterpret_cast<int4*>(&S.pr);
-    const int4* src = prep + e * NW;
-    for (int w = tid; w < NW; w += nt) dst[w] = src[w];
-    __syncthreads();
-    rec_st_ext<T, K>(S.ws, S.pr, tid, nt);
-  };
+  auto load_ext = [&](int64_t e) { rec_load<T, K, nt>(S.ws, S.pr, prep + e * NW, tid); };
   int64_t e = next_event(blockIdx.x);
   if (e < N) load_ext(e);
   while (e < N) {
@@ -849,13 +868,7 @@ __global__ void __launch_bounds__(MF_REC_NT, 4)
     if (ev[0] < 0) break;
     const int64_t e = ev[sub];
     const bool on = e >= 0;
-    if (on) {
-      int4* dst = reinterpret_cast<int4*>(&S.pr);
-      const int4* src = prep + e * NW;
-      for (int w = lt; w < NW; w += TPE) dst[w] = src[w];
-    }
-    __syncthreads();
-    if (on) rec_st_ext<T, K>(S.ws, S.pr, lt, TPE);
+    if (on) rec_load<T, K, TPE>(S.ws, S.pr, prep + e * NW, lt);
     __syncthreads();
     rec_stages_c<T, K, 1, TPE>(S.ws, S.pr.ev, lt, on);
     if (on) rec_st_A<T, K>(S.ws, lt, TPE);
