@@ -36,7 +36,7 @@ ALG_FLOPS = {2: 23601.0, 3: 356161.0, 4: 5744961.0, 5: 102333185.0}
 # Flops per phase-space point the helicity-recycling kernel executes (same
 # counting convention), counted by running its stage functions with the
 # counting scalar (tests/test_flop_counts.py).
-REC_FLOPS = {2: 5817.0, 3: 58190.0, 4: 745707.0, 5: 13242912.0}
+REC_FLOPS = {2: 6297.0, 3: 53550.0, 4: 698059.0, 5: 12752896.0}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max clock
 
 

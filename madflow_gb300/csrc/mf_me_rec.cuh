@@ -127,6 +127,15 @@ MF_D void prep_event(PrepRec<T, K>& r, const double (*p)[4], double mt, double w
     r.WT[b] = oxxxxx<T>(r.ev.pext[2], r.ev.mt, b ? T(1) : T(-1), T(1));
     r.WTB[b] = ixxxxx<T>(r.ev.pext[3], r.ev.mt, b ? T(1) : T(-1), T(-1));
   }
+  // the top-line bilinears of the four (top, anti-top) spin combinations,
+  // M[q][mu] = WTB[q>>1]^T S(e_mu) WT[q&1]: an amplitude in which the full
+  // gluon current J meets the top line directly is J . M (S is linear in J)
+  for (int q = 0; q < 4; ++q)
+    for (int mu = 0; mu < 4; ++mu) {
+      W4<T> e = w4zero<T>();
+      e.v[mu] = cx<T>{T(1), T(0)};
+      r.ev.M[q][mu] = dot4(sandwich_row(r.WTB[q >> 1], e), r.WT[q & 1]);
+    }
   r.scale = (c11.re * c11.re + c11.im * c11.im) / (R::COLOUR_DEN * R::DENOMINATOR);
 }
 
@@ -196,21 +205,6 @@ MF_D W4<T> rec_current(const RecWS<T, K>& ws, const EvData<T, K>& ev, int r, int
   return combine<T>(ev.gv3[m], a3, ev.gv4[m], a4);
 }
 
-// row vector r = F1^T S(V), so that F1^T S(V) F2 = r . F2
-template <class T> MF_D W4<T> sandwich_row(const W4<T>& F1, const W4<T>& V) {
-  cx<T> p03 = V.v[0] + V.v[3], m03 = V.v[0] - V.v[3];
-  cx<T> p12 = V.v[1] + mul_i(V.v[2]), m12 = V.v[1] - mul_i(V.v[2]);
-  W4<T> r;
-  r.v[0] = F1.v[2] * m03 - F1.v[3] * m12;
-  r.v[1] = F1.v[3] * p03 - F1.v[2] * p12;
-  r.v[2] = F1.v[0] * p03 + F1.v[1] * m12;
-  r.v[3] = F1.v[0] * p12 + F1.v[1] * m03;
-  return r;
-}
-template <class T> MF_D cx<T> dot4(const W4<T>& a, const W4<T>& b) {
-  return a.v[0] * b.v[0] + a.v[1] * b.v[1] + a.v[2] * b.v[2] + a.v[3] * b.v[3];
-}
-
 // one item of a program part
 template <class T, int K>
 MF_D void rec_item(RecWS<T, K>& ws, const EvData<T, K>& ev, int type, int L, int r, int sub) {
@@ -228,7 +222,7 @@ MF_D void rec_item(RecWS<T, K>& ws, const EvData<T, K>& ev, int type, int L, int
     const int hg = R::hunpack(s * (1 << K) + sub);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      cx<T> t = dot4(sandwich_row(ws.WTB[q >> 1], Jf), ws.WT[q & 1]);
+      const cx<T> t = Jf.v[0] * ev.M[q][0] + Jf.v[1] * ev.M[q][1] + Jf.v[2] * ev.M[q][2] + Jf.v[3] * ev.M[q][3];
       int c = hg | ((q & 1) << K) | ((q >> 1) << (K + 1));
       ws.A[s * NC + c] = t;
       ws.A[srev * NC + c] = sg < 0 ? -t : t;
@@ -274,27 +268,87 @@ MF_D void rec_stage(RecWS<T, K>& ws, const EvData<T, K>& ev, int stage, int tid,
   }
 }
 
+// Two top-line items of a part that differ in the top spin (type 2) or the
+// anti-top spin (type 3) only: sub and sub + 2^L, sub < 2^L.  They share
+// their gluon-current loads and the spin-independent products of those.
+// Same results as rec_item on each.  (Pairing the gluon-current items the
+// same way was measured slower: the paired currents need more registers.)
+template <class T, int K, int TYPE, int L>
+MF_D void rec_item2(RecWS<T, K>& ws, const EvData<T, K>& ev, int r, int sub) {
+  using R = RecTraits<K>;
+  static_assert(TYPE == 2 || TYPE == 3, "top-line items only");
+  if constexpr (TYPE == 2) {
+    const int hp = sub;  // top spin 0; its partner has top spin 1
+    int4 g[(2 + 2 * L + 3) / 4];
+#pragma unroll
+    for (int k = 0; k < (2 + 2 * L + 3) / 4; ++k) g[k] = R::prog4(r + 4 * k);
+    const int* f = reinterpret_cast<const int*>(g);
+    W4<T> y0 = w4zero<T>(), y1 = w4zero<T>();
+#pragma unroll
+    for (int i = 0; i < L; ++i) {
+      const int prev = f[2 + 2 * i], jsuf = f[3 + 2 * i];
+      const W4<T> Jb = ws.J.get(jsuf + (hp >> i));
+      if (prev < 0) {
+        sv_add<T>(Jb, ws.WT[0], y0);
+        sv_add<T>(Jb, ws.WT[1], y1);
+      } else {
+        const int o = prev + (hp & ((1 << i) - 1));
+        sv_add<T>(Jb, ws.O.get(o), y0);
+        sv_add<T>(Jb, ws.O.get(o + (1 << i)), y1);
+      }
+    }
+    const int m = f[1];
+    ws.O.put(f[0] + hp, topprop<T>(ev.Qt[m], ev.mt, ev.tden[m], y0));
+    ws.O.put(f[0] + hp + (1 << L), topprop<T>(ev.Qt[m], ev.mt, ev.tden[m], y1));
+  } else {
+    const int2 g = R::prog2(r);  // out, J
+    const W4<T> V = ws.J.get(g.y + sub);
+    ws.RW.put(g.x + sub, sandwich_row(ws.WTB[0], V));
+    ws.RW.put(g.x + sub + (1 << L), sandwich_row(ws.WTB[1], V));
+  }
+}
+
+// items in parts P..PEND-1 of the part table
+template <int K, int P, int PEND> MF_HD constexpr int rec_part_items() {
+  using R = RecTraits<K>;
+  if constexpr (P < PEND) {
+    constexpr int type = R::pdesc_c(5 * P), L = R::pdesc_c(5 * P + 1);
+    return (R::pdesc_c(5 * P + 2) << ((type <= 1) ? L : L + 1)) + rec_part_items<K, P + 1, PEND>();
+  } else {
+    return 0;
+  }
+}
+
 // The same stage with the part table folded in at compile time (part P of
-// stage STAGE; the item loops keep their run-time node index only).
-template <class T, int K, int P, int PEND, int NT>
+// stage STAGE; the item loops keep their run-time node index only).  With
+// PAIR each thread takes the top-line items two at a time (rec_item2): used
+// where the stage has more items than threads.
+template <class T, int K, int P, int PEND, int NT, bool PAIR>
 MF_D void rec_stage_parts(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid, int base) {
   if constexpr (P < PEND) {
     using R = RecTraits<K>;
     constexpr int type = R::pdesc_c(5 * P), L = R::pdesc_c(5 * P + 1);
-    constexpr int lper = (type <= 1) ? L : L + 1;
+    constexpr bool pair = PAIR && type >= 2;
+    constexpr int lper = ((type <= 1) ? L : L + 1) - (pair ? 1 : 0);
     constexpr int cnt = R::pdesc_c(5 * P + 2) << lper;
     constexpr int rec0 = R::pdesc_c(5 * P + 3), rsz = R::pdesc_c(5 * P + 4);
     int first = (tid - base) % NT;
     if (first < 0) first += NT;
-    for (int local = first; local < cnt; local += NT)
-      rec_item<T, K>(ws, ev, type, L, rec0 + (local >> lper) * rsz, local & ((1 << lper) - 1));
-    rec_stage_parts<T, K, P + 1, PEND, NT>(ws, ev, tid, base + cnt);
+    for (int local = first; local < cnt; local += NT) {
+      if constexpr (pair)
+        rec_item2<T, K, type, L>(ws, ev, rec0 + (local >> lper) * rsz, local & ((1 << lper) - 1));
+      else
+        rec_item<T, K>(ws, ev, type, L, rec0 + (local >> lper) * rsz, local & ((1 << lper) - 1));
+    }
+    rec_stage_parts<T, K, P + 1, PEND, NT, PAIR>(ws, ev, tid, base + cnt);
   }
 }
 template <class T, int K, int STAGE, int NT>
 MF_D void rec_stage_c(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid) {
   using R = RecTraits<K>;
-  rec_stage_parts<T, K, R::stage_first_c(STAGE - 1), R::stage_first_c(STAGE), NT>(ws, ev, tid, 0);
+  constexpr int P0 = R::stage_first_c(STAGE - 1), P1 = R::stage_first_c(STAGE);
+  constexpr bool PAIR = rec_part_items<K, P0, P1>() > NT;
+  rec_stage_parts<T, K, P0, P1, NT, PAIR>(ws, ev, tid, 0);
 }
 // stages STAGE..K-1, each followed by a block barrier; a thread with on =
 // false only takes part in the barriers
@@ -430,6 +484,22 @@ template <class T, int K> struct RecHostRun {
     double tot = 0.0;
     for (int t = 0; t < nt; ++t) tot += (double)rec_st_colour<T, K>(ws, t, nt);
     return tot;
+  }
+  // the same through the compile-time stage driver the kernels use (with
+  // NT threads: every stage with more than NT items runs paired items)
+  template <int NT> static double run_c(RecWS<T, K>& ws, const PrepRec<T, K>& pr) {
+    for (int t = 0; t < NT; ++t) rec_st_ext<T, K>(ws, pr, t, NT);
+    stages_c<1, NT>(ws, pr.ev);
+    for (int t = 0; t < NT; ++t) rec_st_A<T, K>(ws, t, NT);
+    double tot = 0.0;
+    for (int t = 0; t < NT; ++t) tot += (double)rec_st_colour<T, K>(ws, t, NT);
+    return tot;
+  }
+  template <int ST, int NT> static void stages_c(RecWS<T, K>& ws, const EvData<T, K>& ev) {
+    if constexpr (ST < K) {
+      for (int t = 0; t < NT; ++t) rec_stage_c<T, K, ST, NT>(ws, ev, t);
+      stages_c<ST + 1, NT>(ws, ev);
+    }
   }
 };
 

@@ -76,6 +76,21 @@ template <class T> MF_D cx<T> sandwich(const W4<T>& F1, const W4<T>& V, const W4
   return F1.v[0] * y.v[0] + F1.v[1] * y.v[1] + F1.v[2] * y.v[2] + F1.v[3] * y.v[3];
 }
 
+// row vector r = F1^T S(V), so that F1^T S(V) F2 = r . F2
+template <class T> MF_D W4<T> sandwich_row(const W4<T>& F1, const W4<T>& V) {
+  cx<T> p03 = V.v[0] + V.v[3], m03 = V.v[0] - V.v[3];
+  cx<T> p12 = V.v[1] + mul_i(V.v[2]), m12 = V.v[1] - mul_i(V.v[2]);
+  W4<T> r;
+  r.v[0] = F1.v[2] * m03 - F1.v[3] * m12;
+  r.v[1] = F1.v[3] * p03 - F1.v[2] * p12;
+  r.v[2] = F1.v[0] * p03 + F1.v[1] * m12;
+  r.v[3] = F1.v[0] * p12 + F1.v[1] * m03;
+  return r;
+}
+template <class T> MF_D cx<T> dot4(const W4<T>& a, const W4<T>& b) {
+  return a.v[0] * b.v[0] + a.v[1] * b.v[1] + a.v[2] * b.v[2] + a.v[3] * b.v[3];
+}
+
 // Per-event data shared by all helicities of one event: slot momenta of every
 // subset of gluons (Qg) and of the top line (Qt = p_t + Qg), and the
 // propagator x coupling factors, evaluated in FP64 (double-float for T =
@@ -87,6 +102,7 @@ template <class T, int K> struct EvData {
   cx<T> gv4[1 << K];   // -i GC_12 / Qg^2
   cx<T> tden[1 << K];  // i GC_11 / (Qt^2 - M^2 + i M W)
   T pext[K + 2][4];    // external momenta
+  cx<T> M[4][4];       // WTB[q>>1]^T S(e_mu) WT[q&1]: the top-line bilinears
   T mt;
 };
 

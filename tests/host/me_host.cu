@@ -19,7 +19,8 @@ MF_DEFINE_REC(5)
 
 // |M|^2 of one event; hel_out (optional) [ncomb] in MadGraph helicity order.
 template <int K, class T>
-static double smatrix_one(const double* p, const double* coup, double mt, double wt, double* hel_out) {
+static double smatrix_one(const double* p, const double* coup, double mt, double wt, double* hel_out,
+                          bool compiled = false) {
   using R = RecTraits<K>;
   auto ws = std::make_unique<RecWS<T, K>>();
   auto pr = std::make_unique<PrepRec<T, K>>();
@@ -28,7 +29,7 @@ static double smatrix_one(const double* p, const double* coup, double mt, double
   cx<double> c10 = {coup[0], coup[1]}, c11 = {coup[2], coup[3]}, c12 = {coup[4], coup[5]};
   prep_event<T, K>(*pr, pd, mt, wt, c10, c11, c12);
   const int nt = 7;  // an odd "block size" exercises the item striding
-  double tot = RecHostRun<T, K>::run(*ws, *pr, nt);
+  double tot = compiled ? RecHostRun<T, K>::template run_c<7>(*ws, *pr) : RecHostRun<T, K>::run(*ws, *pr, nt);
   double sc = pr->scale;
   if (hel_out)
     for (int c = 0; c < (1 << (K + 2)); ++c)
@@ -45,6 +46,22 @@ extern "C" int me_host_smatrix(int k, int prec, const double* p, int64_t N, cons
     else if (k == 3) out[e] = prec ? smatrix_one<3, float>(pe, coup, mt, wt, nullptr) : smatrix_one<3, double>(pe, coup, mt, wt, nullptr);
     else if (k == 4) out[e] = prec ? smatrix_one<4, float>(pe, coup, mt, wt, nullptr) : smatrix_one<4, double>(pe, coup, mt, wt, nullptr);
     else if (k == 5) out[e] = prec ? smatrix_one<5, float>(pe, coup, mt, wt, nullptr) : smatrix_one<5, double>(pe, coup, mt, wt, nullptr);
+    else return 1;
+  }
+  return 0;
+}
+
+// The same through the kernels' compile-time stage driver (paired items in
+// every stage with more than 7 items).
+extern "C" int me_host_smatrix_compiled(int k, int prec, const double* p, int64_t N, const double* coup, double mt,
+                                        double wt, double* out) {
+  int np = k + 2;
+  for (int64_t e = 0; e < N; ++e) {
+    const double* pe = p + 4 * np * e;
+    if (k == 2) out[e] = prec ? smatrix_one<2, float>(pe, coup, mt, wt, nullptr, true) : smatrix_one<2, double>(pe, coup, mt, wt, nullptr, true);
+    else if (k == 3) out[e] = prec ? smatrix_one<3, float>(pe, coup, mt, wt, nullptr, true) : smatrix_one<3, double>(pe, coup, mt, wt, nullptr, true);
+    else if (k == 4) out[e] = prec ? smatrix_one<4, float>(pe, coup, mt, wt, nullptr, true) : smatrix_one<4, double>(pe, coup, mt, wt, nullptr, true);
+    else if (k == 5) out[e] = prec ? smatrix_one<5, float>(pe, coup, mt, wt, nullptr, true) : smatrix_one<5, double>(pe, coup, mt, wt, nullptr, true);
     else return 1;
   }
   return 0;

@@ -53,7 +53,8 @@ def _dp(a):
 
 @pytest.mark.parametrize("k", [2, 3, 4, 5])
 def test_generated_recursion_vs_oracle(host_lib, oracle, k):
-    """FP64 generated code within 1e-12 of the oracle; FP32 (mixed) within 5e-5."""
+    """FP64 generated code within 1e-12 of the oracle; FP32 (mixed) within 5e-5; through the
+    run-time stage loop and through the kernels' compile-time driver with paired items."""
     T = oracle.TTNG(k)
     prm = T.params(MT, WT, GC10, GC11, GC12)
     rng = np.random.default_rng(11 + k)
@@ -62,11 +63,12 @@ def test_generated_recursion_vs_oracle(host_lib, oracle, k):
     coup = np.array([GC10.real, 0.0, 0.0, GC11.imag, 0.0, GC12.imag])
     me0 = T.smatrix(p, prm)
     for prec, tol in ((0, 1e-12), (1, 5e-5)):
-        out = np.zeros(len(p))
-        pc = np.ascontiguousarray(p)
-        host_lib.me_host_smatrix(k, prec, _dp(pc), ctypes.c_int64(len(p)), _dp(coup), ctypes.c_double(MT),
-                                 ctypes.c_double(WT), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
-        assert np.max(np.abs(out / me0 - 1)) < tol, (k, prec)
+        for fn in (host_lib.me_host_smatrix, host_lib.me_host_smatrix_compiled):
+            out = np.zeros(len(p))
+            pc = np.ascontiguousarray(p)
+            fn(k, prec, _dp(pc), ctypes.c_int64(len(p)), _dp(coup), ctypes.c_double(MT), ctypes.c_double(WT),
+               out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+            assert np.max(np.abs(out / me0 - 1)) < tol, (k, prec, fn.__name__)
 
 
 @pytest.mark.parametrize("k", [2, 3, 4, 5])
