@@ -33,10 +33,10 @@ CUTS = dict(ptmin=60.0, etamax=2.5, drmin=0.4)
 # div/sqrt/log 1), counted by the oracle's counting scalar
 # (tests/test_flop_counts.py keeps these in step with it).
 ALG_FLOPS = {2: 23601.0, 3: 356161.0, 4: 5744961.0, 5: 102333185.0}
-# Flops per phase-space point the helicity-recycling kernel executes (same
-# counting convention), counted by running its stage functions with the
+# Flops per phase-space point the helicity-recycling FP32 kernel executes
+# (same counting convention), counted by running its stage functions with the
 # counting scalar (tests/test_flop_counts.py).
-REC_FLOPS = {2: 6297.0, 3: 53550.0, 4: 698059.0, 5: 12752896.0}
+REC_FLOPS = {2: 6249.0, 3: 52830.0, 4: 688555.0, 5: 12619936.0}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max clock
 
 

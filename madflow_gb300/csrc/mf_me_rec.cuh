@@ -191,7 +191,12 @@ MF_D W4<T> rec_current(const RecWS<T, K>& ws, const EvData<T, K>& ev, int r, int
     const int4 g = R::prog4(r + 4 * i);  // J offsets and subsets of both sides
     W4<T> a = ws.J.get(g.x + (hp & ((1 << i) - 1)));
     W4<T> b = ws.J.get(g.y + (hp >> i));
-    vvv_add<T>(a, ev.Qg[g.z], b, ev.Qg[g.w], a3);
+    // FP32: the conserved-current form (what it drops is zero up to
+    // rounding); FP64 keeps every term (a counting scalar counts the FP32 form)
+    if constexpr (!std::is_same<T, double>::value)
+      vvv_add_cons<T>(a, ev.Qg[g.z], b, ev.Qg[g.w], a3);
+    else
+      vvv_add<T>(a, ev.Qg[g.z], b, ev.Qg[g.w], a3);
   }
   int q = r + 4 * L;
   for (int i = 1; i < L; ++i)

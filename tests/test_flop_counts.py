@@ -1,6 +1,6 @@
 """The per-event flop counts bench.py reports: the algorithmic count equals
 the oracle's counting-scalar evaluation, the recycled count the product's
-stage functions run with a counting scalar."""
+stage functions run with a counting scalar (in the form of the FP32 kernel)."""
 import ctypes
 
 import numpy as np
