@@ -43,7 +43,7 @@ struct IterArgs {
   float* u_out;        // optional [ndim][N] uniforms
   double* ps_out;      // optional [N][K+2][4] lab-frame momenta of the passing events (event output)
   // pipeline buffers (scratch)
-  double* state;            // [4(K)+6][N] first-pass state (ps_state_words)
+  double* state;            // [4K+16][N] first-pass state (ps_state_words)
   int4* prep;              // [N] per-event records (PrepRec), passing events only
   double* pref;            // [N]
   unsigned char* bins;     // [ndim][N]
@@ -54,8 +54,9 @@ constexpr int MF_MAX_DIM = 32;
 
 // Per-event state of the first pass, stored SoA [ps_state_words][N]: the
 // massless rambo momenta of the K outgoing particles [K][4], its log-weight,
-// s-hat, the x1 x2 weight, x1, x2 and the VEGAS jacobian.
-template <int K> MF_HD constexpr int ps_state_words() { return 4 * K + 6; }
+// s-hat, the x1 x2 weight, x1, x2, the VEGAS jacobian and (batch Newton
+// rule) the Newton iterates x_0 .. x_9.
+template <int K> MF_HD constexpr int ps_state_words() { return 4 * K + 16; }
 
 // Uniforms of dimensions 2j, 2j+1 of an event: 53-bit in FP64, 24-bit in
 // FP32 (the high words of the same Philox4x32-10 block, so an FP32 uniform
@@ -143,11 +144,11 @@ MF_DO void event_massless(const IterArgs& A, int npart, const P* x, double w0, d
 // (2 pi)^(3 nout - 4).  Returns false when the event fails the cuts.
 template <class P>
 MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (*p)[4], double logw, double shat,
-                        double wgt, double x1, double x2, P v, double pw, double& wgt_lum) {
+                        double wgt, double x1, double x2, P v, double pw, double& wgt_lum, double x_start = -1.0) {
   MfConsts KC = mf_consts(A.f32q != 0);
   int nout = npart - 2;
   double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
-  logw = rambo_massive<P>(nout, A.masses, p + 2, roots, logw, KC.acc, newton_iters);
+  logw = rambo_massive<P>(nout, A.masses, p + 2, roots, logw, KC.acc, newton_iters, x_start);
   double wps = (double)ps_exp((P)logw) / pw;
   double ein = roots / 2.0;
   p[0][0] = ein; p[0][1] = 0.0; p[0][2] = 0.0; p[0][3] = ein;
@@ -209,7 +210,7 @@ template <int K, class P> __global__ void __launch_bounds__(256) ps_seed_kernel(
     if (batch_rule) {
       const int lim = min(local, *(volatile int*)kmin);
       const double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
-      const int c = newton_conv_iter(K, A.masses, p + 2, roots, KC.acc, lim);
+      const int c = newton_conv_iter_xs(K, A.masses, p + 2, roots, KC.acc, lim, st + (int64_t)(4 * K + 6) * N, N);
       if (c < lim) {
         local = c;
         atomicMin(kmin, c);
@@ -240,7 +241,10 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
     const double logw = st[(int64_t)(4 * K) * N], shat = st[(int64_t)(4 * K + 1) * N];
     const double wgt = st[(int64_t)(4 * K + 2) * N], x1 = st[(int64_t)(4 * K + 3) * N];
     const double x2 = st[(int64_t)(4 * K + 4) * N], jac = st[(int64_t)(4 * K + 5) * N];
-    bool ok = event_finish<T>(A, NPART, niter, p, logw, shat, wgt, x1, x2, v, pw, wl);
+    // batch rule: one step from the first pass's x_(niter-1) (the steps
+    // before it are the ones the first pass took)
+    const double xs = niter > 0 ? st[(int64_t)(4 * K + 6 + niter - 1) * N] : -1.0;
+    bool ok = event_finish<T>(A, NPART, niter > 0 ? 1 : niter, p, logw, shat, wgt, x1, x2, v, pw, wl, xs);
     A.pref[e] = ok ? jac * wl : 0.0;
     if (A.ps_out) {
       // madflow's all_ps (com_output=False): lab frame, FP64

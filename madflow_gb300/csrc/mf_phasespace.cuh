@@ -124,13 +124,33 @@ MF_HD int newton_conv_iter(int n, const double* masses, const double (*p)[4], do
   return lim < 11 ? lim : 11;
 }
 
+// newton_conv_iter that also keeps the iterates: xs[j * stride] = x after j
+// steps (x_0 the starting value), for j = 0 .. min(steps taken, 9).  The
+// steps of an event are those of rambo_massive, so the second pass can
+// resume from x_(n-1) instead of repeating n-1 steps.
+MF_HD int newton_conv_iter_xs(int n, const double* masses, const double (*p)[4], double sqrts, double acc, int lim,
+                              double* xs, int64_t stride) {
+  double m2[MF_MAX_OUT], e2[MF_MAX_OUT], newE[MF_MAX_OUT], tm = 0.0;
+  for (int i = 0; i < n; ++i) { m2[i] = masses[i] * masses[i]; e2[i] = p[i][0] * p[i][0]; tm += masses[i]; }
+  double r = tm / sqrts;
+  double xf = sqrt(1.0 - r * r);
+  xs[0] = xf;
+  const int last = lim - 1 < 10 ? lim - 1 : 10;
+  for (int it = 1; it <= last; ++it) {
+    if (!newton_step(n, m2, e2, sqrts, acc, xf, newE)) return it;
+    if (it <= 9) xs[it * stride] = xf;
+  }
+  return lim < 11 ? lim : 11;
+}
+
 // Massive correction of rambo (phasespace.py:194-212) running `iters` Newton
-// iterations (iters <= 0: iterate this event to its own convergence).
+// iterations (iters <= 0: iterate this event to its own convergence) from
+// x_start (< 0: the rule's starting value sqrt(1 - (sum m / sqrts)^2)).
 // Rescales p in place and returns the final log-weight.
 // The weight factors run in W (the momenta and the Newton solve stay FP64).
 template <class W = double>
 MF_HD double rambo_massive(int n, const double* masses, double (*p)[4], double sqrts, double logw, double acc,
-                           int iters) {
+                           int iters, double x_start = -1.0) {
   double m2[MF_MAX_OUT], e2[MF_MAX_OUT], newE[MF_MAX_OUT], tm = 0.0;
   for (int i = 0; i < n; ++i) {
     m2[i] = masses[i] * masses[i];
@@ -139,7 +159,7 @@ MF_HD double rambo_massive(int n, const double* masses, double (*p)[4], double s
     tm += masses[i];
   }
   double r = tm / sqrts;
-  double xf = sqrt(1.0 - r * r);
+  double xf = x_start >= 0.0 ? x_start : sqrt(1.0 - r * r);
   if (iters > 0) {
     for (int it = 0; it < iters; ++it) newton_step(n, m2, e2, sqrts, acc, xf, newE);
   } else {
