@@ -135,7 +135,7 @@ MF_DO void event_massless(const IterArgs& A, int npart, const P* x, double w0, d
   double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
   double q[MF_MAX_OUT][4];
   rambo_generate<P>(xr, npart - 2, (P)KC.pi, q);
-  logw = rambo_conformal(q, npart - 2, roots, w0, p + 2);
+  logw = rambo_conformal<sizeof(P) == 4>(q, npart - 2, roots, w0, p + 2);
 }
 
 // Rest of the phase space of one event: massive correction with
@@ -210,7 +210,8 @@ template <int K, class P> __global__ void __launch_bounds__(256) ps_seed_kernel(
     if (batch_rule) {
       const int lim = min(local, *(volatile int*)kmin);
       const double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
-      const int c = newton_conv_iter_xs(K, A.masses, p + 2, roots, KC.acc, lim, st + (int64_t)(4 * K + 6) * N, N);
+      const int c = newton_conv_iter_xs<sizeof(P) == 4>(K, A.masses, p + 2, roots, KC.acc, lim,
+                                                         st + (int64_t)(4 * K + 6) * N, N);
       if (c < lim) {
         local = c;
         atomicMin(kmin, c);

@@ -63,14 +63,24 @@ MF_HD double rambo_w0(int n, double pi) {
 // Conformal transformation and scaling of rambo (phasespace.py:166-192),
 // FP64: p [n][4] from q; returns the log-weight before the massive
 // correction (w0 = rambo_w0(n, pi)).
+// FAST (the mixed-precision path): one reciprocal of the mass instead of
+// five divisions and the log of sqrts in FP32 (the log-weight is used in
+// FP32 there).
+template <bool FAST = false>
 MF_HD double rambo_conformal(const double (*q)[4], int n, double sqrts, double w0, double (*p)[4]) {
   double sum[4] = {0, 0, 0, 0};
   for (int i = 0; i < n; ++i)
     for (int k = 0; k < 4; ++k) sum[k] += q[i][k];
   double qmass = sqrt(sum[0] * sum[0] - (sum[1] * sum[1] + sum[2] * sum[2] + sum[3] * sum[3]));
-  double xs = sqrts / qmass;
-  double b[4];
-  for (int k = 0; k < 4; ++k) b[k] = -sum[k] / qmass;
+  double xs, b[4];
+  if constexpr (FAST) {
+    const double iq = 1.0 / qmass;
+    xs = sqrts * iq;
+    for (int k = 0; k < 4; ++k) b[k] = -sum[k] * iq;
+  } else {
+    xs = sqrts / qmass;
+    for (int k = 0; k < 4; ++k) b[k] = -sum[k] / qmass;
+  }
   double gamma = -b[0];
   double a = 1.0 / (1.0 + gamma);
   for (int i = 0; i < n; ++i) {
@@ -81,7 +91,10 @@ MF_HD double rambo_conformal(const double (*q)[4], int n, double sqrts, double w
     p[i][3] = (q[i][3] + b[3] * tmp) * xs;
     p[i][0] = (q[i][0] * gamma + bq) * xs;
   }
-  return w0 + (double)(2 * n - 4) * log(sqrts);
+  if constexpr (FAST)
+    return w0 + (double)((float)(2 * n - 4) * logf((float)sqrts));
+  else
+    return w0 + (double)(2 * n - 4) * log(sqrts);
 }
 
 // rambo without the massive correction (FP64): p [n][4]; returns the
@@ -92,16 +105,37 @@ MF_HD double rambo_massless(const double* x, int n, double sqrts, double pi, dou
   return rambo_conformal(q, n, sqrts, rambo_w0(n, pi), p);
 }
 
-// One Newton step of _massive_xfactor (phasespace.py:77-92).
-MF_HD bool newton_step(int n, const double* m2, const double* e2, double sqrts, double acc, double& xf, double* newE) {
+// One Newton step of _massive_xfactor (phasespace.py:77-92).  FAST (the
+// mixed-precision path): a massless particle's energy is |E| x and its
+// derivative term E^2 / (|E| x) = |E| / x, so the massless particles cost one
+// division together and no square root (e: the energies |E|).
+template <bool FAST = false>
+MF_HD bool newton_step(int n, const double* m2, const double* e2, double sqrts, double acc, double& xf, double* newE,
+                       const double* e = nullptr) {
   double x2 = xf * xf;
   double f0 = 0.0, g0 = 0.0;
-  for (int i = 0; i < n; ++i) {
-    newE[i] = sqrt(m2[i] + e2[i] * x2);
-    f0 += newE[i];
+  if constexpr (FAST) {
+    double el = 0.0;
+    for (int i = 0; i < n; ++i) {
+      if (m2[i] == 0.0) {
+        newE[i] = e[i] * xf;
+        el += e[i];
+      } else {
+        newE[i] = sqrt(m2[i] + e2[i] * x2);
+        g0 += e2[i] / newE[i];
+      }
+      f0 += newE[i];
+    }
+    f0 = f0 - sqrts;
+    g0 += el / xf;
+  } else {
+    for (int i = 0; i < n; ++i) {
+      newE[i] = sqrt(m2[i] + e2[i] * x2);
+      f0 += newE[i];
+    }
+    f0 = f0 - sqrts;
+    for (int i = 0; i < n; ++i) g0 += e2[i] / newE[i];
   }
-  f0 = f0 - sqrts;
-  for (int i = 0; i < n; ++i) g0 += e2[i] / newE[i];
   double nx = xf - f0 / (xf * g0);
   bool unconverged = f0 > acc;
   if (unconverged) xf = nx;
@@ -128,16 +162,22 @@ MF_HD int newton_conv_iter(int n, const double* masses, const double (*p)[4], do
 // steps (x_0 the starting value), for j = 0 .. min(steps taken, 9).  The
 // steps of an event are those of rambo_massive, so the second pass can
 // resume from x_(n-1) instead of repeating n-1 steps.
+template <bool FAST = false>
 MF_HD int newton_conv_iter_xs(int n, const double* masses, const double (*p)[4], double sqrts, double acc, int lim,
                               double* xs, int64_t stride) {
-  double m2[MF_MAX_OUT], e2[MF_MAX_OUT], newE[MF_MAX_OUT], tm = 0.0;
-  for (int i = 0; i < n; ++i) { m2[i] = masses[i] * masses[i]; e2[i] = p[i][0] * p[i][0]; tm += masses[i]; }
+  double m2[MF_MAX_OUT], e2[MF_MAX_OUT], ea[MF_MAX_OUT], newE[MF_MAX_OUT], tm = 0.0;
+  for (int i = 0; i < n; ++i) {
+    m2[i] = masses[i] * masses[i];
+    e2[i] = p[i][0] * p[i][0];
+    ea[i] = fabs(p[i][0]);
+    tm += masses[i];
+  }
   double r = tm / sqrts;
   double xf = sqrt(1.0 - r * r);
   xs[0] = xf;
   const int last = lim - 1 < 10 ? lim - 1 : 10;
   for (int it = 1; it <= last; ++it) {
-    if (!newton_step(n, m2, e2, sqrts, acc, xf, newE)) return it;
+    if (!newton_step<FAST>(n, m2, e2, sqrts, acc, xf, newE, ea)) return it;
     if (it <= 9) xs[it * stride] = xf;
   }
   return lim < 11 ? lim : 11;
@@ -148,23 +188,26 @@ MF_HD int newton_conv_iter_xs(int n, const double* masses, const double (*p)[4],
 // x_start (< 0: the rule's starting value sqrt(1 - (sum m / sqrts)^2)).
 // Rescales p in place and returns the final log-weight.
 // The weight factors run in W (the momenta and the Newton solve stay FP64).
+// With W = float (the mixed-precision path) the Newton steps are FAST ones.
 template <class W = double>
 MF_HD double rambo_massive(int n, const double* masses, double (*p)[4], double sqrts, double logw, double acc,
                            int iters, double x_start = -1.0) {
-  double m2[MF_MAX_OUT], e2[MF_MAX_OUT], newE[MF_MAX_OUT], tm = 0.0;
+  constexpr bool FAST = sizeof(W) == 4;
+  double m2[MF_MAX_OUT], e2[MF_MAX_OUT], ea[MF_MAX_OUT], newE[MF_MAX_OUT], tm = 0.0;
   for (int i = 0; i < n; ++i) {
     m2[i] = masses[i] * masses[i];
     e2[i] = p[i][0] * p[i][0];
+    ea[i] = fabs(p[i][0]);
     newE[i] = p[i][0];
     tm += masses[i];
   }
   double r = tm / sqrts;
   double xf = x_start >= 0.0 ? x_start : sqrt(1.0 - r * r);
   if (iters > 0) {
-    for (int it = 0; it < iters; ++it) newton_step(n, m2, e2, sqrts, acc, xf, newE);
+    for (int it = 0; it < iters; ++it) newton_step<FAST>(n, m2, e2, sqrts, acc, xf, newE, ea);
   } else {
     for (int it = 0; it < 10; ++it)
-      if (!newton_step(n, m2, e2, sqrts, acc, xf, newE)) break;
+      if (!newton_step<FAST>(n, m2, e2, sqrts, acc, xf, newE, ea)) break;
   }
   W wt2 = W(1), wt3 = W(0);
   for (int i = 0; i < n; ++i) {
