@@ -9,6 +9,14 @@ template <int K, class T> static int rec_smem_bytes() { return (int)sizeof(RecSm
 template <int K, class T> constexpr bool rec_in_smem() { return sizeof(RecSmem<T, K>) <= 200 * 1024; }
 // blocks of the global-workspace kernel per SM (its workspaces are allocated per block)
 constexpr int MF_GWS_PER_SM = 1;
+// resident blocks per SM of the record-writing kernels (ps_iter_kernel,
+// prep_kernel): each thread builds its 1.5 KB record in local memory, and
+// with more blocks the local working set spills out of L1 and L2 (measured:
+// 2 blocks of 128 threads per SM 10.6 ms, 3 or more 11.8 ms, 1 15.1 ms per
+// 10^7 gg > tt~gg events)
+#ifndef MF_PS_BLOCKS_PER_SM
+#define MF_PS_BLOCKS_PER_SM 2
+#endif
 
 static int sm_count() {
   int dev = 0, sms = 0;
@@ -104,7 +112,7 @@ static int sm_count() {
   }                                                                                                            \
   int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,    \
                            int64_t cstride, int4* prep, cudaStream_t st) {                                     \
-    int64_t b = (N + 127) / 128, cap = (int64_t)sm_count() * 16;                                               \
+    int64_t b = (N + 127) / 128, cap = (int64_t)sm_count() * MF_PS_BLOCKS_PER_SM;                              \
     if (b > cap) b = cap;                                                                                      \
     if (b < 1) b = 1;                                                                                          \
     if (prec == 0) prep_kernel<KK, double><<<(int)b, 128, 0, st>>>(ps, N, mt, wt, coup, cstride, prep);       \
@@ -113,7 +121,7 @@ static int sm_count() {
   }                                                                                                            \
   int mf_launch_ps_k##KK(int prec, const IterArgs& A, cudaStream_t st) {                                       \
     int64_t b = (A.N + 127) / 128;                                                                             \
-    int64_t cap = (int64_t)sm_count() * 16;                                                                    \
+    int64_t cap = (int64_t)sm_count() * MF_PS_BLOCKS_PER_SM;                                                   \
     if (b > cap) b = cap;                                                                                      \
     if (b < 1) b = 1;                                                                                          \
     if (prec == 0) ps_iter_kernel<KK, double><<<(int)b, 128, 0, st>>>(A);                                      \
