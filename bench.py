@@ -479,11 +479,11 @@ def main():
     ap.add_argument("--flow-hidden", type=int, default=64)
     ap.add_argument("--flow-batch", type=int, default=2_000_000)
     ap.add_argument("--flow-minibatch", type=int, default=200_000)
-    ap.add_argument("--flow-resample", type=int, default=200_000)
-    ap.add_argument("--flow-lr", type=float, default=5e-3)
+    ap.add_argument("--flow-resample", type=int, default=100_000)
+    ap.add_argument("--flow-lr", type=float, default=1e-2)
     ap.add_argument("--flow-train-batches", type=int, default=20)
     ap.add_argument("--flow-vegas-iters", type=int, default=5)
-    ap.add_argument("--flow-vegas-events", type=int, default=4_000_000)
+    ap.add_argument("--flow-vegas-events", type=int, default=2_000_000)
     ap.add_argument("--precision-points", type=int, default=1_000_000)
     ap.add_argument("--e2e-events", type=int, default=4_000_000)
     ap.add_argument("--e2e-reps", type=int, default=3)
