@@ -327,7 +327,7 @@ template <int K, int P, int PEND> MF_HD constexpr int rec_part_items() {
 // The same stage with the part table folded in at compile time (part P of
 // stage STAGE; the item loops keep their run-time node index only).  With
 // PAIR each thread takes the top-line items two at a time (rec_item2): used
-// where the stage has more items than threads.
+// for four or more gluons where the stage has more items than threads.
 template <class T, int K, int P, int PEND, int NT, bool PAIR>
 MF_D void rec_stage_parts(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid, int base) {
   if constexpr (P < PEND) {
@@ -352,7 +352,8 @@ template <class T, int K, int STAGE, int NT>
 MF_D void rec_stage_c(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid) {
   using R = RecTraits<K>;
   constexpr int P0 = R::stage_first_c(STAGE - 1), P1 = R::stage_first_c(STAGE);
-  constexpr bool PAIR = rec_part_items<K, P0, P1>() > NT;
+  // (measured: pairs pay from four gluons on; with three they cost 17-24%)
+  constexpr bool PAIR = K >= 4 && rec_part_items<K, P0, P1>() > NT;
   rec_stage_parts<T, K, P0, P1, NT, PAIR>(ws, ev, tid, 0);
 }
 // stages STAGE..K-1, each followed by a block barrier; a thread with on =

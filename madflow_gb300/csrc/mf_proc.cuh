@@ -17,6 +17,9 @@ constexpr int MF_GWS_PER_SM = 1;
 #ifndef MF_PS_BLOCKS_PER_SM
 #define MF_PS_BLOCKS_PER_SM 2
 #endif
+#ifndef MF_PREP_BLOCKS_PER_SM
+#define MF_PREP_BLOCKS_PER_SM 2
+#endif
 
 static int sm_count() {
   int dev = 0, sms = 0;
@@ -112,7 +115,7 @@ static int sm_count() {
   }                                                                                                            \
   int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,    \
                            int64_t cstride, int4* prep, cudaStream_t st) {                                     \
-    int64_t b = (N + 127) / 128, cap = (int64_t)sm_count() * MF_PS_BLOCKS_PER_SM;                              \
+    int64_t b = (N + 127) / 128, cap = (int64_t)sm_count() * MF_PREP_BLOCKS_PER_SM;                            \
     if (b > cap) b = cap;                                                                                      \
     if (b < 1) b = 1;                                                                                          \
     if (prec == 0) prep_kernel<KK, double><<<(int)b, 128, 0, st>>>(ps, N, mt, wt, coup, cstride, prep);       \
