@@ -37,7 +37,14 @@ ALG_FLOPS = {2: 23601.0, 3: 356161.0, 4: 5744961.0, 5: 102333185.0}
 # (same counting convention), counted by running its stage functions with the
 # counting scalar (tests/test_flop_counts.py).
 REC_FLOPS = {2: 6249.0, 3: 52830.0, 4: 688555.0, 5: 12619936.0}
+# Bytes of the FP32 per-event record the matrix-element kernel reads (PrepRec)
+REC_BYTES = {4: 1536}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max clock
+# DRAM bytes (read + write) of the matrix-element kernel per passing event:
+# one ncu capture of 10^6 points (profiles/me_rec_kernel_ggttxgg_mixed.md,
+# 1.2147 GB over 760,841 events); the kernel's traffic is its records, so it
+# scales with the events of a launch
+ME_DRAM_BYTES_PER_EVENT = 1596.5
 
 
 def workload(events):
@@ -250,7 +257,10 @@ def run_gpu(args):
                 "d2h_bytes_per_step": int(f_host.numel() * 8), "api": "FusedIntegrand(x) -> f, host buffers",
                 "events_per_step": e2e_n},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-                     "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": None,
+                     "frac": achieved / FP32_NOMINAL_TFLOPS,
+                     "traffic": ME_DRAM_BYTES_PER_EVENT * statistics.mean(int(n) for n in npass.tolist()),
+                     "traffic_unit": "bytes per launch (ncu, 10^6-point capture scaled by the events per launch)",
+                     "algorithmic_bytes_per_event": REC_BYTES[4],
                      "kernel": "me_rec_kernel<4,float,%d>" % tune["colour"],
                      "peak_source": "nominal FP32 SIMT (152 SMs x 128 lanes x 2 x 2.07 GHz); "
                                     "MEASURED_PEAKS.json holds no FP32 figure",
