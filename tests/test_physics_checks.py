@@ -89,3 +89,54 @@ def test_ggttx_analytic(oracle):
     g4 = GC11.imag**4
     ana = g4 * (1 / (6 * t1 * t2) - 3.0 / 8) * (t1**2 + t2**2 + rho - rho**2 / (4 * t1 * t2))
     np.testing.assert_allclose(me, ana, rtol=1e-12)
+
+
+def _lorentz(rng):
+    """A random proper Lorentz transformation: rotation about a random axis,
+    then a boost of speed < 0.8 along another random axis."""
+    ax = rng.normal(size=3)
+    ax /= np.linalg.norm(ax)
+    th = rng.uniform(0, 2 * np.pi)
+    K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+    R = np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K
+    n = rng.normal(size=3)
+    n /= np.linalg.norm(n)
+    b = rng.uniform(0.1, 0.8)
+    g = 1 / np.sqrt(1 - b * b)
+    L = np.eye(4)
+    L[0, 0] = g
+    L[0, 1:] = L[1:, 0] = g * b * n
+    L[1:, 1:] = np.eye(3) + (g - 1) * np.outer(n, n)
+    Rf = np.eye(4)
+    Rf[1:, 1:] = R
+    return L @ Rf
+
+
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
+def test_lorentz_invariance(oracle, host_lib, k):
+    """|M|^2 summed over helicities is Lorentz invariant: the oracle and the
+    product's generated evaluation (host harness, FP64) give the same value
+    for boosted and rotated momenta.  Zero top width: a fixed width in the
+    t-channel propagators breaks gauge invariance, and the sum over physical
+    gluon polarisations then depends on the frame (at 2e-5 for some points).
+    On-shell momenta: Newton iterated per event (the batch rule leaves the
+    slowest events of a batch slightly off shell)."""
+    import ctypes
+
+    T = oracle.TTNG(k)
+    prm = T.params(MT, 0.0, GC10, GC11, GC12)
+    rng = np.random.default_rng(40 + k)
+    x = rng.uniform(size=(64, 4 * k + 2))
+    p, *_ = oracle.ramboflow(x, k + 2, 13000.0, [MT, MT] + [0.0] * (k - 2), rule=oracle.NEWTON_PER_EVENT)
+    q = np.einsum("ab,neb->nea", _lorentz(rng), p)
+    for mom in (p, q):  # momentum conservation survives the transformation
+        assert np.abs(mom[:, :2].sum(1) - mom[:, 2:].sum(1)).max() < 1e-9 * 13000.0
+    me_p, me_q = T.smatrix(p, prm), T.smatrix(q, prm)
+    assert rel_err(me_q, me_p) < 1e-10
+    dp = ctypes.POINTER(ctypes.c_double)
+    coup = np.array([GC10.real, 0.0, 0.0, GC11.imag, 0.0, GC12.imag])
+    out = np.zeros(len(q))
+    qc = np.ascontiguousarray(q)
+    host_lib.me_host_smatrix(k, 0, qc.ctypes.data_as(dp), ctypes.c_int64(len(q)), coup.ctypes.data_as(dp),
+                             ctypes.c_double(MT), ctypes.c_double(0.0), out.ctypes.data_as(dp))
+    assert rel_err(out, me_p) < 1e-10
