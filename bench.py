@@ -489,7 +489,7 @@ def main():
     ap.add_argument("--flow-hidden", type=int, default=64)
     ap.add_argument("--flow-batch", type=int, default=2_000_000)
     ap.add_argument("--flow-minibatch", type=int, default=200_000)
-    ap.add_argument("--flow-resample", type=int, default=100_000)
+    ap.add_argument("--flow-resample", type=int, default=50_000)
     ap.add_argument("--flow-lr", type=float, default=1e-2)
     ap.add_argument("--flow-train-batches", type=int, default=20)
     ap.add_argument("--flow-vegas-iters", type=int, default=5)

@@ -155,6 +155,17 @@ def _clamp_open(x, eps=1e-7):
     return x.clamp(eps, 1.0 - eps)
 
 
+def _backward(flow, loss):
+    """loss.backward() with the conditioner's GEMMs in the flow's precision
+    (TF32 tensor cores when the flow runs its forward GEMMs in TF32)."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = bool(getattr(flow, "tf32", False)) or prev
+    try:
+        loss.backward()
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
 def _train_step(flow, opt, x, w, minibatch, resample=0):
     """Variance-loss updates on one batch (x, w = f/q) drawn from the flow.
 
@@ -176,7 +187,7 @@ def _train_step(flow, opt, x, w, minibatch, resample=0):
         for s in range(0, resample, minibatch):
             loss = -flow.log_prob(xs[s: s + minibatch]).mean()
             opt.zero_grad(set_to_none=True)
-            loss.backward()
+            _backward(flow, loss)
             opt.step()
         return
     mean_w = w.mean()
@@ -187,7 +198,7 @@ def _train_step(flow, opt, x, w, minibatch, resample=0):
         wm = w[s: s + minibatch]
         loss = -((wm * wm / scale).float() * lq).mean()
         opt.zero_grad(set_to_none=True)
-        loss.backward()
+        _backward(flow, loss)
         opt.step()
 
 
