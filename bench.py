@@ -487,7 +487,7 @@ def main():
     ap.add_argument("--flow-bins", type=int, default=8)
     ap.add_argument("--flow-bf16", action="store_true", help="bf16 MLP GEMMs (default TF32)")
     ap.add_argument("--flow-hidden", type=int, default=64)
-    ap.add_argument("--flow-batch", type=int, default=2_000_000)
+    ap.add_argument("--flow-batch", type=int, default=1_000_000)
     ap.add_argument("--flow-minibatch", type=int, default=200_000)
     ap.add_argument("--flow-resample", type=int, default=50_000)
     ap.add_argument("--flow-lr", type=float, default=1e-2)

@@ -282,6 +282,20 @@ int mf_flow_inv(const float* u, const float* params, int64_t n, int nb, int K, f
                 void* stream);
 int mf_flow_grad(const float* x, const float* params, const float* gy, const float* glogdet, int64_t n, int nb, int K,
                  float* gx, float* gparams, void* stream);
+/* One whole coupling layer of the sampling direction in one kernel on the
+ * tensor cores (tcgen05, TF32 operands, FP32 accumulation): the conditioner
+ * MLP na -> 64 -> 64 -> nb (2K+1) with ReLU, then the inverse transform of
+ * the nb transformed dimensions.  z [N][dim] float32 points, updated in place
+ * on the dimensions ib [nb] (int32); the MLP reads the dimensions ia [na] as
+ * 2 z - 1.  W1 [64][na], b1 [64], W2 [64][64], b2 [64], W3 [nb (2K+1)][64],
+ * b3 [nb (2K+1)] in torch.nn.Linear layout (out x in); logq [N] += the sum of
+ * log pdf.  1 <= na, nb <= 16, na + nb <= dim, K in {4, 8, 16},
+ * nb (2K+1) <= 256.  err: device int set to 1 if a bounded tensor-core wait
+ * ran out (the layer is then incomplete), 2 if the library was built without
+ * the tensor-core instructions.  Needs an sm_103 GPU. */
+int mf_flow_inv_layer_tc(float* z, int64_t n, int dim, const int* ia, int na, const int* ib, int nb, int K,
+                         const float* W1, const float* b1, const float* W2, const float* b2, const float* W3,
+                         const float* b3, float* logq, int* err, void* stream);
 
 #ifdef __cplusplus
 }

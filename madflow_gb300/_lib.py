@@ -97,6 +97,8 @@ _SIGS = {
     "mf_pq_forward": (c_int, [c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
     "mf_pq_inverse": (c_int, [c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
     "mf_pq_backward": (c_int, [c_dp, c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
+    "mf_flow_inv_layer_tc": (c_int, [c_dp, c_int64, c_int, c_dp, c_int, c_dp, c_int, c_int, c_dp, c_dp, c_dp, c_dp,
+                                     c_dp, c_dp, c_dp, c_dp, c_void_p]),
 }
 
 

@@ -1,0 +1,355 @@
+// One coupling layer of the normalizing-flow sampler in the sampling
+// direction, fused in one kernel on the 5th-generation tensor cores: the
+// conditioner MLP (na -> 64 -> 64 -> nb (2K+1), ReLU) as three tcgen05
+// kind::tf32 GEMMs with FP32 accumulators in tensor memory, and the inverse
+// piecewise-quadratic transform (Mueller et al., ACM TOG 38 (2019) 145) of
+// the nb transformed dimensions in the epilogue.  The activations of a tile of
+// 128 points stay on chip (tensor memory and shared memory); z is read and
+// written once.
+//
+// Block: 128 threads, thread r owns point r of the tile (tensor-memory lane
+// r).  Shared memory: the three weight matrices as B operands (K-major, no
+// swizzle, 8-row x 16-byte core matrices, LBO 128 bytes along K, SBO
+// (K/4) x 128 bytes between 8-row groups), loaded once per block; the A
+// operands (the conditioning inputs 2z - 1, padded to K = 16, and the hidden
+// activations, K = 64); the biases.  Tensor memory: 256 columns (D1 at 0,
+// D2 at 64, D3 at 0 once D1 and D2 have been read).  Every wait on the MMA
+// completion is bounded (1000 tries of <= 1 ms); one that runs out sets *err,
+// the block stops and frees its tensor memory.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/madflow_gb300.h"
+#include "mf_tcgen05.cuh"
+
+namespace {
+
+constexpr int FH = 64;        // hidden units
+constexpr int FTILE = 128;    // points per tile (MMA M)
+constexpr int FK1 = 16;       // padded conditioning inputs (GEMM1 K)
+constexpr int FTMEM = 256;    // tensor-memory columns per block
+constexpr int FMAXN3 = 256;   // nb (2K+1) padded to 16, at most
+
+// float offset of element (r, k) in a K-major canonical operand with kdim
+// columns
+__host__ __device__ __forceinline__ int canon(int r, int k, int kdim) {
+  return (r >> 3) * (kdim / 4) * 32 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3);
+}
+
+struct FlowTcSmem {
+  float* B1;  // [64][16]
+  float* B2;  // [64][64]
+  float* B3;  // [n3p][64]
+  float* A1;  // [128][16]
+  float* A2;  // [128][64]
+  float* bias;  // b1[64] b2[64] b3[n3p]
+  int* idx;     // ia[16] ib[16]
+  unsigned long long* mbar;
+  uint32_t* tmem;
+  int* bad;
+};
+
+__host__ __device__ inline size_t flow_tc_smem_bytes(int n3p) {
+  size_t f = (size_t)FH * FK1 + FH * FH + (size_t)n3p * FH + FTILE * FK1 + FTILE * FH + 2 * FH + n3p;
+  size_t b = f * 4 + 32 * 4 + 64;
+  b = (b + 1023) / 1024 * 1024 + 1024;  // alignment slack
+  // at least 80 KB, so that at most two blocks (2 x 256 tensor-memory
+  // columns) share an SM
+  return b < 80 * 1024 ? 80 * 1024 : b;
+}
+
+#if MF_TCGEN05
+MF_DO void tc_ld_x1(uint32_t taddr, float& v) {
+  uint32_t r;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(r) : "r"(taddr) : "memory");
+  v = __uint_as_float(r);
+}
+
+// bounded wait for the MMA group committed to bar (all threads of the block
+// call it with the same parity; the result is block-uniform)
+MF_DO bool flow_tc_wait(unsigned long long* bar, uint32_t parity, int* bad) {
+  bool done = false;
+  for (uint32_t spin = 0; spin < 1000u && !done; ++spin) done = tc_mbar_try_wait(bar, parity, 1000000u);
+  if (!done) atomicExch(bad, 1);
+  __syncthreads();
+  return *(volatile int*)bad == 0;
+}
+
+// inverse piecewise-quadratic transform of one dimension from its 2K+1 raw
+// parameters (softmax widths, exp heights normalised to unit area)
+template <int K> MF_DO float pq_inverse_one(const float* p, float u, float& logpdf) {
+  float W[K], V[K + 1];
+  float m = p[0];
+#pragma unroll
+  for (int k = 1; k < K; ++k) m = fmaxf(m, p[k]);
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    W[k] = __expf(p[k] - m);
+    s += W[k];
+  }
+  const float inv = 1.f / s;
+#pragma unroll
+  for (int k = 0; k < K; ++k) W[k] *= inv;
+  float mv = p[K];
+#pragma unroll
+  for (int k = 1; k <= K; ++k) mv = fmaxf(mv, p[K + k]);
+#pragma unroll
+  for (int k = 0; k <= K; ++k) V[k] = __expf(p[K + k] - mv);
+  float norm = 0.f;
+#pragma unroll
+  for (int k = 0; k < K; ++k) norm += 0.5f * (V[k] + V[k + 1]) * W[k];
+  const float in = 1.f / norm;
+#pragma unroll
+  for (int k = 0; k <= K; ++k) V[k] *= in;
+  // the bin of u: the last edge whose CDF is <= u (CDF at the left edges)
+  u = fminf(fmaxf(u, 0.f), 1.f);
+  float Eb = 0.f, Cb = 0.f, Wb = W[0], Vb = V[0], Vn = V[1];
+  float E = 0.f, C = 0.f;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    if (k > 0 && u >= C) {
+      Eb = E;
+      Cb = C;
+      Wb = W[k];
+      Vb = V[k];
+      Vn = V[k + 1];
+    }
+    E += W[k];
+    C += 0.5f * (V[k] + V[k + 1]) * W[k];
+  }
+  const float r = fmaxf(u - Cb, 0.f);
+  const float D = Vn - Vb;
+  const float a = 0.5f * Wb * D, bq = Wb * Vb;
+  float alpha = 2.f * r / (bq + sqrtf(fmaxf(bq * bq + 4.f * a * r, 0.f)));
+  alpha = fminf(fmaxf(alpha, 0.f), 1.f);
+  logpdf = __logf(Vb + alpha * D);
+  return fminf(Eb + alpha * Wb, 1.f);
+}
+#endif
+
+template <int K>
+__global__ void __launch_bounds__(FTILE) flow_inv_layer_tc_kernel(float* __restrict__ z, int64_t n, int dim,
+                                                                  const int* __restrict__ ia, int na,
+                                                                  const int* __restrict__ ib, int nb,
+                                                                  const float* __restrict__ W1,
+                                                                  const float* __restrict__ b1,
+                                                                  const float* __restrict__ W2,
+                                                                  const float* __restrict__ b2,
+                                                                  const float* __restrict__ W3,
+                                                                  const float* __restrict__ b3, int n3p,
+                                                                  float* __restrict__ logq, int* __restrict__ err) {
+#if MF_TCGEN05
+  constexpr int NP = 2 * K + 1;
+  const int n3 = nb * NP;
+  extern __shared__ __align__(1024) unsigned char fsm[];
+  uintptr_t base = (reinterpret_cast<uintptr_t>(fsm) + 1023) & ~(uintptr_t)1023;
+  FlowTcSmem S;
+  S.B1 = reinterpret_cast<float*>(base);
+  S.B2 = S.B1 + FH * FK1;
+  S.B3 = S.B2 + FH * FH;
+  S.A1 = S.B3 + n3p * FH;
+  S.A2 = S.A1 + FTILE * FK1;
+  S.bias = S.A2 + FTILE * FH;
+  S.idx = reinterpret_cast<int*>(S.bias + 2 * FH + n3p);
+  S.mbar = reinterpret_cast<unsigned long long*>(S.idx + 32);
+  S.tmem = reinterpret_cast<uint32_t*>(S.mbar + 1);
+  S.bad = reinterpret_cast<int*>(S.tmem + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  // weights into the canonical B layouts (zero padding), biases, indices
+  for (int i = tid; i < FH * FK1; i += FTILE) {
+    const int r = i / FK1, k = i % FK1;
+    S.B1[canon(r, k, FK1)] = k < na ? W1[r * na + k] : 0.f;
+  }
+  for (int i = tid; i < FH * FH; i += FTILE) S.B2[canon(i / FH, i % FH, FH)] = W2[i];
+  for (int i = tid; i < n3p * FH; i += FTILE) {
+    const int r = i / FH, k = i % FH;
+    S.B3[canon(r, k, FH)] = r < n3 ? W3[r * FH + k] : 0.f;
+  }
+  for (int i = tid; i < FH; i += FTILE) {
+    S.bias[i] = b1[i];
+    S.bias[FH + i] = b2[i];
+  }
+  for (int i = tid; i < n3p; i += FTILE) S.bias[2 * FH + i] = i < n3 ? b3[i] : 0.f;
+  if (tid < 16) {
+    S.idx[tid] = tid < na ? ia[tid] : 0;
+    S.idx[16 + tid] = tid < nb ? ib[tid] : 0;
+  }
+  if (warp == 0) tc_tmem_alloc(S.tmem, FTMEM);
+  if (tid == 0) {
+    tc_mbar_init(S.mbar, 1);
+    *S.bad = 0;
+  }
+  tc_fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = *S.tmem;
+  const uint32_t lane_base = tm + ((uint32_t)(32 * warp) << 16);
+  const uint32_t a1 = tc_smem_u32(S.A1), a2 = tc_smem_u32(S.A2);
+  const uint32_t w1 = tc_smem_u32(S.B1), w2 = tc_smem_u32(S.B2), w3 = tc_smem_u32(S.B3);
+  constexpr uint32_t L = 128, SB1 = (FK1 / 4) * 128, SB2 = (FH / 4) * 128;
+  const uint32_t id64 = tc_idesc_tf32(FTILE, FH), id3 = tc_idesc_tf32(FTILE, n3p);
+  uint32_t phase = 0;
+  const int64_t ntiles = (n + FTILE - 1) / FTILE;
+
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t e = t * FTILE + tid;
+    const bool valid = e < n;
+    float* zr = z + (valid ? e : 0) * dim;
+    // A1: the conditioning inputs 2 z - 1 (zero beyond na and n)
+#pragma unroll
+    for (int k = 0; k < FK1; k += 4) {
+      float4 v;
+      v.x = (valid && k + 0 < na) ? 2.f * zr[S.idx[k + 0]] - 1.f : 0.f;
+      v.y = (valid && k + 1 < na) ? 2.f * zr[S.idx[k + 1]] - 1.f : 0.f;
+      v.z = (valid && k + 2 < na) ? 2.f * zr[S.idx[k + 2]] - 1.f : 0.f;
+      v.w = (valid && k + 3 < na) ? 2.f * zr[S.idx[k + 3]] - 1.f : 0.f;
+      *reinterpret_cast<float4*>(S.A1 + canon(tid, k, FK1)) = v;
+    }
+    tc_fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    // GEMM1: D1 [128][64] = A1 [128][16] B1^T
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int s = 0; s < FK1 / 8; ++s)
+        tc_mma_tf32(tm, tc_smem_desc(a1 + 256 * s, L, SB1), tc_smem_desc(w1 + 256 * s, L, SB1), id64, s > 0);
+      tc_commit(S.mbar);
+    }
+    if (!flow_tc_wait(S.mbar, phase, S.bad)) break;
+    phase ^= 1u;
+    tc_fence_after();
+    // hidden layer 1 -> A2
+#pragma unroll
+    for (int c = 0; c < FH; c += 16) {
+      float d[16];
+      tc_ld_x16(lane_base + c, d);
+      tc_wait_ld();
+#pragma unroll
+      for (int j = 0; j < 16; j += 4) {
+        float4 v;
+        v.x = fmaxf(d[j + 0] + S.bias[c + j + 0], 0.f);
+        v.y = fmaxf(d[j + 1] + S.bias[c + j + 1], 0.f);
+        v.z = fmaxf(d[j + 2] + S.bias[c + j + 2], 0.f);
+        v.w = fmaxf(d[j + 3] + S.bias[c + j + 3], 0.f);
+        *reinterpret_cast<float4*>(S.A2 + canon(tid, c + j, FH)) = v;
+      }
+    }
+    tc_fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    // GEMM2: D2 [128][64] (columns 64..127) = A2 B2^T
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int s = 0; s < FH / 8; ++s)
+        tc_mma_tf32(tm + FH, tc_smem_desc(a2 + 256 * s, L, SB2), tc_smem_desc(w2 + 256 * s, L, SB2), id64, s > 0);
+      tc_commit(S.mbar);
+    }
+    if (!flow_tc_wait(S.mbar, phase, S.bad)) break;
+    phase ^= 1u;
+    tc_fence_after();
+    // hidden layer 2 -> A2 (GEMM2 has read it)
+#pragma unroll
+    for (int c = 0; c < FH; c += 16) {
+      float d[16];
+      tc_ld_x16(lane_base + FH + c, d);
+      tc_wait_ld();
+#pragma unroll
+      for (int j = 0; j < 16; j += 4) {
+        float4 v;
+        v.x = fmaxf(d[j + 0] + S.bias[FH + c + j + 0], 0.f);
+        v.y = fmaxf(d[j + 1] + S.bias[FH + c + j + 1], 0.f);
+        v.z = fmaxf(d[j + 2] + S.bias[FH + c + j + 2], 0.f);
+        v.w = fmaxf(d[j + 3] + S.bias[FH + c + j + 3], 0.f);
+        *reinterpret_cast<float4*>(S.A2 + canon(tid, c + j, FH)) = v;
+      }
+    }
+    tc_fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    // GEMM3: D3 [128][n3p] (columns 0..n3p-1) = A2 B3^T
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int s = 0; s < FH / 8; ++s)
+        tc_mma_tf32(tm, tc_smem_desc(a2 + 256 * s, L, SB2), tc_smem_desc(w3 + 256 * s, L, SB2), id3, s > 0);
+      tc_commit(S.mbar);
+    }
+    if (!flow_tc_wait(S.mbar, phase, S.bad)) break;
+    phase ^= 1u;
+    tc_fence_after();
+    // epilogue: the inverse transform of each transformed dimension
+    float ld = 0.f;
+    for (int d = 0; d < nb; ++d) {
+      float p[NP];
+#pragma unroll
+      for (int j = 0; j < NP; ++j) tc_ld_x1(lane_base + d * NP + j, p[j]);
+      tc_wait_ld();
+#pragma unroll
+      for (int j = 0; j < NP; ++j) p[j] += S.bias[2 * FH + d * NP + j];
+      const int col = S.idx[16 + d];
+      float lp;
+      const float x = pq_inverse_one<K>(p, valid ? zr[col] : 0.5f, lp);
+      if (valid) zr[col] = x;
+      ld += lp;
+    }
+    if (valid) logq[e] += ld;
+    tc_fence_before();
+    __syncthreads();
+  }
+  // a timed-out wait: let the MMA in flight finish (bounded) before the
+  // tensor memory is freed
+  if (*(volatile int*)S.bad) {
+    if (tid == 0) atomicExch(err, 1);
+    bool done = false;
+    for (uint32_t spin = 0; spin < 1000u && !done; ++spin) done = tc_mbar_try_wait(S.mbar, phase, 1000000u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tc_tmem_dealloc(tm, FTMEM);
+  }
+#else
+  if (threadIdx.x == 0 && blockIdx.x == 0 && err) atomicExch(err, 2);
+#endif
+}
+
+template <int K>
+int launch_flow_tc(float* z, int64_t n, int dim, const int* ia, int na, const int* ib, int nb, const float* W1,
+                   const float* b1, const float* W2, const float* b2, const float* W3, const float* b3, float* logq,
+                   int* err, cudaStream_t st) {
+  const int n3 = nb * (2 * K + 1), n3p = (n3 + 15) / 16 * 16;
+  const size_t smem = flow_tc_smem_bytes(n3p);
+  auto fn = flow_inv_layer_tc_kernel<K>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return MF_ERR_CUDA;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t tiles = (n + FTILE - 1) / FTILE, grid = (int64_t)(sms > 0 ? sms : 152) * 2;
+  if (grid > tiles) grid = tiles;
+  fn<<<(int)grid, FTILE, smem, st>>>(z, n, dim, ia, na, ib, nb, W1, b1, W2, b2, W3, b3, n3p, logq, err);
+  return cudaPeekAtLastError() == cudaSuccess ? MF_OK : MF_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" int mf_flow_inv_layer_tc(float* z, int64_t n, int dim, const int* ia, int na, const int* ib, int nb, int K,
+                                    const float* W1, const float* b1, const float* W2, const float* b2,
+                                    const float* W3, const float* b3, float* logq, int* err, void* stream) {
+  if (n < 0 || dim <= 0 || na < 1 || na > 16 || nb < 1 || nb > 16 || na + nb > dim) return MF_ERR_ARG;
+  if (!(K == 4 || K == 8 || K == 16) || ((nb * (2 * K + 1) + 15) / 16) * 16 > FMAXN3) return MF_ERR_ARG;
+  if (n == 0) return MF_OK;
+  if (!z || !ia || !ib || !W1 || !b1 || !W2 || !b2 || !W3 || !b3 || !logq || !err) return MF_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (K) {
+    case 4: return launch_flow_tc<4>(z, n, dim, ia, na, ib, nb, W1, b1, W2, b2, W3, b3, logq, err, st);
+    case 8: return launch_flow_tc<8>(z, n, dim, ia, na, ib, nb, W1, b1, W2, b2, W3, b3, logq, err, st);
+    default: return launch_flow_tc<16>(z, n, dim, ia, na, ib, nb, W1, b1, W2, b2, W3, b3, logq, err, st);
+  }
+}

@@ -83,11 +83,15 @@ def _masks(dim, n_layers, seed):
 
 
 class NormalizingFlow(torch.nn.Module):
-    def __init__(self, dim, n_layers=6, bins=16, hidden=64, n_hidden=2, seed=0, bf16=True, tf32=False):
+    def __init__(self, dim, n_layers=6, bins=16, hidden=64, n_hidden=2, seed=0, bf16=True, tf32=False, fused=None):
         """bf16: conditioner GEMMs in BF16 (autocast); else FP32, with TF32
         tensor-core GEMMs when tf32 is set.  Reduced-precision GEMMs leave
         the estimates unbiased (the sampled log-density is the exact density
-        of the map as evaluated); they perturb the training gradients."""
+        of the map as evaluated); they perturb the training gradients.
+        fused: sample with one tensor-core kernel per coupling layer
+        (mf_flow_inv_layer_tc: the MLP in TF32 and the inverse transform);
+        by default whenever tf32 is set and the shapes fit it (64 hidden
+        units, two hidden layers, 4, 8 or 16 bins)."""
         super().__init__()
         self.dim, self.K, self.bf16, self.tf32 = dim, bins, bf16, tf32
         self.masks = _masks(dim, n_layers, seed)
@@ -106,6 +110,14 @@ class NormalizingFlow(torch.nn.Module):
         self.to(device())
         self._idx = [(torch.nonzero(m).flatten().to(device()), torch.nonzero(~m).flatten().to(device()))
                      for m in self.masks]
+        self._idx32 = [(ib.int().contiguous(), ia.int().contiguous()) for ib, ia in self._idx]
+        fits = (hidden == 64 and n_hidden == 2 and bins in (4, 8, 16)
+                and all(0 < len(ia) <= 16 and 0 < len(ib) <= 16 and len(ib) * (2 * bins + 1) <= 256
+                        for ib, ia in self._idx))
+        if fused and not fits:
+            raise ValueError("the fused sampling kernel needs 64 hidden units, 2 hidden layers, 4/8/16 bins, "
+                             "at most 16 dimensions per half")
+        self.fused = bool(fits and (tf32 and not bf16) if fused is None else fused)
 
     def _params(self, l, x_a):
         if self.bf16:
@@ -130,6 +142,17 @@ class NormalizingFlow(torch.nn.Module):
                   stream_ptr())
         z = u.T.float().contiguous()
         logq = torch.zeros(n, dtype=torch.float32, device=device())
+        if self.fused:
+            err = torch.zeros(1, dtype=torch.int32, device=device())
+            for l, net in enumerate(self.nets):
+                ib, ia = self._idx32[l]
+                w = [t.detach().float().contiguous() for t in (net[0].weight, net[0].bias, net[2].weight,
+                                                               net[2].bias, net[4].weight, net[4].bias)]
+                _lib.call("mf_flow_inv_layer_tc", z.data_ptr(), n, self.dim, ia.data_ptr(), len(ia), ib.data_ptr(),
+                          len(ib), self.K, *[t.data_ptr() for t in w], logq.data_ptr(), err.data_ptr(), stream_ptr())
+            if int(err.item()) != 0:
+                raise RuntimeError(f"mf_flow_inv_layer_tc: device error flag {int(err.item())}")
+            return z.double(), logq.double()
         for l in range(len(self.masks)):
             ib, ia = self._idx[l]
             params = self._params(l, z[:, ia])
