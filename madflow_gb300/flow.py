@@ -189,14 +189,56 @@ def _backward(flow, loss):
         torch.backends.cuda.matmul.allow_tf32 = prev
 
 
-def _train_step(flow, opt, x, w, minibatch, resample=0):
+class _GraphedStep:
+    """One Adam step on the mean log-density of a fixed number of points,
+    captured once as a CUDA graph (the log-density, its backward pass with
+    the custom coupling kernels and the optimizer step: some hundred small
+    launches, replayed as one).  The optimizer must be capturable.  The
+    warm-up steps the capture needs run on a placeholder batch; the weights
+    and the optimizer state are put back afterwards."""
+
+    def __init__(self, flow, opt, n):
+        self.flow, self.opt = flow, opt
+        self.x = torch.full((n, flow.dim), 0.5, dtype=torch.float32, device=device())
+        params = list(flow.parameters())
+        saved = [p.detach().clone() for p in params]
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                self._step()
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._step()
+        with torch.no_grad():
+            for p, v in zip(params, saved):
+                p.copy_(v)
+        for st in opt.state.values():
+            for v in st.values():
+                if torch.is_tensor(v):
+                    v.zero_()
+
+    def _step(self):
+        self.opt.zero_grad(set_to_none=False)
+        loss = -self.flow.log_prob(self.x).mean()
+        _backward(self.flow, loss)
+        self.opt.step()
+
+    def __call__(self, xs):
+        self.x.copy_(xs)
+        self.graph.replay()
+
+
+def _train_step(flow, opt, x, w, minibatch, resample=0, step=None):
     """Variance-loss updates on one batch (x, w = f/q) drawn from the flow.
 
     The gradient of Var(f/q) is -E_q[w^2 d log q] (score function).  With
     resample > 0 it is estimated from `resample` events drawn with
     probability w^2 / sum w^2 (systematic resampling), as
     -(sum w^2) mean(d log q) over them: unbiased, and only the resampled
-    events go through the flow's log-density and its backward pass."""
+    events go through the flow's log-density and its backward pass.
+    step (optional): a _GraphedStep for `resample` points (one minibatch)."""
     if resample > 0:
         w2 = (w * w).double()
         total = float(w2.sum())
@@ -207,6 +249,9 @@ def _train_step(flow, opt, x, w, minibatch, resample=0):
                                                                                       dtype=torch.float64)) / resample
         idx = torch.clamp(torch.searchsorted(cdf, u), max=w.numel() - 1)
         xs = x[idx]
+        if step is not None:
+            step(xs)
+            return
         for s in range(0, resample, minibatch):
             loss = -flow.log_prob(xs[s: s + minibatch]).mean()
             opt.zero_grad(set_to_none=True)
@@ -257,7 +302,7 @@ def _vegas_map(grid, z):
 
 def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size=1_000_000, max_batches=200,
                               train_batches=30, minibatch=100_000, lr=2e-3, seed=99, grid=None, prior=None,
-                              resample=0):
+                              resample=0, graph=True):
     """Integrate while training: every batch is drawn from the current (frozen)
     flow, so mean(f/q) over it is an unbiased estimate with variance
     var(f/q)/n; the estimates of all batches are combined with
@@ -270,10 +315,14 @@ def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size
     f(G(z)) |dG/dz| / q(z).  prior (optional): (wsum, wres) of earlier
     unbiased estimates (e.g. the VEGAS iterations that adapted the grid), in
     the same inverse-variance form.  resample > 0: train on that many events
-    resampled with probability w^2 (see _train_step).
+    resampled with probability w^2 (see _train_step).  graph: with
+    resample > 0 and resample <= minibatch, the training step runs as a
+    captured CUDA graph (_GraphedStep).
 
     Returns (result, error, info)."""
-    opt = torch.optim.Adam(flow.parameters(), lr=lr)
+    graphed = bool(graph and 0 < resample <= minibatch and train_batches > 0)
+    opt = torch.optim.Adam(flow.parameters(), lr=lr, capturable=graphed)
+    step = _GraphedStep(flow, opt, int(resample)) if graphed else None
     wsum, wres = prior if prior is not None else (0.0, 0.0)
     rel_std = float("nan")
     b = 0
@@ -295,7 +344,7 @@ def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size
             if cur != 0 and (1.0 / math.sqrt(wsum)) / abs(cur) <= target_rel_error:
                 break
         if b < train_batches:
-            _train_step(flow, opt, z, w, minibatch, resample)
+            _train_step(flow, opt, z, w, minibatch, resample, step)
     info = {"batches": b + 1, "trained": min(b + 1, int(train_batches)), "last_rel_std": rel_std}
     if wsum == 0:
         return 0.0, 0.0, info

@@ -196,3 +196,32 @@ def test_fused_tensor_core_sampling(cuda, dim, bins):
     with torch.no_grad():
         lp = g.log_prob(zf.float())
     assert float((lp.double() - lf).abs().max()) < 2e-2
+
+
+def test_graphed_training_step_matches_eager(cuda):
+    """The training step captured as a CUDA graph (log-density, backward,
+    Adam) moves the weights as the eager step does, and leaves them untouched
+    when it is built (the capture's warm-up steps are undone)."""
+    import torch
+
+    from madflow_gb300.flow import NormalizingFlow, _GraphedStep, _train_step
+
+    a = NormalizingFlow(6, n_layers=4, bins=8, hidden=32, seed=5, bf16=False, tf32=False)
+    b = NormalizingFlow(6, n_layers=4, bins=8, hidden=32, seed=5, bf16=False, tf32=False)
+    b.load_state_dict(a.state_dict())
+    oa = torch.optim.Adam(a.parameters(), lr=1e-2)
+    ob = torch.optim.Adam(b.parameters(), lr=1e-2, capturable=True)
+    step = _GraphedStep(b, ob, 4096)
+    for pa, pb in zip(a.parameters(), b.parameters()):
+        assert torch.equal(pa, pb)
+    g = torch.Generator(device="cuda").manual_seed(1)
+    for it in range(4):
+        x = torch.rand((20_000, 6), device="cuda", dtype=torch.float64, generator=g)
+        w = torch.exp(-((x - 0.3) ** 2).sum(-1) * 8.0)
+        torch.manual_seed(10 + it)
+        _train_step(a, oa, x, w, 8192, resample=4096)
+        torch.manual_seed(10 + it)
+        _train_step(b, ob, x, w, 8192, resample=4096, step=step)
+    for pa, pb in zip(a.parameters(), b.parameters()):
+        assert float((pa - pb).abs().max()) < 1e-5
+    assert any(float(p.abs().max()) > 0 for p in list(b.parameters())[-2:])
