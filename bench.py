@@ -399,9 +399,10 @@ def time_to_target(args, target=1e-3):
                          "result_pb": res, "error_pb": err, "rel_error": err / abs(res) if res else None,
                          "reached": bool(res and err / abs(res) <= target),
                          "flow": f"{args.flow_layers} piecewise-quadratic coupling layers, {args.flow_bins} bins, "
-                                 f"MLP 2x{args.flow_hidden} ({'bf16' if args.flow_bf16 else 'TF32'} cuBLAS), "
+                                 f"MLP 2x{args.flow_hidden} ({'bf16 cuBLAS' if args.flow_bf16 else 'TF32: sampling in one tcgen05 kernel per layer, training through cuBLAS'}), "
                                  f"lr {args.flow_lr}, on a frozen VEGAS grid, "
-                                 f"trained on {args.flow_resample} events per batch resampled with probability w^2",
+                                 f"trained on {args.flow_resample} events per batch resampled with probability w^2 "
+                                 "(one Adam step, a captured CUDA graph)",
                          "last_std_over_mean": info["last_rel_std"]}
     return out
 
