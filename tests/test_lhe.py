@@ -52,7 +52,7 @@ def test_truncated_wmax():
     t = lhe.truncated_wmax(w, 0.01)
     a = w.abs()
     assert float(torch.clamp(a - t, min=0).sum()) <= 0.01 * float(a.sum()) * (1 + 1e-12)
-    # the next smaller distinct weight would exceed the budget
+    # the next smaller distinct weight would truncate more than the allowed fraction
     s = torch.sort(a, descending=True).values
     nxt = s[s < t].max()
     assert float(torch.clamp(a - nxt, min=0).sum()) > 0.01 * float(a.sum())
