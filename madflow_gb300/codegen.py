@@ -345,6 +345,13 @@ def emit_program(k):
     Stage L (1 <= L <= k-1) holds the gluon currents of length L+1, the top
     currents of length L, the t~ rows of length L and, at L = k-1, the bare
     full-length contractions T0; every item depends on earlier stages only.
+
+    From four gluons on, the t~ rows of length k-1 are not built: the
+    amplitude terms they enter, R(b) . O(a) with |a| = 1, are evaluated as
+    J(b) . MP(a), MP(a)^mu = wtb^T S(e_mu) O(a) the bilinears of the 4k
+    one-gluon top currents (stage 2, part type 4), which are far fewer than
+    the rows.  Their storage is kept (the tensor-core colour operands use
+    it).
     """
     seqs = [s for L in range(1, k) for s in itertools.permutations(range(k), L)]
     jo, off = {}, 0
@@ -389,7 +396,8 @@ def emit_program(k):
     def align_prog():
         prog.extend([0] * (-len(prog) % 4))
 
-    TYPE_J, TYPE_T0, TYPE_O, TYPE_R = 0, 1, 2, 3
+    TYPE_J, TYPE_T0, TYPE_O, TYPE_R, TYPE_MP = 0, 1, 2, 3, 4
+    use_mp = k >= 4
     for stage in range(1, k):
         plist = []
         # gluon currents of length stage+1 (canonical representatives only)
@@ -419,12 +427,22 @@ def emit_program(k):
         plist.append((TYPE_O, L, len(recs), len(prog), len(recs[0])))
         for r in recs:
             prog += r
-        # t~ rows of every sequence of length `stage`
-        recs = [[ro[b], jo[b]] for b in itertools.permutations(range(k), L)]
-        align_prog()
-        plist.append((TYPE_R, L, len(recs), len(prog), 2))
-        for r in recs:
-            prog += r
+        # t~ rows of every sequence of length `stage` (not the longest ones
+        # when the one-gluon bilinears replace them)
+        if not (use_mp and L == k - 1):
+            recs = [[ro[b], jo[b]] for b in itertools.permutations(range(k), L)]
+            align_prog()
+            plist.append((TYPE_R, L, len(recs), len(prog), 2))
+            for r in recs:
+                prog += r
+        # bilinears wtb^T S(e_mu) O(g) of the one-gluon top currents (node:
+        # the gluon; item: its 4 (top spin, helicity) entries)
+        if use_mp and stage == 2:
+            recs = [[oo[(g,)], 0, 0, 0] for g in range(k)]
+            align_prog()
+            plist.append((TYPE_MP, 1, len(recs), len(prog), 4))
+            for r in recs:
+                prog += r
         if stage == k - 1:
             recs = []
             for s in perms:
@@ -440,11 +458,13 @@ def emit_program(k):
             for r in recs:
                 prog += r
         parts.append(plist)
-    # amplitude records: per ordering, for the splits i = 1..k-1: (O offset, R offset)
+    # amplitude records: per ordering, for the splits i = 1..k-1: (O offset,
+    # R offset); with the one-gluon bilinears, (O offset, J offset of the
+    # suffix) for i = 1
     arec = []
     for s in perms:
         for i in range(1, k):
-            arec += [oo[s[:i]], ro[s[i:]]]
+            arec += [oo[s[:i]], jo[s[i:]] if (use_mp and i == 1) else ro[s[i:]]]
     hpack = []
     hunpack = []
     for s in perms:
@@ -476,6 +496,7 @@ def emit_program(k):
     w(f"namespace rec{k} {{")
     w(f"constexpr int J_TOTAL = {J_TOTAL}, O_TOTAL = {O_TOTAL}, R_TOTAL = {R_TOTAL};")
     w(f"constexpr int NSTAGE = {k - 1}, NPART = {len(pdesc) // 5};")
+    w(f"constexpr bool USE_MP = {'true' if use_mp else 'false'};  // one-gluon top-current bilinears")
     body = ", ".join(str(int(v)) for v in prog)
     w(f"__device__ __align__(16) const int prog[{len(prog)}] = {{{body}}};")
     w(f"alignas(16) static const int prog_h[{len(prog)}] = {{{body}}};")

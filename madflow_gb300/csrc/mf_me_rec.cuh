@@ -38,6 +38,7 @@ template <int K> struct RecTraits;
   template <> struct RecTraits<KK> {                                                                      \
     static constexpr int K = KK, J_TOTAL = rec##KK::J_TOTAL, O_TOTAL = rec##KK::O_TOTAL;                  \
     static constexpr int R_TOTAL = rec##KK::R_TOTAL, NSTAGE = rec##KK::NSTAGE;                            \
+    static constexpr bool USE_MP = rec##KK::USE_MP;                                                       \
     static constexpr int NPERM = ttng##KK::NPERM, NCOMB = ttng##KK::NCOMB;                                \
     static constexpr double DENOMINATOR = ttng##KK::DENOMINATOR, COLOUR_DEN = ttng##KK::COLOUR_DEN;       \
     MF_D static int prog(int i) { return MF_TBL(rec##KK, prog, i); }                                      \
@@ -85,6 +86,7 @@ template <class T, int K> struct RecWS {
   W4Planes<T, R::J_TOTAL> J;
   W4Planes<T, R::O_TOTAL> O;
   W4Planes<T, R::R_TOTAL> RW;
+  W4Planes<T, (R::USE_MP ? 8 * K : 0)> MP;  // wtb[tb]^T S(e_mu) O(g): [2 o + tb], o a one-gluon top current
   W4<T> WT[2], WTB[2];
   cx<T> A[R::NPERM * (1 << (K + 2))];  // [ordering][helicity combination]
 };
@@ -131,11 +133,7 @@ MF_D void prep_event(PrepRec<T, K>& r, const double (*p)[4], double mt, double w
   // M[q][mu] = WTB[q>>1]^T S(e_mu) WT[q&1]: an amplitude in which the full
   // gluon current J meets the top line directly is J . M (S is linear in J)
   for (int q = 0; q < 4; ++q)
-    for (int mu = 0; mu < 4; ++mu) {
-      W4<T> e = w4zero<T>();
-      e.v[mu] = cx<T>{T(1), T(0)};
-      r.ev.M[q][mu] = dot4(sandwich_row(r.WTB[q >> 1], e), r.WT[q & 1]);
-    }
+    for (int mu = 0; mu < 4; ++mu) r.ev.M[q][mu] = dot4(unit_row(r.WTB[q >> 1], mu), r.WT[q & 1]);
   r.scale = (c11.re * c11.re + c11.im * c11.im) / (R::COLOUR_DEN * R::DENOMINATOR);
 }
 
@@ -246,10 +244,20 @@ MF_D void rec_item(RecWS<T, K>& ws, const EvData<T, K>& ev, int type, int L, int
     }
     const int m = f[1];
     ws.O.put(f[0] + sub, topprop<T>(ev.Qt[m], ev.mt, ev.tden[m], y));
-  } else {  // t~ row: out, J
+  } else if (type == 3) {  // t~ row: out, J
     const int htb = sub >> L, hp = sub & ((1 << L) - 1);
     const int2 g = R::prog2(r);
     ws.RW.put(g.x + sub, sandwich_row(ws.WTB[htb], ws.J.get(g.y + hp)));
+  } else {  // bilinears of the one-gluon top current o: wtb[tb]^T S(e_mu) O(o)
+    const int o = R::prog4(r).x + sub;
+    const W4<T> Oo = ws.O.get(o);
+#pragma unroll
+    for (int tb = 0; tb < 2; ++tb) {
+      W4<T> m;
+#pragma unroll
+      for (int mu = 0; mu < 4; ++mu) m.v[mu] = dot4(unit_row(ws.WTB[tb], mu), Oo);
+      ws.MP.put(2 * o + tb, m);
+    }
   }
 }
 
@@ -333,7 +341,7 @@ MF_D void rec_stage_parts(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid, int 
   if constexpr (P < PEND) {
     using R = RecTraits<K>;
     constexpr int type = R::pdesc_c(5 * P), L = R::pdesc_c(5 * P + 1);
-    constexpr bool pair = PAIR && type >= 2;
+    constexpr bool pair = PAIR && (type == 2 || type == 3);
     constexpr int lper = ((type <= 1) ? L : L + 1) - (pair ? 1 : 0);
     constexpr int cnt = R::pdesc_c(5 * P + 2) << lper;
     constexpr int rec0 = R::pdesc_c(5 * P + 3), rsz = R::pdesc_c(5 * P + 4);
@@ -385,12 +393,23 @@ template <class T, int K> MF_D void rec_st_A(RecWS<T, K>& ws, int tid, int nt) {
       const int2 orr = R::arec2(s * 2 * (K - 1) + 2 * (i - 1));  // top current, t~ row
       const int oo = orr.x, ro = orr.y;
       const int lo = hfull & ((1 << i) - 1), hi = hfull >> i;
-      W4<T> O0 = ws.O.get(oo + lo), O1 = ws.O.get(oo + (1 << i) + lo);
-      W4<T> R0 = ws.RW.get(ro + hi), R1 = ws.RW.get(ro + (1 << (K - i)) + hi);
-      a[0] += dot4(R0, O0);
-      a[1] += dot4(R0, O1);
-      a[2] += dot4(R1, O0);
-      a[3] += dot4(R1, O1);
+      if (R::USE_MP && i == 1) {
+        // R(b) . O(a) = J(b) . MP(a) for the one-gluon prefix a (ro: the
+        // J offset of the suffix b)
+        const W4<T> Js = ws.J.get(ro + hi);
+        const int o0 = oo + lo, o1 = oo + 2 + lo;
+        a[0] += dot4(Js, ws.MP.get(2 * o0));
+        a[1] += dot4(Js, ws.MP.get(2 * o1));
+        a[2] += dot4(Js, ws.MP.get(2 * o0 + 1));
+        a[3] += dot4(Js, ws.MP.get(2 * o1 + 1));
+      } else {
+        W4<T> O0 = ws.O.get(oo + lo), O1 = ws.O.get(oo + (1 << i) + lo);
+        W4<T> R0 = ws.RW.get(ro + hi), R1 = ws.RW.get(ro + (1 << (K - i)) + hi);
+        a[0] += dot4(R0, O0);
+        a[1] += dot4(R0, O1);
+        a[2] += dot4(R1, O0);
+        a[3] += dot4(R1, O1);
+      }
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) ws.A[s * NC + (hg | ((q & 1) << K) | ((q >> 1) << (K + 1)))] = a[q];

@@ -101,6 +101,21 @@ template <class T> MF_D W4<T> sandwich_row(const W4<T>& F1, const W4<T>& V) {
 template <class T> MF_D cx<T> dot4(const W4<T>& a, const W4<T>& b) {
   return a.v[0] * b.v[0] + a.v[1] * b.v[1] + a.v[2] * b.v[2] + a.v[3] * b.v[3];
 }
+// sandwich_row(F1, e_mu) for the unit vector e_mu (the row of the bilinear
+// F1^T S(e_mu) F2 = row . F2): components of F1 permuted, negated or times i
+template <class T> MF_D W4<T> unit_row(const W4<T>& F1, int mu) {
+  W4<T> r;
+  if (mu == 0) {
+    r.v[0] = F1.v[2]; r.v[1] = F1.v[3]; r.v[2] = F1.v[0]; r.v[3] = F1.v[1];
+  } else if (mu == 1) {
+    r.v[0] = -F1.v[3]; r.v[1] = -F1.v[2]; r.v[2] = F1.v[1]; r.v[3] = F1.v[0];
+  } else if (mu == 2) {
+    r.v[0] = mul_i(F1.v[3]); r.v[1] = mul_mi(F1.v[2]); r.v[2] = mul_mi(F1.v[1]); r.v[3] = mul_i(F1.v[0]);
+  } else {
+    r.v[0] = -F1.v[2]; r.v[1] = F1.v[3]; r.v[2] = F1.v[0]; r.v[3] = -F1.v[1];
+  }
+  return r;
+}
 
 // Per-event data shared by all helicities of one event: slot momenta of every
 // subset of gluons (Qg) and of the top line (Qt = p_t + Qg), and the
