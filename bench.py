@@ -42,9 +42,9 @@ REC_BYTES = {4: 1536}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max clock
 # DRAM bytes (read + write) of the matrix-element kernel per passing event:
 # one ncu capture of 10^6 points (profiles/me_rec_kernel_ggttxgg_mixed.md,
-# 1.2147 GB over 760,841 events); the kernel's traffic is its records, so it
+# 1.2143 GB over 760,841 events); the kernel's traffic is its records, so it
 # scales with the events of a launch
-ME_DRAM_BYTES_PER_EVENT = 1596.5
+ME_DRAM_BYTES_PER_EVENT = 1596.0
 
 
 def workload(events):
