@@ -25,6 +25,26 @@ def test_status_strings_and_argument_errors():
     assert lib.mf_process_create(4, 1, None) == _lib.MF_ERR_ARG
 
 
+def test_flow_layer_argument_checks():
+    """mf_flow_inv_layer_tc rejects the shapes its kernel does not cover
+    before touching the device; an empty batch is a no-op."""
+    lib = _lib.load()
+    f = lib.mf_flow_inv_layer_tc
+    f.restype = ctypes.c_int
+    null = [None] * 8
+
+    def call(n, dim, na, nb, K):
+        return f(None, ctypes.c_int64(n), dim, None, na, None, nb, K, *null, None)
+
+    assert call(0, 18, 9, 9, 8) == 0
+    assert call(10, 18, 9, 9, 5) == _lib.MF_ERR_ARG      # K not in {4, 8, 16}
+    assert call(10, 18, 0, 9, 8) == _lib.MF_ERR_ARG      # no conditioning inputs
+    assert call(10, 40, 20, 20, 8) == _lib.MF_ERR_ARG    # more than 16 per half
+    assert call(10, 10, 9, 9, 8) == _lib.MF_ERR_ARG      # na + nb > dim
+    assert call(10, 32, 16, 16, 8) == _lib.MF_ERR_ARG    # nb (2K+1) = 272 > 256
+    assert call(10, 18, 9, 9, 8) == _lib.MF_ERR_ARG      # null buffers
+
+
 def test_process_info_without_gpu():
     lib = _lib.load()
     h = ctypes.c_void_p()
