@@ -276,6 +276,8 @@ def run_gpu(args):
         out["time_to_1e-3"] = time_to_target(args)
     if args.cpu_baseline and rank == 0:
         out["cpu_baseline"] = cpu_baseline(args)
+    if args.numpy_baseline and rank == 0:
+        out["cpu_baseline_numpy"] = cpu_baseline_numpy(args)
         ttt = out.get("time_to_1e-3")
         if ttt and ttt.get("vegas_fp64", {}).get("events"):
             ev = ttt["vegas_fp64"]["events"] * ttt["vegas_fp64"]["pass_fraction"]
@@ -431,6 +433,34 @@ def cpu_baseline(args, sample=None):
             "seconds": dt, "events": n_me}
 
 
+def cpu_baseline_numpy(args):
+    """The vectorised NumPy FP64 restatement (oracle/np_ref.py: [6, N]
+    complex arrays over the event axis, every helicity separately, madflow's
+    CPU array style) timed on |M|^2 of a bounded sample of the workload's
+    momenta (ramboflow of uniform points, the events that pass the cuts)."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import np_ref
+    import oracle
+
+    oracle.build()
+    rng = np.random.default_rng(args.seed)
+    x = rng.uniform(size=(4 * args.numpy_events, 18))
+    p, *_, x1, x2 = oracle.ramboflow(x, 6, SQRTS, [MT, MT, 0.0, 0.0])
+    lab = oracle.boost_to_lab(p, x1, x2)
+    keep = [e for e in range(len(lab)) if oracle.pass_cuts(lab[e], CUTS["ptmin"], CUTS["etamax"], CUTS["drmin"])]
+    p = p[keep[: args.numpy_events]]
+    plan = np_ref.TTNG(4, oracle.TTNG(4).colour)
+    gs = float(np.sqrt(4 * np.pi * ALPHA_S))
+    plan.smatrix(p[:64], MT, WT, -gs, 1j * gs, 1j * gs * gs)  # warm-up
+    t0 = time.perf_counter()
+    plan.smatrix(p, MT, WT, -gs, 1j * gs, 1j * gs * gs)
+    dt = time.perf_counter() - t0
+    return {"value": len(p) / dt, "unit": "|M|^2 evals/s", "cores": 1, "kind": "port",
+            "sample": f"{len(p)} passing events of the workload, |M|^2 only, {dt:.1f} s", "seconds": dt}
+
+
 def run_reference(args):
     """The reference arm: madflow's CPU path (its FP64 algorithm restated in
     C++/OpenMP, all host cores), W warm-up and K timed steps, each step a
@@ -481,6 +511,9 @@ def main():
     ap.add_argument("--cpu-events", type=int, default=200_000)
     ap.add_argument("--ref-events", type=int, default=40_000)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--numpy-baseline", action="store_true",
+                    help="also time the vectorised NumPy restatement (one core; slow, off by default)")
+    ap.add_argument("--numpy-events", type=int, default=3000)
     ap.add_argument("--no-time-to-target", dest="time_to_target", action="store_false")
     ap.add_argument("--target-events", type=int, default=4_000_000)
     ap.add_argument("--max-iter", type=int, default=40)
