@@ -326,7 +326,7 @@ def _bitrev(h, n):
     return r
 
 
-def emit_program(k):
+def program_data(k):
     """The helicity-recycling evaluation of mf_me_rec.cuh as a flat program.
 
     Storage (shared memory of one event):
@@ -491,6 +491,17 @@ def emit_program(k):
         h[2] = 1 if ht else -1
         h[3] = 1 if htb else -1
         cfg_to_mg.append(hidx[tuple(h)])
+    return dict(k=k, J_TOTAL=J_TOTAL, O_TOTAL=O_TOTAL, R_TOTAL=R_TOTAL, use_mp=use_mp, prog=prog, pdesc=pdesc,
+                stage_first=stage_first, arec=arec, hpack=hpack, hunpack=hunpack,
+                jo_ext=[jo[(q,)] for q in range(k)], cfg_to_mg=cfg_to_mg)
+
+
+def emit_program(k):
+    """The program of program_data(k) as a C++ namespace rec<k>."""
+    d = program_data(k)
+    J_TOTAL, O_TOTAL, R_TOTAL, use_mp = d["J_TOTAL"], d["O_TOTAL"], d["R_TOTAL"], d["use_mp"]
+    prog, pdesc, stage_first, arec = d["prog"], d["pdesc"], d["stage_first"], d["arec"]
+    hpack, hunpack, cfg_to_mg = d["hpack"], d["hunpack"], d["cfg_to_mg"]
     L = []
     w = L.append
     w(f"namespace rec{k} {{")
@@ -510,7 +521,7 @@ def emit_program(k):
     w(f"alignas(8) static const int arec_h[{len(arec)}] = {{{body}}};")
     w(_arr("hpack", "unsigned char", hpack))
     w(_arr("hunpack", "unsigned char", hunpack))
-    w(_arr("jo_ext", "int", [jo[(q,)] for q in range(k)]))
+    w(_arr("jo_ext", "int", d["jo_ext"]))
     w(_arr("cfg_to_mg", "int", cfg_to_mg))
     w("}  // namespace")
     return "\n".join(L)
