@@ -103,3 +103,22 @@ def test_colour_tc_operand_layout():
             seen.add(off)
             assert flat[off] == (num[c][r] if r < n else 0.0)
     assert len(seen) == len(flat)
+
+
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
+def test_compile_time_driver_bitwise_equal(host_lib, oracle, k):
+    """The kernels' compile-time stage driver (paired top-line items from four
+    gluons on) does per item the arithmetic of the run-time stage loop, so
+    both give bitwise the same |M|^2, in FP64 and in FP32."""
+    x = np.random.default_rng(90 + k).uniform(size=(8, 4 * k + 2))
+    p, *_ = oracle.ramboflow(x, k + 2, 13000.0, [MT, MT] + [0.0] * (k - 2))
+    coup = np.array([GC10.real, 0.0, 0.0, GC11.imag, 0.0, GC12.imag])
+    pc = np.ascontiguousarray(p)
+    for prec in (0, 1):
+        outs = []
+        for fn in (host_lib.me_host_smatrix, host_lib.me_host_smatrix_compiled):
+            out = np.zeros(len(p))
+            fn(k, prec, _dp(pc), ctypes.c_int64(len(p)), _dp(coup), ctypes.c_double(MT), ctypes.c_double(WT),
+               out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+            outs.append(out)
+        assert np.array_equal(outs[0], outs[1]), (k, prec)
