@@ -4,7 +4,7 @@ import math
 
 import torch
 
-from .config import DTYPE, DTYPECOMPLEX, device
+from .config import DTYPE, DTYPECOMPLEX
 
 
 def _alphas_to_gs(alpha_s):

@@ -47,7 +47,7 @@ def one_matrix_integration(matrix, model_params, sqrts=7e3, n_events=int(1e5), n
 
 def synthetic_pdf(x, q2):
     """The synthetic gluon PDF x g(x) = A x^-0.2 (1-x)^5 (GPU table lookup)."""
-    from .config import DTYPE, device, stream_ptr, to_device
+    from .config import stream_ptr, to_device
 
     xv = to_device(x).reshape(-1)
     out = torch.empty_like(xv)

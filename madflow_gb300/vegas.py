@@ -20,7 +20,6 @@ import ctypes
 import math
 import time
 
-import numpy as np
 import torch
 
 from . import _lib

@@ -5,7 +5,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from conftest import GC10, GC11, GC12, MT, ROOT, WT
+from conftest import GC10, GC11, GC12, MT, WT
 from madflow_gb300 import codegen
 
 

@@ -4,7 +4,6 @@ Called through the C ABI and compared with mf_vegas_accumulate on the same
 inputs, twice in a row (the second call reuses the array the first left
 behind).  This file runs last so that a failure here leaves every other test
 already run."""
-import ctypes
 
 import numpy as np
 import pytest
