@@ -184,6 +184,8 @@ def run_gpu(args):
             ends[i].synchronize()
             stage_ms.append(integ.stage_ms())
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
         wall = time.perf_counter() - t0
     integ.set_timing(False)
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
