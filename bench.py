@@ -36,7 +36,7 @@ ALG_FLOPS = {2: 23601.0, 3: 356161.0, 4: 5744961.0, 5: 102333185.0}
 # Flops per phase-space point the helicity-recycling FP32 kernel executes
 # (same counting convention), counted by running its stage functions with the
 # counting scalar (tests/test_flop_counts.py).
-REC_FLOPS = {2: 5225.0, 3: 51806.0, 4: 666795.0, 5: 12377952.0}
+REC_FLOPS = {2: 4504.0, 3: 51648.0, 4: 675248.0, 5: 12509560.0}
 # Bytes of the FP32 per-event record the matrix-element kernel reads (PrepRec)
 REC_BYTES = {4: 1536}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max clock

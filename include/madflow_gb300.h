@@ -11,7 +11,10 @@
  *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
  *     Calls are asynchronous with respect to the host unless stated.
  *   - Handles are not shared between host threads without external locking;
- *     distinct handles may be used concurrently.
+ *     distinct handles may be used concurrently.  A handle owns scratch
+ *     buffers that every call with it reuses (records, work counter, block
+ *     partials): calls with one handle must not overlap on the GPU, so issue
+ *     them on one stream or order the streams (events) between them.
  *
  * Particle order of g g > t t~ + (k-2) g is MadGraph's: 0, 1 incoming gluons,
  * 2 = t, 3 = t~, 4.. outgoing gluons.  Momenta are (E, px, py, pz), GeV.
@@ -212,16 +215,36 @@ int mf_process_tuning(const mf_process* proc, int* colour, int* waves, int* tune
 int mf_process_set_tuning(mf_process* proc, int colour, int waves);
 
 /* Device error flags the handle's kernels raised (no counterpart in the
- * reference): bit 0 = a bounded wait on the tensor cores ran out (the
- * affected events got NaN).  Synchronous device-to-host read; clear != 0
- * resets the flags. */
+ * reference): bit 0 = a bounded wait on the tensor cores ran out (the event
+ * being evaluated and every later event of the same thread block got NaN in
+ * out and hel_out; events that needed no work keep 0); bit 1 = non-finite
+ * weights were replaced by 0 in an accumulation (see mf_process_nonfinite).
+ * Synchronous device-to-host read; clear != 0 resets the flags. */
 int mf_process_error_flags(mf_process* proc, int* flags, int clear);
+/* Number of event weights jac * f of mf_vegas_iteration / mf_integrand /
+ * mf_vegas_events calls that were not finite (NaN or +-inf, e.g. from
+ * non-finite caller points) and entered the sums, the histogram and f_out as
+ * 0, since the last clear (no counterpart in the reference, which would
+ * carry the NaN into its integral).  Synchronous read; clear != 0 resets the
+ * count.  Returns MF_ERR_NONFINITE when *count > 0, else MF_OK. */
+int mf_process_nonfinite(mf_process* proc, int64_t* count, int clear);
+/* Tries (~1 ms each) of every bounded wait of the matrix-element kernels on
+ * the tensor cores before a thread block gives up (default 1000, about 1 s;
+ * 0 <= tries <= 100000).  With tries = 0 the first wait of every block gives
+ * up at once, which exercises the error path of bit 0 above without a GPU
+ * fault: the block still waits (bounded, at the default limit) for its
+ * tensor-core work to finish before it frees its tensor memory.  No
+ * counterpart in the reference. */
+int mf_process_set_wait_limit(mf_process* proc, int tries);
 int mf_process_stage_ms(const mf_process* proc, float* ms);
 
 /* VEGAS accumulation for an integrand evaluated by the caller: f [N], jac
  * [N], bins [ndim][N] (from mf_vegas_sample); results (device)
  * [2 + ndim*nbins] as in mf_vegas_iteration, with w = f*jac*inv_n.
- * Deterministic (fixed-order reductions). */
+ * ndim * nbins <= 8192.  A bin index outside [0, nbins) adds to no bin (it
+ * still counts in the sums of w and w^2).  Deterministic (fixed-order
+ * reductions).  The block partials live in a buffer per host thread and
+ * device, so calls of one thread on different streams must not overlap. */
 int mf_vegas_accumulate(const double* f, const double* jac, const int32_t* bins, int64_t n_events, int ndim,
                         int nbins, double inv_n, double* results, void* stream);
 
@@ -245,7 +268,8 @@ int mf_vegas_accumulate_noalloc(const double* f, const double* jac, const int32_
 int mf_vegas_refine(double* grid, const double* hist, int ndim, int nbins, double alpha, void* stream);
 
 /* Stand-alone VEGAS map: u [ndim][N] -> x [ndim][N], jac [N], bins
- * [ndim][N] int32 (bit-exact bin indices for identical uniforms). */
+ * [ndim][N] int32 (bit-exact bin indices for identical uniforms).  A uniform
+ * outside [0, 1) is mapped through the nearest edge bin. */
 int mf_vegas_sample(const double* grid, int ndim, int nbins, const double* u, int64_t n_events, double* x,
                     double* jac, int32_t* bins, void* stream);
 

@@ -36,6 +36,11 @@ class MadflowError(RuntimeError):
         self.status = status
 
 
+class DeviceError(RuntimeError):
+    """A kernel of a madflow_gb300 handle reported an error on the device
+    (a bounded wait on the tensor cores ran out; the affected events got NaN)."""
+
+
 class IntegrandConfig(ctypes.Structure):
     _fields_ = [
         ("kind", c_int),
@@ -85,6 +90,8 @@ _SIGS = {
     "mf_vegas_accumulate": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
     "mf_process_set_timing": (c_int, [c_void_p, c_int]),
     "mf_process_error_flags": (c_int, [c_void_p, ctypes.POINTER(c_int), c_int]),
+    "mf_process_nonfinite": (c_int, [c_void_p, ctypes.POINTER(c_int64), c_int]),
+    "mf_process_set_wait_limit": (c_int, [c_void_p, c_int]),
     "mf_process_tuning": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                                   ctypes.POINTER(ctypes.c_float)]),
     "mf_process_set_tuning": (c_int, [c_void_p, c_int, c_int]),

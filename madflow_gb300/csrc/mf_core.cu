@@ -31,6 +31,27 @@ int blocks_for(int64_t n, int threads = 256) {
   return (int)(b < 1 ? 1 : b);
 }
 
+// The accumulation kernels keep the histogram of every dimension in dynamic
+// shared memory: up to kAccumMaxBins bins in all plus 3 doubles per thread.
+// Their attribute is raised once per device to that largest size (a
+// process-wide setting, so it is never lowered by a later, smaller call).
+constexpr int kAccumMaxBins = 8192;
+constexpr int kAccumSmemMax = (kAccumMaxBins + 3 * 256) * (int)sizeof(double);
+std::mutex g_attr_mu;
+int smem_attr_once(const void* fn, bool* done_per_dev) {
+  int dev = 0;
+  int st = cuda_status(cudaGetDevice(&dev));
+  if (st) return st;
+  if (dev < 0 || dev >= 64) return MF_ERR_CAPACITY;
+  std::lock_guard<std::mutex> lk(g_attr_mu);
+  if (!done_per_dev[dev]) {
+    st = cuda_status(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kAccumSmemMax));
+    if (st) return st;
+    done_per_dev[dev] = true;
+  }
+  return MF_OK;
+}
+
 // ---- synthetic PDF table, one copy per device ------------------------------
 constexpr int kNX = 100, kNQ = 50;
 struct PdfHost {
@@ -123,7 +144,11 @@ __global__ void rambo_conv_kernel(const double* __restrict__ x, int64_t N, int n
     }
     double p[MF_MAX_OUT][4];
     rambo_massless(xr, n, roots, K.pi, p);
-    local = min(local, newton_conv_iter(n, M.m, p, roots, K.acc));
+    // a non-finite event takes no part in the batch minimum (its f0 > ACC
+    // test is false at once and would stop the iteration for every event)
+    double chk = roots;
+    for (int i = 0; i < n; ++i) chk += p[i][0];
+    if (isfinite(chk)) local = min(local, newton_conv_iter(n, M.m, p, roots, K.acc));
   }
   for (int o = 16; o > 0; o >>= 1) local = min(local, __shfl_xor_sync(0xffffffffu, local, o));
   if ((threadIdx.x & 31) == 0) atomicMin(kmin, local);
@@ -293,6 +318,8 @@ __global__ void vegas_sample_kernel(const double* __restrict__ div, int ndim, in
     for (int d = 0; d < ndim; ++d) {
       double xn = u[(int64_t)d * N + e] * (double)nb;
       int i = (int)xn;
+      // caller uniforms outside [0, 1) (or NaN) fall in the edge bins
+      if (!(xn >= 0.0)) i = 0;
       if (i > nb - 1) i = nb - 1;
       double frac = xn - (double)i;
       double lo = div[d * (nb + 1) + i];
@@ -397,7 +424,11 @@ __global__ void vegas_accum_kernel(const double* __restrict__ f, const double* _
     for (int d = threadIdx.x; d < ndim; d += blockDim.x) {
       const int32_t* bd = bins + (int64_t)d * N + c0;
       double* hd = hist + d * nb;
-      for (int j = 0; j < cn; ++j) hd[bd[j]] += w2[j];
+      // bins come from the caller: an index outside [0, nb) is not added
+      for (int j = 0; j < cn; ++j) {
+        const int32_t b = bd[j];
+        if ((uint32_t)b < (uint32_t)nb) hd[b] += w2[j];
+      }
     }
     __syncthreads();
   }
@@ -445,9 +476,11 @@ struct mf_process {
   double* d_me = nullptr;   // [cap]
   unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
   int64_t event_cap = 0;
-  int* d_err = nullptr;     // device error flags of the kernels (bit 0: a tensor-core wait ran out)
+  int* d_err = nullptr;     // device error flags of the kernels (bit 0: a tensor-core wait ran out,
+                            // bit 1: non-finite weights were zeroed)
+  unsigned long long* d_nonfinite = nullptr;  // count of the zeroed non-finite weights
   // matrix-element launch configuration and the autotuner's record
-  MeTune tune = {1, 8};
+  MeTune tune = {1, 8, MF_TC_WAIT_TRIES};
   bool tuned = false;
   float tune_ms[MF_TUNE_VARIANTS] = {};
   // optional stage timing of the fused iteration (events on the caller's stream)
@@ -517,6 +550,7 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_me) cudaFree(p->d_me);
   if (p->d_bins) cudaFree(p->d_bins);
   if (p->d_err) cudaFree(p->d_err);
+  if (p->d_nonfinite) cudaFree(p->d_nonfinite);
   for (cudaEvent_t e : p->tev)
     if (e) cudaEventDestroy(e);
   delete p;
@@ -624,17 +658,26 @@ static int fill_masses(const double* masses, int n, Masses& M, bool& massive) {
   return MF_OK;
 }
 
-// scratch int for the Newton rule: a small per-thread cache keyed by device
+// scratch int for the Newton rule: one per host thread and device, freed
+// when the thread exits
+struct NewtonScratch {
+  int* ptr[64] = {nullptr};
+  ~NewtonScratch() {
+    for (int* p : ptr)
+      if (p) cudaFree(p);
+  }
+};
 static int newton_scratch(int** out) {
-  static thread_local int* ptr[64] = {nullptr};
+  static thread_local NewtonScratch S;
   int dev = 0;
   int st = cuda_status(cudaGetDevice(&dev));
   if (st) return st;
-  if (!ptr[dev]) {
-    st = cuda_status(cudaMalloc(&ptr[dev], sizeof(int)));
+  if (dev < 0 || dev >= 64) return MF_ERR_CAPACITY;
+  if (!S.ptr[dev]) {
+    st = cuda_status(cudaMalloc(&S.ptr[dev], sizeof(int)));
     if (st) return st;
   }
-  *out = ptr[dev];
+  *out = S.ptr[dev];
   return MF_OK;
 }
 
@@ -817,7 +860,7 @@ static int autotune_me(mf_process* p, const int4* prep, int64_t N, const double*
         p->tune_ms[4 * c + w] = -1.0f;
         continue;
       }
-      MeTune t = {c, kTuneWaves[w]};
+      MeTune t = {c, kTuneWaves[w], p->tune.wait_tries};
       float ms = 0.0f;
       for (int rep = 0; rep < 2 && !st; ++rep) {  // the first launch of a variant is a warm-up
         st = cuda_status(cudaEventRecord(a, S(stream)));
@@ -848,6 +891,11 @@ static int ensure_events(mf_process* p, int64_t N) {
   if (!p->d_err) {
     int st = cuda_status(cudaMalloc(&p->d_err, sizeof(int)));
     if (!st) st = cuda_status(cudaMemset(p->d_err, 0, sizeof(int)));
+    if (st) return st;
+  }
+  if (!p->d_nonfinite) {
+    int st = cuda_status(cudaMalloc(&p->d_nonfinite, sizeof(unsigned long long)));
+    if (!st) st = cuda_status(cudaMemset(p->d_nonfinite, 0, sizeof(unsigned long long)));
     if (st) return st;
   }
   const int64_t wsb = mf_ws_bytes(p->k, p->prec);
@@ -932,9 +980,11 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
     return last_launch();
   mark(3);
   size_t shm = (size_t)(A.ndim * A.nb + 3 * 256) * sizeof(double);
-  cudaFuncSetAttribute(accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  static bool attr_done[64] = {false};
+  st = smem_attr_once((const void*)accum_kernel, attr_done);
+  if (st) return st;
   accum_kernel<<<accum_grid, 256, shm, S(stream)>>>(A.pref, A.me, A.bins, A.N, A.ndim, A.nb, A.inv_n, f_out,
-                                                     results ? p->d_partials : nullptr);
+                                                     results ? p->d_partials : nullptr, p->d_err, p->d_nonfinite);
   if (results)
     reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(p->d_partials, accum_grid, width, results);
   mark(4);
@@ -954,8 +1004,14 @@ int mf_process_tuning(const mf_process* p, int* colour, int* waves, int* tuned, 
 int mf_process_set_tuning(mf_process* p, int colour, int waves) {
   if (!p || (colour != 0 && colour != 1) || (waves != 1 && waves != 2 && waves != 4 && waves != 8)) return MF_ERR_ARG;
   if (colour == 1 && (p->prec == MF_PREC_FP64 || !mf_colour_tc(p->k))) return MF_ERR_UNSUPPORTED;
-  p->tune = {colour, waves};
+  p->tune = {colour, waves, p->tune.wait_tries};
   p->tuned = true;
+  return MF_OK;
+}
+
+int mf_process_set_wait_limit(mf_process* p, int tries) {
+  if (!p || tries < 0 || tries > 100000) return MF_ERR_ARG;
+  p->tune.wait_tries = tries;
   return MF_OK;
 }
 
@@ -966,6 +1022,18 @@ int mf_process_error_flags(mf_process* p, int* flags, int clear) {
   int st = cuda_status(cudaMemcpy(flags, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (!st && clear) st = cuda_status(cudaMemset(p->d_err, 0, sizeof(int)));
   return st;
+}
+
+int mf_process_nonfinite(mf_process* p, int64_t* count, int clear) {
+  if (!p || !count) return MF_ERR_ARG;
+  *count = 0;
+  if (!p->d_nonfinite) return MF_OK;
+  unsigned long long c = 0;
+  int st = cuda_status(cudaMemcpy(&c, p->d_nonfinite, sizeof(c), cudaMemcpyDeviceToHost));
+  if (!st && clear) st = cuda_status(cudaMemset(p->d_nonfinite, 0, sizeof(c)));
+  if (st) return st;
+  *count = (int64_t)c;
+  return c ? MF_ERR_NONFINITE : MF_OK;
 }
 
 int mf_process_set_timing(mf_process* p, int enable) {
@@ -1084,29 +1152,44 @@ int mf_unweight(const double* w, int64_t N, double w_max, uint64_t seed, uint32_
   return last_launch();
 }
 
+// Block partials of mf_vegas_accumulate: one buffer per host thread and
+// device (calls of different threads never share one), freed when the thread
+// exits.
+struct AccumPartials {
+  double* part[64] = {nullptr};
+  size_t cap[64] = {0};
+  ~AccumPartials() {
+    for (double* p : part)
+      if (p) cudaFree(p);
+  }
+};
+
 int mf_vegas_accumulate(const double* f, const double* jac, const int32_t* bins, int64_t N, int ndim, int nb,
                         double inv_n, double* results, void* stream) {
-  if (!f || !jac || !bins || !results || N <= 0 || ndim <= 0 || nb < 2 || ndim * nb > 8192) return MF_ERR_ARG;
-  static thread_local double* part[64] = {nullptr};
-  static thread_local size_t cap[64] = {0};
+  if (!f || !jac || !bins || !results || N <= 0 || ndim <= 0 || nb < 2 || (int64_t)ndim * nb > kAccumMaxBins)
+    return MF_ERR_ARG;
+  static thread_local AccumPartials P;
   int dev = 0;
   int st = cuda_status(cudaGetDevice(&dev));
   if (st) return st;
+  if (dev < 0 || dev >= 64) return MF_ERR_CAPACITY;
   int blocks = 256;
   int width = 2 + ndim * nb;
   size_t need = (size_t)blocks * width;
-  if (cap[dev] < need) {
-    if (part[dev]) cudaFree(part[dev]);
-    part[dev] = nullptr;
-    cap[dev] = 0;
-    st = cuda_status(cudaMalloc(&part[dev], need * sizeof(double)));
+  if (P.cap[dev] < need) {
+    if (P.part[dev]) cudaFree(P.part[dev]);
+    P.part[dev] = nullptr;
+    P.cap[dev] = 0;
+    st = cuda_status(cudaMalloc(&P.part[dev], need * sizeof(double)));
     if (st) return st;
-    cap[dev] = need;
+    P.cap[dev] = need;
   }
+  static bool attr_done[64] = {false};
+  st = smem_attr_once((const void*)vegas_accum_kernel, attr_done);
+  if (st) return st;
   size_t shm = (size_t)(ndim * nb + 3 * 256) * sizeof(double);
-  cudaFuncSetAttribute(vegas_accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  vegas_accum_kernel<<<blocks, 256, shm, S(stream)>>>(f, jac, bins, N, ndim, nb, inv_n, part[dev]);
-  reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(part[dev], blocks, width, results);
+  vegas_accum_kernel<<<blocks, 256, shm, S(stream)>>>(f, jac, bins, N, ndim, nb, inv_n, P.part[dev]);
+  reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(P.part[dev], blocks, width, results);
   return last_launch();
 }
 
@@ -1159,8 +1242,10 @@ int mf_vegas_accumulate_noalloc(const double* f, const double* jac, const int32_
   const int width = 2 + ndim * nb;
   // every block writes all `width` entries of its row, so the partials left
   // by an earlier call never need clearing
+  static bool attr_done[64] = {false};
+  st = smem_attr_once((const void*)vegas_accum_kernel, attr_done);
+  if (st) return st;
   size_t shm = (size_t)(ndim * nb + 3 * 256) * sizeof(double);
-  cudaFuncSetAttribute(vegas_accum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   vegas_accum_kernel<<<blocks, 256, shm, S(stream)>>>(f, jac, bins, N, ndim, nb, inv_n, part);
   reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(part, blocks, width, results);
   return last_launch();

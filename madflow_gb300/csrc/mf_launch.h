@@ -7,9 +7,13 @@ struct IterArgs;
 // Launch configuration of the matrix-element kernel (chosen by the
 // autotuner): colour sum on the SIMT lanes (0) or the tensor cores (1), and
 // the grid as `waves` x (SMs x resident blocks per SM).
+// wait_tries: ~1 ms tries of each bounded wait on the tensor cores before a
+// block gives up (its events then get NaN and error bit 0 is raised).
+constexpr int MF_TC_WAIT_TRIES = 1000;
 struct MeTune {
   int colour;
   int waves;
+  int wait_tries;
 };
 // Work list of one multi-process launch: n processes, process j with k[j]
 // gluons, records prep[j], its events at list positions [off[j], off[j+1]),

@@ -207,7 +207,13 @@ template <int K, class P> __global__ void __launch_bounds__(256) ps_seed_kernel(
     st[(int64_t)(4 * K + 3) * N] = x1;
     st[(int64_t)(4 * K + 4) * N] = x2;
     st[(int64_t)(4 * K + 5) * N] = (double)jacp;
-    if (batch_rule) {
+    // a non-finite event (e.g. from non-finite caller points) takes no part
+    // in the batch minimum: its f0 > ACC test is false at once, which would
+    // otherwise stop the Newton iteration of the whole batch
+    double chk = logw + shat;
+#pragma unroll
+    for (int i = 0; i < K; ++i) chk += p[i + 2][0];
+    if (batch_rule && isfinite(chk)) {
       const int lim = min(local, *(volatile int*)kmin);
       const double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
       const int c = newton_conv_iter_xs<sizeof(P) == 4>(K, A.masses, p + 2, roots, KC.acc, lim,
@@ -266,12 +272,19 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
   }
 }
 
+// The weight f = pref * me of an event; a non-finite f (NaN or +-inf from a
+// non-finite input point or matrix element) is replaced by 0.
+MF_DO double finite_weight(double f) { return isfinite(f) ? f : 0.0; }
+
 // w = pref * me * inv_n; block b owns a contiguous slice of events.  f_out
-// (optional) = pref * me.  partials [gridDim][2 + ndim*nb].
+// (optional) = pref * me.  partials [gridDim][2 + ndim*nb].  Non-finite
+// weights are counted into *nonfinite (bit 1 of *err set) and enter the sums,
+// the histogram and f_out as 0.
 static __global__ void __launch_bounds__(256) accum_kernel(const double* __restrict__ pref, const double* __restrict__ me,
                                                     const unsigned char* __restrict__ bins, int64_t N, int ndim,
                                                     int nb, double inv_n, double* __restrict__ f_out,
-                                                    double* __restrict__ partials) {
+                                                    double* __restrict__ partials, int* __restrict__ err,
+                                                    unsigned long long* __restrict__ nonfinite) {
   extern __shared__ double sh[];  // [ndim*nb] + [2*blockDim] + [blockDim]
   double* hist = sh;
   double* red = sh + ndim * nb;
@@ -280,12 +293,19 @@ static __global__ void __launch_bounds__(256) accum_kernel(const double* __restr
   int64_t e0 = (int64_t)blockIdx.x * per, e1 = min(N, e0 + per);
   for (int i = threadIdx.x; i < ndim * nb; i += blockDim.x) hist[i] = 0.0;
   double a = 0.0, b = 0.0;
+  unsigned int bad = 0;
   for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-    double f = pref[e] * me[e];
+    const double f0 = pref[e] * me[e];
+    const double f = finite_weight(f0);
+    bad += f0 != f;
     if (f_out) f_out[e] = f;
     double w = f * inv_n;
     a += w;
     b += w * w;
+  }
+  if (bad) {
+    if (nonfinite) atomicAdd(nonfinite, (unsigned long long)bad);
+    if (err) atomicOr(err, 2);
   }
   red[threadIdx.x] = a;
   red[blockDim.x + threadIdx.x] = b;
@@ -304,7 +324,7 @@ static __global__ void __launch_bounds__(256) accum_kernel(const double* __restr
     for (int64_t c0 = e0; c0 < e1; c0 += blockDim.x) {
       const int64_t e = c0 + threadIdx.x;
       if (e < e1) {
-        const double w = pref[e] * me[e] * inv_n;
+        const double w = finite_weight(pref[e] * me[e]) * inv_n;
         w2[threadIdx.x] = w * w;
       }
       __syncthreads();

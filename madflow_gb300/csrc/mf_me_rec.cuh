@@ -125,15 +125,23 @@ MF_D void prep_event(PrepRec<T, K>& r, const double (*p)[4], double mt, double w
     for (int b = 0; b < 2; ++b)
       r.G[q][b] = vxxxxx<T>(r.ev.pext[part], T(0), b ? T(1) : T(-1), part < 2 ? T(-1) : T(1), sqh);
   }
+  // The top and anti-top spinors, and from them the top-line bilinears of
+  // the four (top, anti-top) spin combinations M[q][mu] = WTB[q>>1]^T
+  // S(e_mu) WT[q&1] (an amplitude in which the full gluon current J meets
+  // the top line directly is J . M, S being linear in J), are formed in FP64
+  // and stored in T.  The small spinor components sqrt(E - |p|) of a boosted
+  // top lose their digits to cancellation in FP32, and where a top runs
+  // along a beam gluon the sum over diagrams amplifies that error about
+  // 1e5-fold (|M|^2 off by up to 4e-2 in FP32 spinors, 1e-6 with these).
+  W4<double> wt64[2], wtb64[2];
   for (int b = 0; b < 2; ++b) {
-    r.WT[b] = oxxxxx<T>(r.ev.pext[2], r.ev.mt, b ? T(1) : T(-1), T(1));
-    r.WTB[b] = ixxxxx<T>(r.ev.pext[3], r.ev.mt, b ? T(1) : T(-1), T(-1));
+    wt64[b] = oxxxxx<double>(p[2], mt, b ? 1.0 : -1.0, 1.0);
+    wtb64[b] = ixxxxx<double>(p[3], mt, b ? 1.0 : -1.0, -1.0);
+    r.WT[b] = w4cast<T>(wt64[b]);
+    r.WTB[b] = w4cast<T>(wtb64[b]);
   }
-  // the top-line bilinears of the four (top, anti-top) spin combinations,
-  // M[q][mu] = WTB[q>>1]^T S(e_mu) WT[q&1]: an amplitude in which the full
-  // gluon current J meets the top line directly is J . M (S is linear in J)
   for (int q = 0; q < 4; ++q)
-    for (int mu = 0; mu < 4; ++mu) r.ev.M[q][mu] = dot4(unit_row(r.WTB[q >> 1], mu), r.WT[q & 1]);
+    for (int mu = 0; mu < 4; ++mu) r.ev.M[q][mu] = ccast<T>(dot4(unit_row(wtb64[q >> 1], mu), wt64[q & 1]));
   r.scale = (c11.re * c11.re + c11.im * c11.im) / (R::COLOUR_DEN * R::DENOMINATOR);
 }
 
@@ -189,12 +197,11 @@ MF_D W4<T> rec_current(const RecWS<T, K>& ws, const EvData<T, K>& ev, int r, int
     const int4 g = R::prog4(r + 4 * i);  // J offsets and subsets of both sides
     W4<T> a = ws.J.get(g.x + (hp & ((1 << i) - 1)));
     W4<T> b = ws.J.get(g.y + (hp >> i));
-    // FP32: the conserved-current form (what it drops is zero up to
-    // rounding); FP64 keeps every term (a counting scalar counts the FP32 form)
-    if constexpr (!std::is_same<T, double>::value)
-      vvv_add_cons<T>(a, ev.Qg[g.z], b, ev.Qg[g.w], a3);
-    else
-      vvv_add<T>(a, ev.Qg[g.z], b, ev.Qg[g.w], a3);
+    // every term of the vertex, also in FP32: the conserved-current form
+    // (which drops the a.Qa and b.Qb terms) lost up to 1e-2 of |M|^2 where
+    // two gluons are nearly collinear, since FP32 currents are conserved
+    // only up to rounding
+    vvv_add<T>(a, ev.Qg[g.z], b, ev.Qg[g.w], a3);
   }
   int q = r + 4 * L;
   for (int i = 1; i < L; ++i)
@@ -585,6 +592,23 @@ template <class T, int K, int NT> MF_DO double me_rec_event(RecSmem<T, K>& S, co
   return r;
 }
 
+// After a bounded tensor-core wait ran out: the events e, e + stride, ...
+// below N of a block get NaN in out (and hel_out), except events with
+// skip[e] == +-0, which need no work and get 0 as usual.  Every thread of the
+// block takes part (no barrier); thread tid writes the helicity rows tid,
+// tid + nt, ...
+template <int K>
+MF_DO void mark_rest_nan(int64_t e, int64_t N, int64_t stride, const double* __restrict__ skip,
+                         double* __restrict__ out, double* __restrict__ hel_out, int tid, int nt) {
+  const double qnan = __longlong_as_double(0x7ff8000000000000ll);
+  for (; e < N; e += stride) {
+    const bool none = skip && (__double_as_longlong(skip[e]) << 1) == 0;
+    if (tid == 0) out[e] = none ? 0.0 : qnan;
+    if (hel_out && !none)
+      for (int c = tid; c < (1 << (K + 2)); c += nt) hel_out[(int64_t)c * N + e] = qnan;
+  }
+}
+
 // Processes whose workspace does not fit in shared memory (five gluons: 523
 // KB in FP32) keep it in global memory, one per block (ws [gridDim]); the
 // record and the reduction stay in shared memory.  Same stages and outputs
@@ -619,7 +643,7 @@ template <int K, class T, int COLOUR>
 __global__ void __launch_bounds__(MF_GWS_NT)
     me_gws_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
                   double* __restrict__ out, double* __restrict__ hel_out, RecWS<T, K>* __restrict__ ws_all,
-                  int* __restrict__ err) {
+                  int* __restrict__ err, uint32_t wait_tries) {
   using R = RecTraits<K>;
   constexpr bool TC = COLOUR == 1 && use_colour_tc_gws<T, K>();
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -701,7 +725,7 @@ __global__ void __launch_bounds__(MF_GWS_NT)
           }
           // every thread waits: the next chunk overwrites the operands
           bool done = false;
-          for (uint32_t spin = 0; spin < 1000u; ++spin) {
+          for (uint32_t spin = 0; spin < wait_tries; ++spin) {
             done = tc_mbar_try_wait(&S.mbar, phase, 1000000u);
             if (__all_sync(0xffffffffu, done)) break;
           }
@@ -751,7 +775,12 @@ __global__ void __launch_bounds__(MF_GWS_NT)
       out[e] = bad ? __longlong_as_double(0x7ff8000000000000ll) : (double)tot * sc;
       if (bad && err) atomicOr(err, 1);
     }
-    if (bad) break;
+    if (bad) {
+      // the tensor cores are no longer trusted: every later event of this
+      // block that needs work gets NaN (no stale value survives in out)
+      mark_rest_nan<K>(e + gridDim.x, N, gridDim.x, skip, out, hel_out, tid, nt);
+      break;
+    }
   }
 #if MF_TCGEN05
   if constexpr (TC) {
@@ -782,7 +811,8 @@ template <class T, int K> constexpr bool use_colour_tc() {
 template <int K, class T, int COLOUR>
 __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     me_rec_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
-                  double* __restrict__ out, double* __restrict__ hel_out, int* __restrict__ err) {
+                  double* __restrict__ out, double* __restrict__ hel_out, int* __restrict__ err,
+                  uint32_t wait_tries) {
   using R = RecTraits<K>;
   constexpr bool TC = COLOUR == 1 && use_colour_tc<T, K>();
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -860,7 +890,7 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
         // bounded, warp-uniform wait (the accumulator loads are warp-collective)
         // (each try suspends for up to 1 ms; 1000 tries bound the wait to ~1 s)
         bool done = false;
-        for (uint32_t spin = 0; spin < 1000u; ++spin) {
+        for (uint32_t spin = 0; spin < wait_tries; ++spin) {
           done = tc_mbar_try_wait(&S.mbar, phase, 1000000u);
           if (__all_sync(0xffffffffu, done)) break;
         }
@@ -904,7 +934,11 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
       out[e] = bad ? __longlong_as_double(0x7ff8000000000000ll) : (double)tot * sc;
       if (bad && err) atomicOr(err, 1);
     }
-    if (bad) break;
+    if (bad) {
+      // every later event of this block that needs work gets NaN
+      mark_rest_nan<K>(en, N, gridDim.x, skip, out, hel_out, tid, nt);
+      break;
+    }
     if constexpr (!TC)
       if (en < N) load_ext(en);
     e = en;

@@ -41,7 +41,7 @@ static int sm_count() {
   }                                                                                                            \
   template <class T, int COLOUR>                                                                               \
   static int me_rec_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out, double* hel_out, \
-                                 int* err, int waves, cudaStream_t st) {                                       \
+                                 int* err, int waves, uint32_t tries, cudaStream_t st) {                                       \
     if constexpr (events_per_block<KK>() > 1) {                                                                \
       /* several events per block (few helicities and colour flows) */                                        \
       const void* fm = (const void*)me_rec_multi_kernel<KK, T>;                                                \
@@ -71,7 +71,7 @@ static int sm_count() {
       int64_t g = (int64_t)sm_count() * per * (waves > 0 ? waves : 1);                                         \
       if (g > N) g = N;                                                                                        \
       if (g < 1) g = 1;                                                                                        \
-      me_rec_kernel<KK, T, COLOUR><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out, err);        \
+      me_rec_kernel<KK, T, COLOUR><<<(int)g, MF_REC_NT, bytes, st>>>(prep, N, skip, out, hel_out, err, tries); \
       return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                     \
     }                                                                                                          \
   }                                                                                                            \
@@ -81,14 +81,15 @@ static int sm_count() {
   bool mf_colour_tc_k##KK() { return TcTraits<KK>::enabled; }                                                  \
   template <class T, int COLOUR>                                                                               \
   static int me_gws_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out, double* hel_out,  \
-                                 int* err, void* ws, cudaStream_t st) {                                        \
+                                 int* err, void* ws, uint32_t tries, cudaStream_t st) {                        \
     if (!ws) return 3;                                                                                         \
     const void* fn = (const void*)me_gws_kernel<KK, T, COLOUR>;                                                \
     int bytes = gws_smem_bytes<T, KK>(COLOUR);                                                                 \
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);                              \
     int64_t g = (int64_t)sm_count() * MF_GWS_PER_SM;                                                           \
     me_gws_kernel<KK, T, COLOUR><<<(int)g, MF_GWS_NT, bytes, st>>>(prep, N, skip, out, hel_out,                \
-                                                                   reinterpret_cast<RecWS<T, KK>*>(ws), err);  \
+                                                                   reinterpret_cast<RecWS<T, KK>*>(ws), err,   \
+                                                                   tries);                                     \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }                                                                                                            \
   int64_t mf_ws_bytes_k##KK(int prec) {                                                                        \
@@ -99,18 +100,18 @@ static int sm_count() {
                          double* hel_out, int* err, MeTune t, void* ws, cudaStream_t st) {                     \
     if (prec == 0) {                                                                                           \
       if constexpr (rec_in_smem<KK, double>())                                                                 \
-        return me_rec_launch_k##KK<double, 0>(prep, N, skip, out, hel_out, err, t.waves, st);                 \
+        return me_rec_launch_k##KK<double, 0>(prep, N, skip, out, hel_out, err, t.waves, (uint32_t)t.wait_tries, st);                 \
       else                                                                                                     \
-        return me_gws_launch_k##KK<double, 0>(prep, N, skip, out, hel_out, err, ws, st);                       \
+        return me_gws_launch_k##KK<double, 0>(prep, N, skip, out, hel_out, err, ws, (uint32_t)t.wait_tries, st);                       \
     }                                                                                                          \
     if constexpr (!rec_in_smem<KK, float>()) {                                                                 \
       if constexpr (TcTraits<KK>::enabled)                                                                     \
-        if (t.colour == 1) return me_gws_launch_k##KK<float, 1>(prep, N, skip, out, hel_out, err, ws, st);     \
-      return me_gws_launch_k##KK<float, 0>(prep, N, skip, out, hel_out, err, ws, st);                          \
+        if (t.colour == 1) return me_gws_launch_k##KK<float, 1>(prep, N, skip, out, hel_out, err, ws, (uint32_t)t.wait_tries, st);     \
+      return me_gws_launch_k##KK<float, 0>(prep, N, skip, out, hel_out, err, ws, (uint32_t)t.wait_tries, st);                          \
     } else {                                                                                                   \
       if constexpr (TcTraits<KK>::enabled)                                                                     \
-        if (t.colour == 1) return me_rec_launch_k##KK<float, 1>(prep, N, skip, out, hel_out, err, t.waves, st); \
-      return me_rec_launch_k##KK<float, 0>(prep, N, skip, out, hel_out, err, t.waves, st);                    \
+        if (t.colour == 1) return me_rec_launch_k##KK<float, 1>(prep, N, skip, out, hel_out, err, t.waves, (uint32_t)t.wait_tries, st); \
+      return me_rec_launch_k##KK<float, 0>(prep, N, skip, out, hel_out, err, t.waves, (uint32_t)t.wait_tries, st);                    \
     }                                                                                                          \
   }                                                                                                            \
   int mf_launch_prep_k##KK(int prec, const double* ps, int64_t N, double mt, double wt, const double* coup,    \

@@ -32,17 +32,6 @@ template <class T> MF_D void vvv_add(const W4<T>& a, const T* Qa, const W4<T>& b
 #pragma unroll
   for (int k = 0; k < 4; ++k) acc.v[k] += (Qb[k] - Qa[k]) * ab + a.v[k] * ca - b.v[k] * cb;
 }
-// The same for conserved currents (Qa.a = Qb.b = 0: external gluons and
-// Berends-Giele currents, Nucl. Phys. B306 (1988) 759):
-//   acc += (a.b)(Qb-Qa) + 2 a (b.Qa) - 2 b (a.Qb).
-template <class T>
-MF_D void vvv_add_cons(const W4<T>& a, const T* Qa, const W4<T>& b, const T* Qb, W4<T>& acc) {
-  cx<T> ab = mdot(a, b);
-  cx<T> ca = T(2) * mdotq(b, Qa[0], Qa[1], Qa[2], Qa[3]);
-  cx<T> cb = T(2) * mdotq(a, Qb[0], Qb[1], Qb[2], Qb[3]);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) acc.v[k] += (Qb[k] - Qa[k]) * ab + a.v[k] * ca - b.v[k] * cb;
-}
 // Four-gluon colour-ordered contact term for the order (a, b, d, off-shell):
 //   acc += 2 b (a.d) - a (b.d) - d (a.b)
 template <class T> MF_D void vvvv_add(const W4<T>& a, const W4<T>& b, const W4<T>& d, W4<T>& acc) {

@@ -19,6 +19,7 @@ Two paths:
 import ctypes
 import math
 import time
+import warnings
 
 import torch
 
@@ -73,6 +74,27 @@ class FusedIntegrand:
                   grid.shape[1] - 1, int(seed), int(stream_id), iteration_dev.data_ptr(), int(n_events),
                   results.data_ptr(), f_out.data_ptr() if f_out is not None else None,
                   u_out.data_ptr() if u_out is not None else None, stream_ptr())
+
+    def check_errors(self, clear=True):
+        """Read the handle's device error state (synchronous).  Raises
+        DeviceError when a bounded tensor-core wait ran out (bit 0 of
+        mf_process_error_flags: the affected events got NaN); returns the
+        number of non-finite event weights that entered the sums as 0 since
+        the last check (mf_process_nonfinite)."""
+        flags = ctypes.c_int()
+        _lib.call("mf_process_error_flags", self.matrix.handle, ctypes.byref(flags), int(bool(clear)))
+        count = ctypes.c_int64()
+        st = _lib.load().mf_process_nonfinite(self.matrix.handle, ctypes.byref(count), int(bool(clear)))
+        if st not in (_lib.MF_OK, _lib.MF_ERR_NONFINITE):
+            raise _lib.MadflowError(st, "mf_process_nonfinite")
+        if flags.value & 1:
+            raise _lib.DeviceError("a bounded wait on the tensor cores ran out in the matrix-element kernel; "
+                                   "the affected events were set to NaN")
+        return int(count.value)
+
+    def set_wait_limit(self, tries):
+        """Tries (~1 ms each) of each bounded tensor-core wait (default 1000)."""
+        _lib.call("mf_process_set_wait_limit", self.matrix.handle, int(tries))
 
     def tuning(self):
         """The matrix-element launch configuration of the handle: colour sum
@@ -158,6 +180,7 @@ class VegasFlow:
         self.width = 2 + self.n_dim * self.nbins
         self.results = torch.zeros(self.width, dtype=DTYPE, device=device())
         self.history = []  # (result, sigma) per iteration
+        self.nonfinite = 0  # event weights that were not finite and entered the sums as 0
         self.integrand = None
         self._graph = None
 
@@ -199,6 +222,12 @@ class VegasFlow:
                       jac.data_ptr(), bins.data_ptr(), stream_ptr())
             f = self.integrand(x.T, n_dim=self.n_dim, weight=jac / self.n_events)
             f = to_device(f).reshape(-1)
+            bad = ~torch.isfinite(f)
+            nbad = int(bad.sum())
+            if nbad:
+                # counted and zeroed, as the fused path does on the device
+                f = torch.where(bad, torch.zeros_like(f), f)
+                self._note_nonfinite(nbad)
             _lib.call("mf_vegas_accumulate", f.data_ptr(), jac.data_ptr(), bins.data_ptr(), n, self.n_dim,
                       self.nbins, 1.0 / self.n_events, tmp.data_ptr(), stream_ptr())
             res += tmp
@@ -250,16 +279,31 @@ class VegasFlow:
             return
         self._graph.replay()
 
+    def _note_nonfinite(self, n):
+        self.nonfinite += n
+        warnings.warn(f"{n} non-finite event weights entered iteration {len(self.history) + 1} as 0",
+                      RuntimeWarning, stacklevel=3)
+
+    def _check_device(self):
+        """After an iteration's results reached the host: raise if a kernel
+        reported a tensor-core timeout, count zeroed non-finite weights."""
+        if isinstance(self.integrand, FusedIntegrand):
+            n = self.integrand.check_errors()
+            if n:
+                self._note_nonfinite(n)
+
     def run_event(self):
         if self.group is not None:
             self._iteration_sharded()
             r = self.results[:2].double().cpu().numpy()
+            self._check_device()
             return iteration_estimate(float(r[0]), float(r[1]), self.n_events, self.world)
         if isinstance(self.integrand, FusedIntegrand):
             self._iteration_fused()
         else:
             self._iteration_python()
         r = self.results[:2].double().cpu().numpy()
+        self._check_device()
         n = self.n_events
         res = float(r[0])
         var = (n * float(r[1]) - res * res) / (n - 1.0)

@@ -94,16 +94,26 @@ inline CountF fmin(CountF a, CountF b) { return a.v < b.v ? a : b; }
 inline CountF fmax(CountF a, CountF b) { return a.v < b.v ? b : a; }
 inline CountF floor(CountF a) { return CountF(std::floor(a.v)); }
 
-// Flops of one event of the recycled evaluation (all helicity combinations).
-extern "C" double me_host_flops(int k, const double* p, const double* coup, double mt, double wt) {
+// Flops of one event of the recycled evaluation (all helicity combinations)
+// as the matrix-element kernel runs it: the stages, amplitudes and colour sum
+// from a ready record (the record itself is built by the phase-space kernel).
+template <int K> static double stage_flops(const double* p, const double* coup, double mt, double wt) {
+  auto ws = std::make_unique<RecWS<CountF, K>>();
+  auto pr = std::make_unique<PrepRec<CountF, K>>();
+  double pd[K + 2][4];
+  std::memcpy(pd, p, sizeof(pd));
+  prep_event<CountF, K>(*pr, pd, mt, wt, {coup[0], coup[1]}, {coup[2], coup[3]}, {coup[4], coup[5]});
   CountF::n = 0;
-  double out = 0.0;
-  if (k == 2) out = smatrix_one<2, CountF>(p, coup, mt, wt, nullptr);
-  else if (k == 3) out = smatrix_one<3, CountF>(p, coup, mt, wt, nullptr);
-  else if (k == 4) out = smatrix_one<4, CountF>(p, coup, mt, wt, nullptr);
-  else if (k == 5) out = smatrix_one<5, CountF>(p, coup, mt, wt, nullptr);
-  (void)out;
+  double tot = RecHostRun<CountF, K>::run(*ws, *pr, 7);
+  (void)tot;
   return (double)CountF::n;
+}
+extern "C" double me_host_flops(int k, const double* p, const double* coup, double mt, double wt) {
+  if (k == 2) return stage_flops<2>(p, coup, mt, wt);
+  if (k == 3) return stage_flops<3>(p, coup, mt, wt);
+  if (k == 4) return stage_flops<4>(p, coup, mt, wt);
+  if (k == 5) return stage_flops<5>(p, coup, mt, wt);
+  return 0.0;
 }
 
 extern "C" int me_host_helicities(int k, const double* p, const double* coup, double mt, double wt, double* hel_out) {
