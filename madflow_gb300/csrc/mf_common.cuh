@@ -42,12 +42,6 @@ template <class T> MF_HD W4<T> w4zero() {
   for (int i = 0; i < 4; ++i) z.v[i] = cx<T>{T(0), T(0)};
   return z;
 }
-template <class T, class S> MF_HD W4<T> w4cast(const W4<S>& a) {
-  W4<T> z;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) z.v[i] = ccast<T>(a.v[i]);
-  return z;
-}
 template <class T> MF_HD W4<T> neg(const W4<T>& a) {
   W4<T> z;
 #pragma unroll

@@ -79,7 +79,6 @@ const PdfHost& pdf_host() {
 }
 std::mutex g_pdf_mu;
 double* g_pdf_dev[64] = {nullptr};
-float* g_pdf_devf[64] = {nullptr};
 int pdf_device_table(PdfTable& T) {
   int dev = 0;
   int st = cuda_status(cudaGetDevice(&dev));
@@ -90,23 +89,16 @@ int pdf_device_table(PdfTable& T) {
     std::lock_guard<std::mutex> lk(g_pdf_mu);
     if (!g_pdf_dev[dev]) {
       double* d = nullptr;
-      float* f = nullptr;
-      std::vector<float> tf(H.tab.begin(), H.tab.end());
       st = cuda_status(cudaMalloc(&d, sizeof(double) * kNX * kNQ));
-      if (!st) st = cuda_status(cudaMalloc(&f, sizeof(float) * kNX * kNQ));
       if (!st) st = cuda_status(cudaMemcpy(d, H.tab.data(), sizeof(double) * kNX * kNQ, cudaMemcpyHostToDevice));
-      if (!st) st = cuda_status(cudaMemcpy(f, tf.data(), sizeof(float) * kNX * kNQ, cudaMemcpyHostToDevice));
       if (st) {
         cudaFree(d);
-        cudaFree(f);
         return st;
       }
       g_pdf_dev[dev] = d;
-      g_pdf_devf[dev] = f;
     }
   }
   T.tab = g_pdf_dev[dev];
-  T.tabf = g_pdf_devf[dev];
   T.nx = kNX;
   T.nq = kNQ;
   T.lx0 = H.lx0;

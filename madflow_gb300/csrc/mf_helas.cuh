@@ -9,6 +9,17 @@ template <class T> MF_D T tf_sign(T y) { return y > T(0) ? T(1) : (y < T(0) ? T(
 // floor(a / 2) of the small integers the helicity projectors take, in T
 template <class T> MF_D int floordiv2(T a) { return (int)floor(a * T(0.5)); }
 
+// pp + p3 of a massive fermion (pp = |p|).  For a fermion moving along -z
+// the sum cancels; in FP32 it is then formed as (p1^2 + p2^2) / (pp - p3),
+// which is exact algebra without the cancellation (a top quark running along
+// a beam lost up to 4e-2 of |M|^2 to the rounded difference).  FP64 keeps
+// the reference's sum (wavefunctions_flow.py:214, :418).
+template <class T> MF_D T pp_plus_p3(const T* p, T pp) {
+  if constexpr (sizeof(T) == 4)
+    if (p[3] < T(0)) return (p[1] * p[1] + p[2] * p[2]) / (pp - p[3]);
+  return fmax(pp + p[3], T(0));
+}
+
 // _ox_massive_pp_zero (wavefunctions_flow.py:370-392)
 template <class T> MF_D void ox_massive_pp_zero(T fmass, T nsf, int ip, int im, W4<T>& f) {
   T s0 = sqrt(fabs(fmass));
@@ -36,7 +47,7 @@ template <class T> MF_D W4<T> ixxxxx(const T* p, T fmass, T nhel, T nsf) {
     T sq = sqrt(p[0] + pp);
     T om[2] = {sq, fmass / sq};
     T sfo0 = sf0 * om[ip], sfo1 = sf1 * om[im];
-    T pp3 = fmax(pp + p[3], T(0));
+    T pp3 = pp_plus_p3<T>(p, pp);
     cx<T> chi1;
     if (pp3 == T(0)) chi1 = {-nh, T(0)};
     else {
@@ -77,7 +88,7 @@ template <class T> MF_D W4<T> oxxxxx(const T* p, T fmass, T nhel, T nsf) {
     T om[2] = {sq, fmass / sq};
     int ip = floordiv2<T>(T(1) + nh), im = floordiv2<T>(T(1) - nh);
     T sfo0 = sf0 * om[ip], sfo1 = sf1 * om[im];
-    T pp3 = fmax(pp + p[3], T(0));
+    T pp3 = pp_plus_p3<T>(p, pp);
     cx<T> chi1;
     if (pp3 == T(0)) chi1 = {-nh, T(0)};
     else {

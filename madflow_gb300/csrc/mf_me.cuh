@@ -124,12 +124,10 @@ MF_DO void event_massless(const IterArgs& A, int npart, const P* x, double w0, d
     shat = A.sqrts * A.sqrts;
     wgt = 1.0;
   } else {
-    P sh, wg, a1, a2;
-    get_x1x2<P>(x[0], x[1], (P)A.shat_min, (P)(A.sqrts * A.sqrts), sh, wg, a1, a2);
-    shat = sh;
-    wgt = wg;
-    x1 = a1;
-    x2 = a2;
+    // x1, x2, s-hat and the x1 x2 weight in FP64 for either precision: the
+    // PDF's (1 - x)^5 falls steeply towards x = 1, where the FP32 rounding
+    // of x1 = tau^u1 showed up as 1e-3 of the weight
+    get_x1x2<double>((double)x[0], (double)x[1], A.shat_min, A.sqrts * A.sqrts, shat, wgt, x1, x2);
     xr = x + 2;
   }
   double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
@@ -142,14 +140,18 @@ MF_DO void event_massless(const IterArgs& A, int npart, const P* x, double w0, d
 // newton_iters iterations (<= 0: per event), incoming momenta, flux, lab
 // boost, cuts and luminosity.  v: the PDF table coordinate of Q^2; pw:
 // (2 pi)^(3 nout - 4).  Returns false when the event fails the cuts.
+// The event weight (the exponentiated log-weight, flux, luminosity) is FP64
+// for either precision P: exp of an FP32 log-weight of 30 to 50 alone erred
+// by 2e-6; the cuts are decided in P.
 template <class P>
 MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (*p)[4], double logw, double shat,
-                        double wgt, double x1, double x2, P v, double pw, double& wgt_lum, double x_start = -1.0) {
+                        double wgt, double x1, double x2, double v, double pw, double& wgt_lum,
+                        double x_start = -1.0) {
   MfConsts KC = mf_consts(A.f32q != 0);
   int nout = npart - 2;
   double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
   logw = rambo_massive<P>(nout, A.masses, p + 2, roots, logw, KC.acc, newton_iters, x_start);
-  double wps = (double)ps_exp((P)logw) / pw;
+  double wps = exp(logw) / pw;
   double ein = roots / 2.0;
   p[0][0] = ein; p[0][1] = 0.0; p[0][2] = 0.0; p[0][3] = ein;
   p[1][0] = ein; p[1][1] = 0.0; p[1][2] = 0.0; p[1][3] = -ein;
@@ -169,8 +171,8 @@ MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (
     }
     ok = pass_gluon_cuts<P>(plab, npart, (P)A.ptmin, (P)A.etamax, (P)A.drmin);
   }
-  P lum = pdf_xfx_v<P>(A.pdf, (P)x1, v) * pdf_xfx_v<P>(A.pdf, (P)x2, v) / (P)x1 / (P)x2;
-  wgt_lum = wgt * (double)lum;
+  const double lum = pdf_xfx_v(A.pdf, x1, v) * pdf_xfx_v(A.pdf, x2, v) / x1 / x2;
+  wgt_lum = wgt * lum;
   return ok;
 }
 
@@ -236,7 +238,7 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
   // the batch rule runs at most 10 iterations (11 = no event converged)
   const int niter = min(*A.newton_iters, 10);
   const MfConsts KC = mf_consts(A.f32q != 0);
-  const T v = (T)pdf_qcoord(A.pdf, A.q2);
+  const double v = pdf_qcoord(A.pdf, A.q2);
   const double pw = pow(2.0 * KC.pi, (double)(3 * K - 4));
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
     double p[NPART][4], wl;

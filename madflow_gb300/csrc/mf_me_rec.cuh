@@ -125,23 +125,15 @@ MF_D void prep_event(PrepRec<T, K>& r, const double (*p)[4], double mt, double w
     for (int b = 0; b < 2; ++b)
       r.G[q][b] = vxxxxx<T>(r.ev.pext[part], T(0), b ? T(1) : T(-1), part < 2 ? T(-1) : T(1), sqh);
   }
-  // The top and anti-top spinors, and from them the top-line bilinears of
-  // the four (top, anti-top) spin combinations M[q][mu] = WTB[q>>1]^T
-  // S(e_mu) WT[q&1] (an amplitude in which the full gluon current J meets
-  // the top line directly is J . M, S being linear in J), are formed in FP64
-  // and stored in T.  The small spinor components sqrt(E - |p|) of a boosted
-  // top lose their digits to cancellation in FP32, and where a top runs
-  // along a beam gluon the sum over diagrams amplifies that error about
-  // 1e5-fold (|M|^2 off by up to 4e-2 in FP32 spinors, 1e-6 with these).
-  W4<double> wt64[2], wtb64[2];
   for (int b = 0; b < 2; ++b) {
-    wt64[b] = oxxxxx<double>(p[2], mt, b ? 1.0 : -1.0, 1.0);
-    wtb64[b] = ixxxxx<double>(p[3], mt, b ? 1.0 : -1.0, -1.0);
-    r.WT[b] = w4cast<T>(wt64[b]);
-    r.WTB[b] = w4cast<T>(wtb64[b]);
+    r.WT[b] = oxxxxx<T>(r.ev.pext[2], r.ev.mt, b ? T(1) : T(-1), T(1));
+    r.WTB[b] = ixxxxx<T>(r.ev.pext[3], r.ev.mt, b ? T(1) : T(-1), T(-1));
   }
+  // the top-line bilinears of the four (top, anti-top) spin combinations,
+  // M[q][mu] = WTB[q>>1]^T S(e_mu) WT[q&1]: an amplitude in which the full
+  // gluon current J meets the top line directly is J . M (S is linear in J)
   for (int q = 0; q < 4; ++q)
-    for (int mu = 0; mu < 4; ++mu) r.ev.M[q][mu] = ccast<T>(dot4(unit_row(wtb64[q >> 1], mu), wt64[q & 1]));
+    for (int mu = 0; mu < 4; ++mu) r.ev.M[q][mu] = dot4(unit_row(r.WTB[q >> 1], mu), r.WT[q & 1]);
   r.scale = (c11.re * c11.re + c11.im * c11.im) / (R::COLOUR_DEN * R::DENOMINATOR);
 }
 

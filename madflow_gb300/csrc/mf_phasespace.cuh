@@ -64,8 +64,7 @@ MF_HD double rambo_w0(int n, double pi) {
 // FP64: p [n][4] from q; returns the log-weight before the massive
 // correction (w0 = rambo_w0(n, pi)).
 // FAST (the mixed-precision path): one reciprocal of the mass instead of
-// five divisions and the log of sqrts in FP32 (the log-weight is used in
-// FP32 there).
+// five divisions.
 template <bool FAST = false>
 MF_HD double rambo_conformal(const double (*q)[4], int n, double sqrts, double w0, double (*p)[4]) {
   double sum[4] = {0, 0, 0, 0};
@@ -91,10 +90,7 @@ MF_HD double rambo_conformal(const double (*q)[4], int n, double sqrts, double w
     p[i][3] = (q[i][3] + b[3] * tmp) * xs;
     p[i][0] = (q[i][0] * gamma + bq) * xs;
   }
-  if constexpr (FAST)
-    return w0 + (double)((float)(2 * n - 4) * logf((float)sqrts));
-  else
-    return w0 + (double)(2 * n - 4) * log(sqrts);
+  return w0 + (double)(2 * n - 4) * log(sqrts);
 }
 
 // rambo without the massive correction (FP64): p [n][4]; returns the
@@ -187,8 +183,9 @@ MF_HD int newton_conv_iter_xs(int n, const double* masses, const double (*p)[4],
 // iterations (iters <= 0: iterate this event to its own convergence) from
 // x_start (< 0: the rule's starting value sqrt(1 - (sum m / sqrts)^2)).
 // Rescales p in place and returns the final log-weight.
-// The weight factors run in W (the momenta and the Newton solve stay FP64).
-// With W = float (the mixed-precision path) the Newton steps are FAST ones.
+// The weight products run in W (the momenta, the Newton solve and the logs
+// stay FP64).  With W = float (the mixed-precision path) the Newton steps are
+// FAST ones.
 template <class W = double>
 MF_HD double rambo_massive(int n, const double* masses, double (*p)[4], double sqrts, double logw, double acc,
                            int iters, double x_start = -1.0) {
@@ -220,8 +217,9 @@ MF_HD double rambo_massive(int n, const double* masses, double (*p)[4], double s
     p[i][2] *= xf;
     p[i][3] *= xf;
   }
-  const W a = (W)(2 * n - 3) * ps_log((W)xf), b = ps_log(wt2 / wt3 * (W)sqrts);
-  return logw + (double)a + (double)b;
+  // the logs in FP64: the log-weight is exponentiated in FP64
+  const double a = (double)(2 * n - 3) * log(xf), b = log((double)(wt2 / wt3) * sqrts);
+  return logw + a + b;
 }
 
 // _get_x1x2 (phasespace.py:215-233)
@@ -277,7 +275,6 @@ template <class P> MF_HD bool pass_gluon_cuts(const P (*plab)[4], int npart, P p
 // bicubic convolution (Keys 1981, a = -1/2) with clamped edge nodes.
 struct PdfTable {
   const double* tab;  // [nq][nx]
-  const float* tabf;  // the same table rounded to FP32
   int nx, nq;
   double lx0, dlx, lq0, dlq;
 };
@@ -287,28 +284,26 @@ template <class P> MF_HD P keys_w(P t) {
   if (t < P(2)) return ((P(-0.5) * t + P(2.5)) * t - P(4)) * t + P(2);
   return P(0);
 }
-template <class P> MF_HD const P* pdf_tab(const PdfTable& T);
-template <> MF_HD const double* pdf_tab<double>(const PdfTable& T) { return T.tab; }
-template <> MF_HD const float* pdf_tab<float>(const PdfTable& T) { return T.tabf; }
 // table coordinate of log Q^2 (the same for every event of a batch)
 MF_HD double pdf_qcoord(const PdfTable& T, double q2) { return (log(q2) - T.lq0) / T.dlq; }
-// x g(x, Q^2) with v = pdf_qcoord(T, q2)
-template <class P> MF_HD P pdf_xfx_v(const PdfTable& T, P x, P v) {
-  const P* tab = pdf_tab<P>(T);
-  P u = (ps_log(x) - (P)T.lx0) / (P)T.dlx;
-  int iu = (int)ps_floor(u), iv = (int)ps_floor(v);
-  P fu = u - iu, fv = v - iv;
-  P wu[4];
-  for (int b = -1; b <= 2; ++b) wu[b + 1] = keys_w<P>(fu - b);
-  P s = P(0);
+// x g(x, Q^2) with v = pdf_qcoord(T, q2), FP64 (the indices are clamped to
+// the table, so any x, NaN included, reads inside it)
+MF_HD double pdf_xfx_v(const PdfTable& T, double x, double v) {
+  const double* tab = T.tab;
+  double u = (log(x) - T.lx0) / T.dlx;
+  int iu = (int)floor(u), iv = (int)floor(v);
+  double fu = u - iu, fv = v - iv;
+  double wu[4];
+  for (int b = -1; b <= 2; ++b) wu[b + 1] = keys_w<double>(fu - b);
+  double s = 0.0;
   for (int a = -1; a <= 2; ++a) {
     int qi = min(max(iv + a, 0), T.nq - 1);
-    P wv = keys_w<P>(fv - a);
+    double wv = keys_w<double>(fv - a);
     for (int b = -1; b <= 2; ++b) {
       int xi = min(max(iu + b, 0), T.nx - 1);
       s += wv * wu[b + 1] * tab[qi * T.nx + xi];
     }
   }
-  return s > P(0) ? s : P(0);  // the cubic can overshoot below zero next to x = 1
+  return s > 0.0 ? s : 0.0;  // the cubic can overshoot below zero next to x = 1
 }
-MF_HD double pdf_xfx(const PdfTable& T, double x, double q2) { return pdf_xfx_v<double>(T, x, pdf_qcoord(T, q2)); }
+MF_HD double pdf_xfx(const PdfTable& T, double x, double q2) { return pdf_xfx_v(T, x, pdf_qcoord(T, q2)); }

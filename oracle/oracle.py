@@ -15,30 +15,35 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libmf_oracle.so")
+# the same source at -O3 with fused multiply-adds: the timed CPU baseline
+FAST_LIB_PATH = os.path.join(HERE, "_build", "libmf_oracle_fast.so")
+FAST_FLAGS = "-O3 -ffp-contract=fast -fno-math-errno -fopenmp"
 
-_lib = None
+_libs = {}
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 
 
 def build(force=False):
-    """Compile the oracle with the committed Makefile (a few seconds)."""
-    if force or not os.path.exists(LIB_PATH) or _stale():
+    """Compile the oracle (parity build and timing build) with the committed
+    Makefile (a few seconds)."""
+    if force or any(not os.path.exists(p) or _stale(p) for p in (LIB_PATH, FAST_LIB_PATH)):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
 
-def _stale():
-    so = os.path.getmtime(LIB_PATH)
-    return any(os.path.getmtime(os.path.join(HERE, f)) > so for f in ("mf_oracle.cpp", "mf_oracle.hpp"))
+def _stale(path):
+    so = os.path.getmtime(path)
+    return any(os.path.getmtime(os.path.join(HERE, f)) > so for f in ("mf_oracle.cpp", "mf_oracle.hpp", "Makefile"))
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def lib(fast=False):
+    """The parity build, or with fast=True the timing build (-O3, fused
+    multiply-adds; results agree with the parity build to rounding)."""
+    if fast not in _libs:
         build()
-        _lib = ctypes.CDLL(LIB_PATH)
+        _lib = ctypes.CDLL(FAST_LIB_PATH if fast else LIB_PATH)
         _lib.orc_ttng_create.restype = ctypes.c_void_p
         _lib.orc_ttng_create.argtypes = [ctypes.c_int, _dp]
         for name in ("orc_ttng_destroy",):
@@ -52,7 +57,8 @@ def lib():
         _lib.orc_ramboflow.restype = ctypes.c_int
         _lib.orc_pass_cuts.restype = ctypes.c_int
         _lib.orc_num_threads.restype = ctypes.c_int
-    return _lib
+        _libs[fast] = _lib
+    return _libs[fast]
 
 
 def _p(a):
@@ -190,18 +196,19 @@ C4 = -1.0
 class TTNG:
     """tt~ + k gluons (k = total number of gluons, 2..5) in the oracle."""
 
-    def __init__(self, k, colour=None):
-        self.k = k
+    def __init__(self, k, colour=None, fast=False):
+        self.k, self.fast = k, fast
+        L = lib(fast)
         c = None if colour is None else _c64(colour)
-        self.h = lib().orc_ttng_create(ctypes.c_int(k), _p(c))
+        self.h = L.orc_ttng_create(ctypes.c_int(k), _p(c))
         info = (ctypes.c_int * 6)()
-        lib().orc_ttng_info(ctypes.c_void_p(self.h), info)
+        L.orc_ttng_info(ctypes.c_void_p(self.h), info)
         self.nperm, self.njnode, self.nonode, self.ncomb, self.npart = info[1], info[2], info[3], info[4], info[5]
-        self.denominator = lib().orc_ttng_denominator(ctypes.c_void_p(self.h))
+        self.denominator = L.orc_ttng_denominator(ctypes.c_void_p(self.h))
 
     def __del__(self):
         try:
-            lib().orc_ttng_destroy(ctypes.c_void_p(self.h))
+            lib(self.fast).orc_ttng_destroy(ctypes.c_void_p(self.h))
         except Exception:
             pass
 
@@ -326,14 +333,17 @@ def pass_cuts(plab, ptmin, etamax, drmin):
                                     ctypes.c_double(etamax), ctypes.c_double(drmin)))
 
 
-def integrand(cfg, x, plan=None):
-    """cfg: [kind, k, sqrts, mt, wt, alphas, ptmin, etamax, drmin, newton_rule]"""
+def integrand(cfg, x, plan=None, fast=False):
+    """cfg: [kind, k, sqrts, mt, wt, alphas, ptmin, etamax, drmin, newton_rule].
+    fast: the timing build (plan, if given, must come from the same build)."""
+    if plan is not None:
+        fast = plan.fast
     x = _c64(x)
     f = np.empty(x.shape[0])
-    lib().orc_integrand(_p(_c64(cfg)), ctypes.c_void_p(plan.h if plan is not None else None), _p(x),
-                        ctypes.c_int64(x.shape[0]), _p(f))
+    lib(fast).orc_integrand(_p(_c64(cfg)), ctypes.c_void_p(plan.h if plan is not None else None), _p(x),
+                            ctypes.c_int64(x.shape[0]), _p(f))
     return f
 
 
-def num_threads():
-    return lib().orc_num_threads()
+def num_threads(fast=False):
+    return lib(fast).orc_num_threads()
