@@ -88,6 +88,22 @@ def test_wavefunctions_golden(cuda, golden):
                 assert scaled_err(_np(wf.vxxxxx(pw, mass, nhel, nsv)), golden[f"wf_vx_{tag}"]) < 1e-15, tag
 
 
+def test_sxxxxx(cuda, golden):
+    """sxxxxx (wavefunctions_flow.py:34-51) cannot run in the reference
+    (tf.expand_dims on a rank-0 tensor), so there is no golden vector: the
+    evident intent is the 3-slot scalar wavefunction [p0, p3] nss, [p1, p2]
+    nss, 1."""
+    from madflow_gb300 import wavefunctions as wf
+
+    pw = golden["wf_p"]
+    for nss in (-1.0, 1.0):
+        out = _np(wf.sxxxxx(pw, nss))
+        assert out.shape == (3, pw.shape[0])
+        np.testing.assert_array_equal(out[0], (pw[:, 0] + 1j * pw[:, 3]) * nss)
+        np.testing.assert_array_equal(out[1], (pw[:, 1] + 1j * pw[:, 2]) * nss)
+        np.testing.assert_array_equal(out[2], np.ones(pw.shape[0], dtype=complex))
+
+
 def test_aloha_golden(cuda, golden):
     from madflow_gb300 import aloha
 
