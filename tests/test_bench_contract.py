@@ -25,3 +25,24 @@ def test_reference_arm_json_line():
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert "workload" in d["config"]
+
+
+def test_gpus_flag_launches_ranks():
+    """--gpus 2 without a torchrun environment starts two ranks itself
+    (torch.distributed.run on 127.0.0.1); the reference arm then prints one
+    line from rank 0 with n_gpus = 2 and the other rank exits without work."""
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1",
+                        "--warmup", "1", "--ref-events", "1000"], capture_output=True, text=True, cwd=ROOT,
+                       timeout=600, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip().startswith("{")]
+    assert len(lines) == 1
+    assert json.loads(lines[0])["n_gpus"] == 2
+
+
+def test_gpus_flag_must_match_world_size():
+    env = dict(os.environ, WORLD_SIZE="3", RANK="0", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1"],
+                       capture_output=True, text=True, cwd=ROOT, timeout=600, env=env)
+    assert r.returncode != 0 and "WORLD_SIZE" in r.stderr
