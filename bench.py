@@ -540,6 +540,15 @@ def _flow(args, integ, layers, bins, bf16):
                            bf16=bf16, tf32=not bf16)
 
 
+def _flow_kernels(flow):
+    if flow.bf16:
+        return "BF16 GEMMs with FP32 accumulation (torch autocast, cuBLAS) and the hand-written transform kernels"
+    train = "training in the hand-written FP32 layer kernels" if flow.native else "training through torch/cuBLAS"
+    sample = ("sampling in one tcgen05 TF32 kernel per layer" if flow.fused else
+              "sampling in the hand-written FP32 layer kernels" if flow.native else "sampling through torch/cuBLAS")
+    return f"{sample}, {train}"
+
+
 def _flow_leg(args, integ, target, layers, bins, bf16, vegas_iters, vegas_events, batch, train_batches,
               max_batches):
     """A few VEGAS iterations adapt a grid, then the flow refines the proposal
@@ -565,16 +574,19 @@ def _flow_leg(args, integ, target, layers, bins, bf16, vegas_iters, vegas_events
     v.compile(integ)
     vr, ve = v.run_integration(vegas_iters)
     flow = _flow(args, integ, layers, bins, bf16)
+    t_flow = time.perf_counter()
     res, err, info = run(flow, v.grid, (1.0 / ve ** 2, vr / ve ** 2), target, max_batches, train_batches)
     torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    return {"seconds": dt, "vegas_iterations": vegas_iters, "vegas_events_per_iteration": vegas_events,
+    t1 = time.perf_counter()
+    dt = t1 - t0
+    return {"seconds": dt, "vegas_seconds": t_flow - t0, "flow_seconds": t1 - t_flow,
+            "vegas_iterations": vegas_iters, "vegas_events_per_iteration": vegas_events,
             "flow_batches": info["batches"], "trained_batches": info["trained"], "events_per_batch": batch,
             "events": info["batches"] * batch + vegas_iters * vegas_events,
             "result_pb": res, "error_pb": err, "rel_error": err / abs(res) if res else None,
             "reached": bool(res and err / abs(res) <= target),
             "flow": f"{layers} piecewise-quadratic coupling layers, {bins} bins, MLP 2x{args.flow_hidden} "
-                    f"({'BF16 GEMMs with FP32 accumulation (cuBLAS)' if bf16 else 'TF32: sampling in one tcgen05 kernel per layer, training through cuBLAS'}), "
+                    f"({_flow_kernels(flow)}), "
                     f"lr {args.flow_lr}, on a frozen VEGAS grid, trained on {args.flow_resample} events per batch "
                     "resampled with probability w^2 (one Adam step, a captured CUDA graph)",
             "last_std_over_mean": info["last_rel_std"]}, flow, v.grid
@@ -653,10 +665,13 @@ def flow_vs_vegas(args, cfg, target=1e-3):
     vg = _vegas_to_target(cfg, _lib.MF_PREC_MIXED, n, args.seed + 1, args.max_iter * 4, target)
     out = {"target_rel_error": target, "vegas": _public(vg)}
     out["vegas"]["unweighting_efficiency"] = _unweighting_efficiency(_sample_vegas(integ, vg["vegas"].grid, n, 77))
-    fl, flow, grid = _flow_leg(args, integ, target, 6, 16, True, args.flow_vegas_iters, args.flow_vegas_events,
-                               n, 20, args.max_iter * 4)
-    fl["unweighting_efficiency"] = _unweighting_efficiency(_sample_flow(integ, flow, grid, n, 78))
-    out["flow"] = fl
+    # the configuration's flow in the hand-written FP32 kernels, and with its
+    # BF16 GEMMs through cuBLAS
+    for key, bf16 in (("flow", False), ("flow_bf16_cublas", True)):
+        fl, flow, grid = _flow_leg(args, integ, target, 6, 16, bf16, args.flow_vegas_iters, args.flow_vegas_events,
+                                   n, 20, args.max_iter * 4)
+        fl["unweighting_efficiency"] = _unweighting_efficiency(_sample_flow(integ, flow, grid, n, 78))
+        out[key] = fl
     return out
 
 
@@ -685,7 +700,7 @@ def flow_vs_vegas_budget(args, cfg, budget_iters=10):
                      "rel_error": err / abs(res) if res else None,
                      "unweighting_efficiency": _unweighting_efficiency(_sample_vegas(integ, v.grid, n, 77))}}
     vi = 3
-    fl, flow, grid = _flow_leg(args, integ, 0.0, 6, 16, True, vi, n, n, budget_iters - vi, budget_iters - vi)
+    fl, flow, grid = _flow_leg(args, integ, 0.0, 6, 16, False, vi, n, n, budget_iters - vi, budget_iters - vi)
     fl["unweighting_efficiency"] = _unweighting_efficiency(_sample_flow(integ, flow, grid, n, 78))
     out["flow"] = fl
     return out

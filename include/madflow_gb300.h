@@ -321,6 +321,37 @@ int mf_flow_inv_layer_tc(float* z, int64_t n, int dim, const int* ia, int na, co
                          const float* W1, const float* b1, const float* W2, const float* b2, const float* W3,
                          const float* b3, float* logq, int* err, void* stream);
 
+/* Whole coupling layers in hand-written FP32 kernels (no counterpart in the
+ * reference): the conditioner MLP na -> 64 -> 64 -> nb (2K+1) with ReLU (the
+ * same weights and layouts as mf_flow_inv_layer_tc), then the transform of
+ * the dimensions ib.  z_in, z_out [N][dim] float32 (may be the same array);
+ * ia [na], ib [nb] device int32 dimension indices (clamped to [0, dim));
+ * 1 <= na, nb <= 16, na + nb <= dim, K in {4, 8, 16}, nb (2K+1) <= 320;
+ * logq [N] += the sum over ib of log pdf.
+ * mf_flow_layer_density: y = CDF(x) on ib (the density direction of
+ * training, NormalizingFlow.log_prob); mf_flow_layer_sample: x = CDF^-1(u)
+ * (sampling, for shapes mf_flow_inv_layer_tc does not take). */
+int mf_flow_layer_density(const float* z_in, float* z_out, int64_t n, int dim, const int* ia, int na, const int* ib,
+                          int nb, int K, const float* W1, const float* b1, const float* W2, const float* b2,
+                          const float* W3, const float* b3, float* logq, void* stream);
+int mf_flow_layer_sample(const float* z_in, float* z_out, int64_t n, int dim, const int* ia, int na, const int* ib,
+                         int nb, int K, const float* W1, const float* b1, const float* W2, const float* b2,
+                         const float* W3, const float* b3, float* logq, void* stream);
+/* Gradient of mf_flow_layer_density: z_in [N][dim] the layer's input,
+ * g_out [N][dim] = dL/d(output), glogdet [N] = dL/d(the layer's log pdf
+ * sum) -> g_in [N][dim] = dL/d(input) (not aliasing z_in or g_out) and the
+ * weight gradients gW1 [64][na], gb1 [64], gW2 [64][64], gb2 [64],
+ * gW3 [nb (2K+1)][64], gb3 [nb (2K+1)] (overwritten, not accumulated).
+ * workspace: device scratch of at least mf_flow_layer_grad_workspace bytes
+ * (the partial sums of up to one block per SM, summed in a fixed order, so
+ * the gradient is reproducible). */
+int mf_flow_layer_grad_workspace(int na, int nb, int K, int64_t* bytes);
+int mf_flow_layer_grad(const float* z_in, const float* g_out, float* g_in, int64_t n, int dim, const int* ia, int na,
+                       const int* ib, int nb, int K, const float* W1, const float* b1, const float* W2,
+                       const float* b2, const float* W3, const float* b3, const float* glogdet, float* gW1, float* gb1,
+                       float* gW2, float* gb2, float* gW3, float* gb3, float* workspace, int64_t workspace_bytes,
+                       void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -104,6 +104,13 @@ _SIGS = {
     "mf_pq_forward": (c_int, [c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
     "mf_pq_inverse": (c_int, [c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
     "mf_pq_backward": (c_int, [c_dp, c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
+    "mf_flow_layer_density": (c_int, [c_dp, c_dp, c_int64, c_int, c_dp, c_int, c_dp, c_int, c_int] + [c_dp] * 7
+                              + [c_void_p]),
+    "mf_flow_layer_sample": (c_int, [c_dp, c_dp, c_int64, c_int, c_dp, c_int, c_dp, c_int, c_int] + [c_dp] * 7
+                             + [c_void_p]),
+    "mf_flow_layer_grad_workspace": (c_int, [c_int, c_int, c_int, ctypes.POINTER(c_int64)]),
+    "mf_flow_layer_grad": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_dp, c_int, c_dp, c_int, c_int] + [c_dp] * 13
+                           + [c_dp, c_int64, c_void_p]),
     "mf_flow_inv_layer_tc": (c_int, [c_dp, c_int64, c_int, c_dp, c_int, c_dp, c_int, c_int, c_dp, c_dp, c_dp, c_dp,
                                      c_dp, c_dp, c_dp, c_dp, c_void_p]),
 }

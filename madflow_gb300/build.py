@@ -17,7 +17,7 @@ LIB_NAME = "libmadflow_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-SOURCES = ["mf_core.cu", "mf_proc_k2.cu", "mf_proc_k3.cu", "mf_proc_k4.cu", "mf_proc_k5.cu", "mf_proc_multi.cu", "mf_flow.cu", "mf_flow_tc.cu"]
+SOURCES = ["mf_core.cu", "mf_proc_k2.cu", "mf_proc_k3.cu", "mf_proc_k4.cu", "mf_proc_k5.cu", "mf_proc_multi.cu", "mf_flow.cu", "mf_flow_tc.cu", "mf_flow_train.cu"]
 
 
 def nvcc():

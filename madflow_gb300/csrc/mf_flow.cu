@@ -12,44 +12,12 @@
 #include <cuda_runtime.h>
 
 #include "../../include/madflow_gb300.h"
+#include "mf_pq.cuh"
 
 namespace {
-constexpr int KMAX = 64;
-
-struct Bins {
-  float W[KMAX], V[KMAX + 1], E[KMAX + 1], C[KMAX + 1];  // widths, heights, edges, CDF at edges
-};
-
-__device__ __forceinline__ void make_bins(const float* __restrict__ p, int K, Bins& b) {
-  float m = p[0];
-  for (int k = 1; k < K; ++k) m = fmaxf(m, p[k]);
-  float s = 0.f;
-  for (int k = 0; k < K; ++k) {
-    b.W[k] = __expf(p[k] - m);
-    s += b.W[k];
-  }
-  float inv = 1.f / s;
-  for (int k = 0; k < K; ++k) b.W[k] *= inv;
-  float mv = p[K];
-  for (int k = 1; k <= K; ++k) mv = fmaxf(mv, p[K + k]);
-  for (int k = 0; k <= K; ++k) b.V[k] = __expf(p[K + k] - mv);
-  float norm = 0.f;
-  for (int k = 0; k < K; ++k) norm += 0.5f * (b.V[k] + b.V[k + 1]) * b.W[k];
-  float in = 1.f / norm;
-  for (int k = 0; k <= K; ++k) b.V[k] *= in;
-  b.E[0] = 0.f;
-  b.C[0] = 0.f;
-  for (int k = 0; k < K; ++k) {
-    b.E[k + 1] = b.E[k] + b.W[k];
-    b.C[k + 1] = b.C[k] + 0.5f * (b.V[k] + b.V[k + 1]) * b.W[k];
-  }
-}
-
-__device__ __forceinline__ int find_bin(const float* edges, int K, float x) {
-  int b = 0;
-  for (int k = 1; k < K; ++k) b += (x >= edges[k]) ? 1 : 0;
-  return b;
-}
+using mfpq::Bins;
+using mfpq::KMAX;
+using mfpq::make_bins;
 
 // y = CDF(x), logdet = sum log pdf(x)
 __global__ void pq_forward_kernel(const float* __restrict__ x, const float* __restrict__ params, int64_t N, int nb,
@@ -60,12 +28,8 @@ __global__ void pq_forward_kernel(const float* __restrict__ x, const float* __re
   float ld = 0.f;
   for (int d = 0; d < nb; ++d) {
     make_bins(params + ((int64_t)e * nb + d) * (2 * K + 1), K, b);
-    float xv = fminf(fmaxf(x[e * nb + d], 0.f), 1.f);
-    int k = find_bin(b.E, K, xv);
-    float t = xv - b.E[k];
-    float D = b.V[k + 1] - b.V[k];
-    float pdf = b.V[k] + t / b.W[k] * D;
-    y[e * nb + d] = fminf(b.C[k] + t * b.V[k] + 0.5f * t * t / b.W[k] * D, 1.f);
+    float pdf;
+    y[e * nb + d] = mfpq::pq_fwd1(b, K, x[e * nb + d], &pdf);
     ld += __logf(pdf);
   }
   logdet[e] = ld;
@@ -80,16 +44,9 @@ __global__ void pq_inverse_kernel(const float* __restrict__ u, const float* __re
   float ld = 0.f;
   for (int d = 0; d < nb; ++d) {
     make_bins(params + ((int64_t)e * nb + d) * (2 * K + 1), K, b);
-    float uv = fminf(fmaxf(u[e * nb + d], 0.f), 1.f);
-    int k = find_bin(b.C, K, uv);
-    float r = fmaxf(uv - b.C[k], 0.f);
-    float D = b.V[k + 1] - b.V[k];
-    float a = 0.5f * b.W[k] * D, bq = b.W[k] * b.V[k];
-    // alpha solving a alpha^2 + bq alpha = r, in the cancellation-free form
-    float alpha = 2.f * r / (bq + sqrtf(fmaxf(bq * bq + 4.f * a * r, 0.f)));
-    alpha = fminf(fmaxf(alpha, 0.f), 1.f);
-    x[e * nb + d] = fminf(b.E[k] + alpha * b.W[k], 1.f);
-    ld += __logf(b.V[k] + alpha * D);
+    float pdf;
+    x[e * nb + d] = mfpq::pq_inv1(b, K, u[e * nb + d], &pdf);
+    ld += __logf(pdf);
   }
   logdet[e] = ld;
 }
@@ -101,47 +58,10 @@ __global__ void pq_backward_kernel(const float* __restrict__ x, const float* __r
                                    int K, float* __restrict__ gx, float* __restrict__ gparams) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= N) return;
-  Bins b;
-  float gW[KMAX], gV[KMAX + 1];
   float gl = gld ? gld[e] : 0.f;
   for (int d = 0; d < nb; ++d) {
-    const float* p = params + ((int64_t)e * nb + d) * (2 * K + 1);
-    make_bins(p, K, b);
-    float xv = fminf(fmaxf(x[e * nb + d], 0.f), 1.f);
-    float g = gy ? gy[e * nb + d] : 0.f;
-    int k = find_bin(b.E, K, xv);
-    float t = xv - b.E[k];
-    float Wb = b.W[k];
-    float D = b.V[k + 1] - b.V[k];
-    float pdf = b.V[k] + t / Wb * D;
-    float glp = gl / pdf;  // dL/dpdf
-    gx[e * nb + d] = g * pdf + glp * D / Wb;
-    for (int j = 0; j < K; ++j) gW[j] = 0.f;
-    for (int j = 0; j <= K; ++j) gV[j] = 0.f;
-    // y = c_k + t V_k + t^2/(2 W_k) D ; pdf = V_k + t/W_k D ; t = x - e_k
-    for (int j = 0; j < k; ++j) {
-      gW[j] += g * (0.5f * (b.V[j] + b.V[j + 1]) - pdf) + glp * (-D / Wb);
-      gV[j] += g * 0.5f * b.W[j];
-      gV[j + 1] += g * 0.5f * b.W[j];
-    }
-    gW[k] += g * (-0.5f * t * t * D / (Wb * Wb)) + glp * (-t * D / (Wb * Wb));
-    gV[k] += g * (t - 0.5f * t * t / Wb) + glp * (1.f - t / Wb);
-    gV[k + 1] += g * (0.5f * t * t / Wb) + glp * (t / Wb);
-    // chain through V = exp(V~)/norm(W, V~) and W = softmax(W~)
-    float S = 0.f;
-    for (int j = 0; j <= K; ++j) S += gV[j] * b.V[j];
-    float geff[KMAX];
-    float sw = 0.f;
-    for (int j = 0; j < K; ++j) {
-      geff[j] = gW[j] - S * 0.5f * (b.V[j] + b.V[j + 1]);
-      sw += geff[j] * b.W[j];
-    }
-    float* gp = gparams + ((int64_t)e * nb + d) * (2 * K + 1);
-    for (int j = 0; j < K; ++j) gp[j] = b.W[j] * (geff[j] - sw);
-    for (int j = 0; j <= K; ++j) {
-      float wl = j > 0 ? b.W[j - 1] : 0.f, wr = j < K ? b.W[j] : 0.f;
-      gp[K + j] = b.V[j] * (gV[j] - S * 0.5f * (wl + wr));
-    }
+    const int64_t o = ((int64_t)e * nb + d) * (2 * K + 1);
+    gx[e * nb + d] = mfpq::pq_bwd1(params + o, K, x[e * nb + d], gy ? gy[e * nb + d] : 0.f, gl, gparams + o);
   }
 }
 

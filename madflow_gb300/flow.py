@@ -6,16 +6,27 @@ Architecture (Mueller et al., "Neural Importance Sampling", ACM TOG 38 (2019)
 of the dimensions with bins (K widths, K+1 vertex heights) predicted by an MLP
 of ``n_hidden`` hidden layers of ``hidden`` units from the other half.
 
-Compute split: the conditioner MLPs are plain GEMMs, run in BF16 with FP32
-accumulation (cuBLAS via torch autocast), weights kept in FP32; the coupling
-transform, its inverse (sampling), log-Jacobian and backward pass are the
-hand-written CUDA kernels of ``mf_flow.cu`` behind the C ABI.
+Compute split (two hidden layers of 64 units, 4, 8 or 16 bins, at most 16
+dimensions per half):
+  * training runs in hand-written FP32 kernels (``mf_flow_train.cu``): per
+    coupling layer, the MLP and the transform in the density direction, and
+    their gradient (the MLP backward as tiled GEMMs in shared memory, the
+    transform's backward per point and dimension, weight gradients summed in
+    a fixed order); Adam updates the weights;
+  * sampling runs one tcgen05 kernel per coupling layer (``mf_flow_tc.cu``:
+    the MLP as three TF32 GEMMs with tensor-memory accumulators, the inverse
+    transform in the epilogue) when the layer fits it (at most 256 MLP
+    outputs) and TF32 is chosen, else the hand-written FP32 layer kernel.
+Other shapes, and ``bf16=True``, run the conditioner through torch (cuBLAS,
+BF16 under autocast) with the hand-written transform kernels of
+``mf_flow.cu`` (forward, inverse, log-Jacobian, backward).
 
 Training minimises the variance of the weights f/q with the score-function
 gradient  d Var/d theta = -E_q[(f/q)^2 d log q/d theta]  on batches drawn from
 the flow itself; the integral estimate mean(f/q) stays unbiased for any
 trained state, and each integration iteration uses one frozen state.
 """
+import ctypes
 import math
 import time
 
@@ -83,15 +94,19 @@ def _masks(dim, n_layers, seed):
 
 
 class NormalizingFlow(torch.nn.Module):
-    def __init__(self, dim, n_layers=6, bins=16, hidden=64, n_hidden=2, seed=0, bf16=True, tf32=False, fused=None):
-        """bf16: conditioner GEMMs in BF16 (autocast); else FP32, with TF32
-        tensor-core GEMMs when tf32 is set.  Reduced-precision GEMMs leave
-        the estimates unbiased (the sampled log-density is the exact density
-        of the map as evaluated); they perturb the training gradients.
-        fused: sample with one tensor-core kernel per coupling layer
-        (mf_flow_inv_layer_tc: the MLP in TF32 and the inverse transform);
-        by default whenever tf32 is set and the shapes fit it (64 hidden
-        units, two hidden layers, 4, 8 or 16 bins)."""
+    def __init__(self, dim, n_layers=6, bins=16, hidden=64, n_hidden=2, seed=0, bf16=False, tf32=False, fused=None,
+                 native=None):
+        """native: train (and sample, where the tensor-core layer does not
+        apply) with the hand-written FP32 layer kernels; by default whenever
+        the shapes fit them (64 hidden units, two hidden layers, 4, 8 or 16
+        bins, at most 16 dimensions per half, nb (2K+1) <= 320) and bf16 is
+        not set.  bf16: conditioner GEMMs in BF16 through torch autocast
+        (cuBLAS) instead.  fused: sample with one tensor-core kernel per
+        coupling layer (mf_flow_inv_layer_tc: the MLP in TF32 and the inverse
+        transform); by default whenever tf32 is set and the shapes fit it
+        (also nb (2K+1) <= 256).  Reduced-precision GEMMs leave the estimates
+        unbiased (the sampled log-density is the exact density of the map as
+        evaluated); they perturb the training gradients."""
         super().__init__()
         self.dim, self.K, self.bf16, self.tf32 = dim, bins, bf16, tf32
         self.masks = _masks(dim, n_layers, seed)
@@ -118,6 +133,79 @@ class NormalizingFlow(torch.nn.Module):
             raise ValueError("the fused sampling kernel needs 64 hidden units, 2 hidden layers, 4/8/16 bins, "
                              "at most 16 dimensions per half")
         self.fused = bool(fits and (tf32 and not bf16) if fused is None else fused)
+        nfits = (hidden == 64 and n_hidden == 2 and bins in (4, 8, 16)
+                 and all(0 < len(ia) <= 16 and 0 < len(ib) <= 16 and len(ib) * (2 * bins + 1) <= 320
+                         for ib, ia in self._idx))
+        if native and not nfits:
+            raise ValueError("the native layer kernels need 64 hidden units, 2 hidden layers, 4/8/16 bins, "
+                             "at most 16 dimensions per half and nb (2K+1) <= 320")
+        self.native = bool(nfits and not bf16 if native is None else native)
+        if self.native:
+            ws = 0
+            for ib, ia in self._idx:
+                b = ctypes.c_int64()
+                _lib.call("mf_flow_layer_grad_workspace", len(ia), len(ib), bins, ctypes.byref(b))
+                ws = max(ws, b.value)
+            self._workspace = torch.empty(ws // 4 + 1, dtype=torch.float32, device=device())
+            for p in self.parameters():
+                p.grad = torch.zeros_like(p)
+
+    def _layer_ptrs(self, l):
+        """Device pointers of layer l's weights (W1, b1, W2, b2, W3, b3)."""
+        net = self.nets[l]
+        return [t.data_ptr() for t in (net[0].weight, net[0].bias, net[2].weight, net[2].bias, net[4].weight,
+                                       net[4].bias)]
+
+    def _layer_grad_ptrs(self, l):
+        net = self.nets[l]
+        ts = (net[0].weight, net[0].bias, net[2].weight, net[2].bias, net[4].weight, net[4].bias)
+        for t in ts:
+            if t.grad is None:  # after zero_grad(set_to_none=True)
+                t.grad = torch.zeros_like(t)
+        return [t.grad.data_ptr() for t in ts]
+
+    @torch.no_grad()
+    def native_backward(self, x, glogq):
+        """Gradient of L = sum_i glogq_i log q(x_i) with respect to every
+        weight, in the hand-written kernels: the density direction through
+        all layers (storing each layer's input), then the layers' gradients
+        in reverse.  Writes p.grad of every parameter (overwriting) and
+        returns log q(x) (float32)."""
+        n = x.shape[0]
+        z = x.float().contiguous()
+        logq = torch.zeros(n, dtype=torch.float32, device=z.device)
+        gl = glogq.float().contiguous()
+        inputs = []
+        for l in reversed(range(len(self.masks))):
+            ib, ia = self._idx32[l]
+            zn = torch.empty_like(z)
+            _lib.call("mf_flow_layer_density", z.data_ptr(), zn.data_ptr(), n, self.dim, ia.data_ptr(), len(ia),
+                      ib.data_ptr(), len(ib), self.K, *self._layer_ptrs(l), logq.data_ptr(), stream_ptr())
+            inputs.append(z)
+            z = zn
+        g = torch.zeros_like(z)
+        for j, l in enumerate(range(len(self.masks))):
+            ib, ia = self._idx32[l]
+            zin = inputs[len(inputs) - 1 - j]
+            gin = torch.empty_like(zin)
+            _lib.call("mf_flow_layer_grad", zin.data_ptr(), g.data_ptr(), gin.data_ptr(), n, self.dim, ia.data_ptr(),
+                      len(ia), ib.data_ptr(), len(ib), self.K, *self._layer_ptrs(l), gl.data_ptr(),
+                      *self._layer_grad_ptrs(l), self._workspace.data_ptr(), self._workspace.numel() * 4,
+                      stream_ptr())
+            g = gin
+        return logq
+
+    @torch.no_grad()
+    def native_log_prob(self, x):
+        """log q(x) through the hand-written density-direction kernels."""
+        n = x.shape[0]
+        z = x.float().contiguous().clone()
+        logq = torch.zeros(n, dtype=torch.float32, device=z.device)
+        for l in reversed(range(len(self.masks))):
+            ib, ia = self._idx32[l]
+            _lib.call("mf_flow_layer_density", z.data_ptr(), z.data_ptr(), n, self.dim, ia.data_ptr(), len(ia),
+                      ib.data_ptr(), len(ib), self.K, *self._layer_ptrs(l), logq.data_ptr(), stream_ptr())
+        return logq
 
     def _params(self, l, x_a):
         if self.bf16:
@@ -152,6 +240,12 @@ class NormalizingFlow(torch.nn.Module):
                           len(ib), self.K, *[t.data_ptr() for t in w], logq.data_ptr(), err.data_ptr(), stream_ptr())
             if int(err.item()) != 0:
                 raise RuntimeError(f"mf_flow_inv_layer_tc: device error flag {int(err.item())}")
+            return z.double(), logq.double()
+        if self.native:
+            for l in range(len(self.masks)):
+                ib, ia = self._idx32[l]
+                _lib.call("mf_flow_layer_sample", z.data_ptr(), z.data_ptr(), n, self.dim, ia.data_ptr(), len(ia),
+                          ib.data_ptr(), len(ib), self.K, *self._layer_ptrs(l), logq.data_ptr(), stream_ptr())
             return z.double(), logq.double()
         for l in range(len(self.masks)):
             ib, ia = self._idx[l]
@@ -200,6 +294,7 @@ class _GraphedStep:
     def __init__(self, flow, opt, n):
         self.flow, self.opt = flow, opt
         self.x = torch.full((n, flow.dim), 0.5, dtype=torch.float32, device=device())
+        self.gl = torch.full((n,), -1.0 / n, dtype=torch.float32, device=device())
         params = list(flow.parameters())
         saved = [p.detach().clone() for p in params]
         side = torch.cuda.Stream()
@@ -220,9 +315,13 @@ class _GraphedStep:
                     v.zero_()
 
     def _step(self):
-        self.opt.zero_grad(set_to_none=False)
-        loss = -self.flow.log_prob(self.x).mean()
-        _backward(self.flow, loss)
+        if self.flow.native:
+            # the loss -mean log q: dL/dlog q_i = -1/n; the kernels overwrite p.grad
+            self.flow.native_backward(self.x, self.gl)
+        else:
+            self.opt.zero_grad(set_to_none=False)
+            loss = -self.flow.log_prob(self.x).mean()
+            _backward(self.flow, loss)
         self.opt.step()
 
     def __call__(self, xs):
@@ -253,20 +352,29 @@ def _train_step(flow, opt, x, w, minibatch, resample=0, step=None):
             step(xs)
             return
         for s in range(0, resample, minibatch):
-            loss = -flow.log_prob(xs[s: s + minibatch]).mean()
-            opt.zero_grad(set_to_none=True)
-            _backward(flow, loss)
+            xm = xs[s: s + minibatch]
+            if flow.native:
+                flow.native_backward(xm, torch.full((xm.shape[0],), -1.0 / xm.shape[0], dtype=torch.float32,
+                                                    device=xm.device))
+            else:
+                loss = -flow.log_prob(xm).mean()
+                opt.zero_grad(set_to_none=True)
+                _backward(flow, loss)
             opt.step()
         return
     mean_w = w.mean()
     scale = (mean_w * mean_w).clamp_min(1e-300)
     n = x.shape[0]
     for s in range(0, n, minibatch):
-        lq = flow.log_prob(x[s: s + minibatch])
         wm = w[s: s + minibatch]
-        loss = -((wm * wm / scale).float() * lq).mean()
-        opt.zero_grad(set_to_none=True)
-        _backward(flow, loss)
+        coef = (wm * wm / scale).float()
+        if flow.native:
+            flow.native_backward(x[s: s + minibatch], -coef / wm.shape[0])
+        else:
+            lq = flow.log_prob(x[s: s + minibatch])
+            loss = -(coef * lq).mean()
+            opt.zero_grad(set_to_none=True)
+            _backward(flow, loss)
         opt.step()
 
 
