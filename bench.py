@@ -20,6 +20,9 @@ configurations are
       of 10^6) against plain VEGAS: time, events, unweighting efficiency
   c5  g g > t t~ g g g, c3 cuts, 10^6 points per iteration, mixed; flow
       against VEGAS on an equal event budget
+  pp  p p > t t~ at leading order: g g > t t~ and the light-quark channels
+      q q~ > t t~ (and mirror images) with synthetic quark densities, 10^7
+      points per iteration, FP64 and mixed, and the quark channels' share
 
 --gpus N without a torchrun environment starts N ranks itself (one per GPU,
 weak scaling: every rank integrates its own Philox stream and the iteration
@@ -83,6 +86,13 @@ CONFIGS = {
                process="gg_ttxggg (1240 diagrams, 120 colour flows, 128 helicities)"),
 }
 CONFIGS["c4"] = dict(CONFIGS["c3"], workload=CONFIGS["c3"]["workload"] + "; normalizing-flow proposal")
+# p p > t t~ at leading order (madflow's first example): g g and the light
+# q q~ / q~ q channels with synthetic quark densities beside the gluon
+CONFIGS["pp"] = dict(k=2, kind=1, sqrts=13000.0, cuts={}, events=10_000_000, iterations=10, precision="mixed",
+                     initial_states="pp",
+                     workload=f"p p > t t~ (g g + q q~ + q~ q, q = d u s c), sqrt(S)=13 TeV, {PDF} and synthetic "
+                              "quark densities, no cuts, 10-dim ramboflow, VEGAS 50 bins/dim",
+                     process="gg_ttx (3 diagrams) + uux_ttx (1 diagram, 4 flavours and their mirror images)")
 KERNELS = {2: "me_rec_multi_kernel<2,{T}>", 3: "me_rec_multi_kernel<3,{T}>", 4: "me_rec_kernel<4,{T},{C}>",
            5: "me_gws_kernel<5,{T},{C}>"}
 
@@ -190,7 +200,7 @@ def make_integrand(prec, cfg=None):
 
     cfg = cfg or CONFIGS["c3"]
     return FusedIntegrand(cfg["k"], kind=cfg["kind"], sqrts=cfg["sqrts"], mt=MT, wt=WT, alpha_s=ALPHA_S,
-                          precision=prec, **cfg["cuts"])
+                          precision=prec, initial_states=cfg.get("initial_states", "gg"), **cfg["cuts"])
 
 
 def _prec_code(name):
@@ -379,9 +389,15 @@ def extras(args, cfg, prec_name, out):
     if args.precision_points and cfg["k"] > 2:
         n = args.precision_points if k < 5 else min(args.precision_points, 100_000)
         out["mixed_vs_fp64"] = precision_study(cfg, n, args.seed + 2)
-    if name in ("c1", "c2", "c5") and args.integration:
+    if name in ("c1", "c2", "c5", "pp") and args.integration:
         out["integration"] = {p: integration(cfg, p, cfg["events"], cfg["iterations"], args.seed + 5)
-                              for p in (("fp64", "mixed") if name == "c2" else (prec_name,))}
+                              for p in (("fp64", "mixed") if name in ("c2", "pp") else (prec_name,))}
+        if name == "pp":
+            # the g g channel alone on the same points: the quark channels' share
+            gg = integration(dict(cfg, initial_states="gg"), "mixed", cfg["events"], cfg["iterations"],
+                             args.seed + 5)
+            out["integration"]["gg_only_mixed"] = gg
+            out["integration"]["qq_share"] = 1.0 - gg["result_pb"] / out["integration"]["mixed"]["result_pb"]
         if name == "c1":
             out["integration"]["oracle_replay"] = oracle_replay(cfg, cfg["events"], cfg["iterations"], args.seed + 5)
         if name == "c2":
@@ -736,7 +752,7 @@ def cpu_baseline(args, cfg, sample=None):
     x = rng.uniform(size=(n, ndim))
     c = cfg["cuts"]
     ocfg = [cfg["kind"], k, cfg["sqrts"], MT, WT, ALPHA_S, c.get("ptmin", 0.0), c.get("etamax", 0.0),
-            c.get("drmin", 0.0), 0]
+            c.get("drmin", 0.0), 0, 1 if cfg.get("initial_states") == "pp" else 0]
     oracle.integrand(ocfg, x[: min(256, n)], plan)  # warm-up
     t0 = time.perf_counter()
     f = oracle.integrand(ocfg, x, plan)

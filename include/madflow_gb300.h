@@ -119,6 +119,7 @@ int mf_VVV1P0_1(const double* V2, const double* V3, const double* coup, double M
  *           PDF luminosity f(x1) f(x2) / (x1 x2) at Q^2 = q2 (utilities.py:42-53),
  *           cuts on the outgoing gluons (pT > ptmin, |eta| < etamax,
  *           Delta R > drmin in the lab frame; <= 0 disables). */
+typedef enum { MF_INITIAL_GG = 0, MF_INITIAL_PP = 1 } mf_initial_states;
 typedef struct {
   int kind;
   double sqrts;
@@ -127,6 +128,14 @@ typedef struct {
   double ptmin, etamax, drmin;
   double q2;
   int newton_rule;
+  /* MF_INITIAL_GG: the g g process alone.  MF_INITIAL_PP (kind 1, two
+   * gluons, i.e. p p > t t~ at leading order): f = weight x [L_gg |M|^2(g g >
+   * t t~) + L_qq |M|^2(q q~ > t t~)], L_qq summed over the initial states
+   * (q, q~) and their mirror images (q~, q), q = d u s c, of the synthetic
+   * quark densities (mf_pdf_xfx_flavour), as madflow sums its processes
+   * (scripts/madflow_exec.py:444-458, utilities.py:25-39).  Other
+   * multiplicities with MF_INITIAL_PP: MF_ERR_UNSUPPORTED. */
+  int initial_states;
 } mf_integrand_config;
 
 /* Number of integration dimensions of a configuration (8 for kind 0,
@@ -168,7 +177,9 @@ int mf_smatrix_multi(mf_process* const* procs, int nproc, const double* const* p
  * events failing the cuts, as in mf_vegas_iteration) and ps_out
  * [N][nexternal][4] the lab-frame momenta (E, px, py, pz) madflow passes to
  * its writer (PhaseSpaceGenerator(com_output=False)); zero rows for events
- * failing the cuts.  The VEGAS event weight is f_out / N. */
+ * failing the cuts.  The VEGAS event weight is f_out / N.  One channel only (an
+ * event names its initial-state flavours): initial_states MF_INITIAL_GG, else
+ * MF_ERR_UNSUPPORTED. */
 int mf_vegas_events(const mf_process* proc, const mf_integrand_config* cfg, const double* grid, int nbins,
                     uint64_t seed, uint32_t stream_id, int iteration, int64_t n_events, double* f_out,
                     double* ps_out, void* stream);
@@ -281,6 +292,22 @@ int mf_philox_uniforms(uint64_t seed, uint32_t stream_id, uint32_t iteration, ui
  * int x g dx = 1/2) on a 100 (log x) x 50 (log Q^2) table, bicubic lookup:
  * x [N], out [N]. */
 int mf_pdf_xfx(const double* x, int64_t n, double q2, double* out, void* stream);
+/* The synthetic density of flavour pdg (21 gluon; 1..4 d u s c; -1..-4 their
+ * antiquarks), the same tables and lookup: x u_v = A x^0.5 (1-x)^3 (int u_v
+ * = 2), x d_v = A x^0.5 (1-x)^4 (int d_v = 1), sea x qbar = A x^-0.2 (1-x)^7
+ * with int x qbar = 0.03 (ubar, dbar), 0.015 (s = sbar), 0.005 (c = cbar),
+ * u = u_v + ubar, d = d_v + dbar.  The reference reads LHAPDF grids through
+ * pdfflow (scripts/madflow_exec.py:412-417); these stand in for them. */
+int mf_pdf_xfx_flavour(int pdg, const double* x, int64_t n, double q2, double* out, void* stream);
+
+/* q q~ > t t~ (the light-quark processes of p p > t t~; MadGraph's u u~ >
+ * t t~ module: smatrix(all_ps, mdl_MT, mdl_WT, GC_11),
+ * matrix_method_python.inc:80-104): ps [4][4][N] (q, q~, t, t~), couplings
+ * as mf_smatrix (GC_11 is used), out [N] |M|^2 averaged over the initial
+ * spins and colours.  precision MF_PREC_FP64 or MF_PREC_MIXED (FP32 spinors
+ * and bilinears).  No scratch, no handle. */
+int mf_smatrix_qq_ttx(int precision, const double* ps, int64_t n_events, double mdl_MT, double mdl_WT,
+                      const double* couplings, int64_t coupling_stride, double* out, void* stream);
 
 /* ---- normalizing-flow importance sampler ---------------------------------
  * No counterpart in the reference (an addition of this implementation, used as

@@ -22,6 +22,7 @@ MF_STAGES = 4
 MF_TUNE_VARIANTS = 8
 MF_PREC_FP64, MF_PREC_MIXED = 0, 1
 MF_NEWTON_BATCH, MF_NEWTON_PER_EVENT = 0, 1
+MF_INITIAL_GG, MF_INITIAL_PP = 0, 1
 
 
 class MadflowError(RuntimeError):
@@ -53,6 +54,7 @@ class IntegrandConfig(ctypes.Structure):
         ("drmin", c_double),
         ("q2", c_double),
         ("newton_rule", c_int),
+        ("initial_states", c_int),
     ]
 
 
@@ -101,6 +103,8 @@ _SIGS = {
     "mf_vegas_sample": (c_int, [c_dp, c_int, c_int, c_dp, c_int64, c_dp, c_dp, c_dp, c_void_p]),
     "mf_philox_uniforms": (c_int, [c_uint64, c_uint32, c_uint32, c_uint64, c_int64, c_int, c_dp, c_void_p]),
     "mf_pdf_xfx": (c_int, [c_dp, c_int64, c_double, c_dp, c_void_p]),
+    "mf_pdf_xfx_flavour": (c_int, [c_int, c_dp, c_int64, c_double, c_dp, c_void_p]),
+    "mf_smatrix_qq_ttx": (c_int, [c_int, c_dp, c_int64, c_double, c_double, c_dp, c_int64, c_dp, c_void_p]),
     "mf_pq_forward": (c_int, [c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
     "mf_pq_inverse": (c_int, [c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
     "mf_pq_backward": (c_int, [c_dp, c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),

@@ -52,27 +52,45 @@ int smem_attr_once(const void* fn, bool* done_per_dev) {
   return MF_OK;
 }
 
-// ---- synthetic PDF table, one copy per device ------------------------------
+// ---- synthetic PDF tables, one copy per device -----------------------------
+// The gluon of the configurations, x g = A x^-0.2 (1-x)^5 with int x g = 1/2,
+// and synthetic quarks for p p > t t~ (x f independent of Q):
+//   valence  x u_v = A x^0.5 (1-x)^3 (int u_v = 2), x d_v = A x^0.5 (1-x)^4
+//            (int d_v = 1);
+//   sea      x qbar = A x^-0.2 (1-x)^7 with int x qbar = 0.03 (ubar, dbar),
+//            0.015 (s = sbar), 0.005 (c = cbar);  u = u_v + ubar, d = d_v + dbar.
+// Tables [MF_PDF_NF][kNQ][kNX] in the flavour order of pdf_flavour_index.
 constexpr int kNX = 100, kNQ = 50;
 struct PdfHost {
   std::vector<double> tab;
   double lx0, dlx, lq0, dlq;
 };
+double beta_fn(double a, double b) { return std::exp(std::lgamma(a) + std::lgamma(b) - std::lgamma(a + b)); }
+double synth_xfx(int pdg, double x) {
+  if (x >= 1.0) return 0.0;
+  if (pdg == 21) return 0.5 / beta_fn(0.8, 6.0) * std::pow(x, -0.2) * std::pow(1.0 - x, 5.0);
+  const int a = pdg < 0 ? -pdg : pdg;
+  const double frac = a <= 2 ? 0.03 : (a == 3 ? 0.015 : 0.005);
+  double v = frac / beta_fn(0.8, 8.0) * std::pow(x, -0.2) * std::pow(1.0 - x, 7.0);
+  if (pdg == 2) v += 2.0 / beta_fn(0.5, 4.0) * std::pow(x, 0.5) * std::pow(1.0 - x, 3.0);
+  if (pdg == 1) v += 1.0 / beta_fn(0.5, 5.0) * std::pow(x, 0.5) * std::pow(1.0 - x, 4.0);
+  return v;
+}
 const PdfHost& pdf_host() {
   static PdfHost P = [] {
     PdfHost h;
-    double A = 0.5 / std::exp(std::lgamma(0.8) + std::lgamma(6.0) - std::lgamma(6.8));
     h.lx0 = std::log(1e-6);
     h.dlx = (0.0 - h.lx0) / (kNX - 1);
     h.lq0 = std::log(1.0);
     h.dlq = (std::log(1e10) - h.lq0) / (kNQ - 1);
-    h.tab.resize(kNX * kNQ);
-    for (int iq = 0; iq < kNQ; ++iq)
-      for (int ix = 0; ix < kNX; ++ix) {
-        double x = std::exp(h.lx0 + ix * h.dlx);
-        if (ix == kNX - 1) x = 1.0;
-        h.tab[iq * kNX + ix] = A * std::pow(x, -0.2) * std::pow(1.0 - x, 5.0);
-      }
+    h.tab.resize((size_t)MF_PDF_NF * kNX * kNQ);
+    for (int f = 0; f < MF_PDF_NF; ++f)
+      for (int iq = 0; iq < kNQ; ++iq)
+        for (int ix = 0; ix < kNX; ++ix) {
+          double x = std::exp(h.lx0 + ix * h.dlx);
+          if (ix == kNX - 1) x = 1.0;
+          h.tab[((size_t)f * kNQ + iq) * kNX + ix] = synth_xfx(pdf_flavour_pdg(f), x);
+        }
     return h;
   }();
   return P;
@@ -89,8 +107,9 @@ int pdf_device_table(PdfTable& T) {
     std::lock_guard<std::mutex> lk(g_pdf_mu);
     if (!g_pdf_dev[dev]) {
       double* d = nullptr;
-      st = cuda_status(cudaMalloc(&d, sizeof(double) * kNX * kNQ));
-      if (!st) st = cuda_status(cudaMemcpy(d, H.tab.data(), sizeof(double) * kNX * kNQ, cudaMemcpyHostToDevice));
+      const size_t bytes = sizeof(double) * H.tab.size();
+      st = cuda_status(cudaMalloc(&d, bytes));
+      if (!st) st = cuda_status(cudaMemcpy(d, H.tab.data(), bytes, cudaMemcpyHostToDevice));
       if (st) {
         cudaFree(d);
         return st;
@@ -444,6 +463,26 @@ __global__ void pdf_kernel(PdfTable P, const double* __restrict__ x, int64_t N, 
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x)
     out[e] = pdf_xfx(P, x[e], q2);
 }
+__global__ void pdf_flavour_kernel(PdfTable P, int f, const double* __restrict__ x, int64_t N, double q2,
+                                   double* __restrict__ out) {
+  const double v = pdf_qcoord(P, q2);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = pdf_xfx_fv(P, f, x[e], v);
+}
+
+// q q~ > t t~, one thread per event: ps [4][4][N] (q, q~, t, t~), couplings
+// [N or 1][3] complex (GC_11 used)
+__global__ void qq_ttx_kernel(int prec, const double* __restrict__ ps, int64_t N, double mt,
+                              const double* __restrict__ coup, int64_t cstride, double* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double p[4][4];
+    for (int i = 0; i < 4; ++i)
+      for (int c = 0; c < 4; ++c) p[i][c] = ps[((int64_t)i * 4 + c) * N + e];
+    const double* cp = coup + 6 * cstride * e;
+    const double g11sq = cp[2] * cp[2] + cp[3] * cp[3];
+    out[e] = prec == MF_PREC_FP64 ? uux_ttx_me<double>(p, mt, g11sq) : uux_ttx_me<float>(p, mt, g11sq);
+  }
+}
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -466,6 +505,8 @@ struct mf_process {
   double* d_state = nullptr; // [state words][cap] first-pass phase-space state
   double* d_pref = nullptr; // [cap]
   double* d_me = nullptr;   // [cap]
+  double* d_extra = nullptr;  // [extra_cap] weights of further channels (p p > t t~)
+  int64_t extra_cap = 0;
   unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
   int64_t event_cap = 0;
   int* d_err = nullptr;     // device error flags of the kernels (bit 0: a tensor-core wait ran out,
@@ -543,6 +584,7 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_bins) cudaFree(p->d_bins);
   if (p->d_err) cudaFree(p->d_err);
   if (p->d_nonfinite) cudaFree(p->d_nonfinite);
+  if (p->d_extra) cudaFree(p->d_extra);
   for (cudaEvent_t e : p->tev)
     if (e) cudaEventDestroy(e);
   delete p;
@@ -789,6 +831,9 @@ static int ensure_partials(mf_process* p, size_t n) {
 
 static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, IterArgs& A) {
   std::memset(&A, 0, sizeof(A));
+  if (c->initial_states != MF_INITIAL_GG && c->initial_states != MF_INITIAL_PP) return MF_ERR_ARG;
+  if (c->initial_states == MF_INITIAL_PP && (c->kind != 1 || p->k != 2)) return MF_ERR_UNSUPPORTED;
+  A.qq = c->initial_states == MF_INITIAL_PP;
   A.kind = c->kind;
   A.sqrts = c->sqrts;
   A.mt = c->mt;
@@ -926,6 +971,15 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   A.state = p->d_state;
   A.pref = p->d_pref;
   A.me = p->d_me;
+  if (A.qq && p->extra_cap < A.N) {
+    cudaFree(p->d_extra);
+    p->d_extra = nullptr;
+    p->extra_cap = 0;
+    st = cuda_status(cudaMalloc(&p->d_extra, sizeof(double) * (size_t)A.N));
+    if (st) return st;
+    p->extra_cap = A.N;
+  }
+  A.extra = A.qq ? p->d_extra : nullptr;
   A.bins = A.x_in ? nullptr : p->d_bins;
   int accum_grid = 8 * 152;
   {
@@ -975,7 +1029,8 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   static bool attr_done[64] = {false};
   st = smem_attr_once((const void*)accum_kernel, attr_done);
   if (st) return st;
-  accum_kernel<<<accum_grid, 256, shm, S(stream)>>>(A.pref, A.me, A.bins, A.N, A.ndim, A.nb, A.inv_n, f_out,
+  accum_kernel<<<accum_grid, 256, shm, S(stream)>>>(A.pref, A.me, A.qq ? A.extra : nullptr, A.bins, A.N, A.ndim,
+                                                     A.nb, A.inv_n, f_out,
                                                      results ? p->d_partials : nullptr, p->d_err, p->d_nonfinite);
   if (results)
     reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(p->d_partials, accum_grid, width, results);
@@ -1100,6 +1155,8 @@ int mf_vegas_events(const mf_process* pc, const mf_integrand_config* c, const do
   mf_process* p = const_cast<mf_process*>(pc);
   int ndim = 0;
   if (!p || !c || !grid || !f_out || !ps_out || N <= 0 || nb < 2 || nb > 255 || iteration < 0) return MF_ERR_ARG;
+  // an event record names its initial-state flavours: one channel only
+  if (c->initial_states != MF_INITIAL_GG) return MF_ERR_UNSUPPORTED;
   int st = mf_integrand_ndim(p, c, &ndim);
   if (st) return st;
   if (ndim > MF_MAX_DIM) return MF_ERR_CAPACITY;
@@ -1262,6 +1319,28 @@ int mf_philox_uniforms(uint64_t seed, uint32_t stream_id, uint32_t it, uint64_t 
   if (N < 0 || ndim <= 0 || (N > 0 && !u)) return MF_ERR_ARG;
   if (N == 0) return MF_OK;
   philox_kernel<<<blocks_for(N), 256, 0, S(stream)>>>(seed, stream_id, it, e0, N, ndim, u);
+  return last_launch();
+}
+
+int mf_pdf_xfx_flavour(int pdg, const double* x, int64_t N, double q2, double* out, void* stream) {
+  const int f = pdf_flavour_index(pdg);
+  if (f < 0 || N < 0 || (N > 0 && (!x || !out))) return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  PdfTable P;
+  int st = pdf_device_table(P);
+  if (st) return st;
+  pdf_flavour_kernel<<<blocks_for(N), 256, 0, S(stream)>>>(P, f, x, N, q2, out);
+  return last_launch();
+}
+
+int mf_smatrix_qq_ttx(int precision, const double* ps, int64_t N, double mt, double wt, const double* coup,
+                      int64_t cstride, double* out, void* stream) {
+  (void)wt;  // the s-channel gluon carries no width; kept for the exporter's parameter order
+  if ((precision != MF_PREC_FP64 && precision != MF_PREC_MIXED) || N < 0 || (N > 0 && (!ps || !coup || !out)) ||
+      (cstride != 0 && cstride != 1))
+    return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  qq_ttx_kernel<<<blocks_for(N, 128), 128, 0, S(stream)>>>(precision, ps, N, mt, coup, cstride, out);
   return last_launch();
 }
 

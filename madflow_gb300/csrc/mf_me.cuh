@@ -20,6 +20,7 @@
 // so that an iteration is bit-reproducible.
 #pragma once
 #include "mf_me_rec.cuh"
+#include "mf_qq.cuh"
 
 struct IterArgs {
   const double* div;  // VEGAS grid [ndim][nb+1]
@@ -42,6 +43,8 @@ struct IterArgs {
   const double* x_in;  // optional [ndim][N] points (integrand API): no Philox / VEGAS map, jac = 1
   float* u_out;        // optional [ndim][N] uniforms
   double* ps_out;      // optional [N][K+2][4] lab-frame momenta of the passing events (event output)
+  int qq;              // p p > t t~: add the light-quark channels q q~ and q~ q (K = 2 only)
+  double* extra;       // [N] with qq: jac x weight x quark luminosity x |M|^2(q q~ > t t~)
   // pipeline buffers (scratch)
   double* state;            // [4K+16][N] first-pass state (ps_state_words)
   int4* prep;              // [N] per-event records (PrepRec), passing events only
@@ -146,7 +149,7 @@ MF_DO void event_massless(const IterArgs& A, int npart, const P* x, double w0, d
 template <class P>
 MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (*p)[4], double logw, double shat,
                         double wgt, double x1, double x2, double v, double pw, double& wgt_lum,
-                        double x_start = -1.0) {
+                        double x_start = -1.0, double* wgt_ps = nullptr) {
   MfConsts KC = mf_consts(A.f32q != 0);
   int nout = npart - 2;
   double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
@@ -162,6 +165,7 @@ MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (
   wgt = wgt * wps;
   wgt = wgt * KC.gev2pb;
   wgt = wgt / (2.0 * shat);
+  if (wgt_ps) *wgt_ps = wgt;  // the weight before the luminosity
   bool ok = true;
   if (A.ptmin > 0.0 || A.etamax > 0.0 || A.drmin > 0.0) {
     P plab[MF_MAX_OUT + 2][4];
@@ -253,8 +257,21 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
     // batch rule: one step from the first pass's x_(niter-1) (the steps
     // before it are the ones the first pass took)
     const double xs = niter > 0 ? st[(int64_t)(4 * K + 6 + niter - 1) * N] : -1.0;
-    bool ok = event_finish<T>(A, NPART, niter > 0 ? 1 : niter, p, logw, shat, wgt, x1, x2, v, pw, wl, xs);
+    double wps = 0.0;
+    bool ok = event_finish<T>(A, NPART, niter > 0 ? 1 : niter, p, logw, shat, wgt, x1, x2, v, pw, wl, xs, &wps);
     A.pref[e] = ok ? jac * wl : 0.0;
+    if constexpr (K == 2) {
+      // the light-quark channels of p p > t t~, one thread per event (two
+      // orders of magnitude cheaper than the block-per-event gluon channel)
+      if (A.qq) {
+        double ex = 0.0;
+        if (ok) {
+          const double g11sq = A.gc11.re * A.gc11.re + A.gc11.im * A.gc11.im;
+          ex = jac * wps * pdf_qq_luminosity(A.pdf, x1, x2, v) * uux_ttx_me<T>(p, A.mt, g11sq);
+        }
+        A.extra[e] = ex;
+      }
+    }
     if (A.ps_out) {
       // madflow's all_ps (com_output=False): lab frame, FP64
       double* q = A.ps_out + (int64_t)e * NPART * 4;
@@ -278,11 +295,13 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
 // non-finite input point or matrix element) is replaced by 0.
 MF_DO double finite_weight(double f) { return isfinite(f) ? f : 0.0; }
 
-// w = pref * me * inv_n; block b owns a contiguous slice of events.  f_out
-// (optional) = pref * me.  partials [gridDim][2 + ndim*nb].  Non-finite
+// w = (pref * me + extra) * inv_n (extra optional: further channels of the
+// same events); block b owns a contiguous slice of events.  f_out
+// (optional) = pref * me + extra.  partials [gridDim][2 + ndim*nb].  Non-finite
 // weights are counted into *nonfinite (bit 1 of *err set) and enter the sums,
 // the histogram and f_out as 0.
 static __global__ void __launch_bounds__(256) accum_kernel(const double* __restrict__ pref, const double* __restrict__ me,
+                                                    const double* __restrict__ extra,
                                                     const unsigned char* __restrict__ bins, int64_t N, int ndim,
                                                     int nb, double inv_n, double* __restrict__ f_out,
                                                     double* __restrict__ partials, int* __restrict__ err,
@@ -297,7 +316,7 @@ static __global__ void __launch_bounds__(256) accum_kernel(const double* __restr
   double a = 0.0, b = 0.0;
   unsigned int bad = 0;
   for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-    const double f0 = pref[e] * me[e];
+    const double f0 = pref[e] * me[e] + (extra ? extra[e] : 0.0);
     const double f = finite_weight(f0);
     bad += f0 != f;
     if (f_out) f_out[e] = f;
@@ -326,7 +345,7 @@ static __global__ void __launch_bounds__(256) accum_kernel(const double* __restr
     for (int64_t c0 = e0; c0 < e1; c0 += blockDim.x) {
       const int64_t e = c0 + threadIdx.x;
       if (e < e1) {
-        const double w = finite_weight(pref[e] * me[e]) * inv_n;
+        const double w = finite_weight(pref[e] * me[e] + (extra ? extra[e] : 0.0)) * inv_n;
         w2[threadIdx.x] = w * w;
       }
       __syncthreads();

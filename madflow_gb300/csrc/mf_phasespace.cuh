@@ -274,7 +274,7 @@ template <class P> MF_HD bool pass_gluon_cuts(const P (*plab)[4], int npart, P p
 // Synthetic gluon PDF x g(x) read back from its (log x, log Q^2) table by
 // bicubic convolution (Keys 1981, a = -1/2) with clamped edge nodes.
 struct PdfTable {
-  const double* tab;  // [nq][nx]
+  const double* tab;  // [MF_PDF_NF][nq][nx], the gluon first
   int nx, nq;
   double lx0, dlx, lq0, dlq;
 };
@@ -284,12 +284,23 @@ template <class P> MF_HD P keys_w(P t) {
   if (t < P(2)) return ((P(-0.5) * t + P(2.5)) * t - P(4)) * t + P(2);
   return P(0);
 }
+// Flavours of the tables: 0 gluon, 1..4 d u s c, 5..8 their antiquarks.
+constexpr int MF_PDF_NF = 9;
+MF_HD int pdf_flavour_pdg(int f) { return f == 0 ? 21 : (f <= 4 ? f : 4 - f); }
+// table index of a PDG code (21, +-1..+-4), -1 for others
+MF_HD int pdf_flavour_index(int pdg) {
+  if (pdg == 21) return 0;
+  if (pdg >= 1 && pdg <= 4) return pdg;
+  if (pdg <= -1 && pdg >= -4) return 4 - pdg;
+  return -1;
+}
 // table coordinate of log Q^2 (the same for every event of a batch)
 MF_HD double pdf_qcoord(const PdfTable& T, double q2) { return (log(q2) - T.lq0) / T.dlq; }
-// x g(x, Q^2) with v = pdf_qcoord(T, q2), FP64 (the indices are clamped to
-// the table, so any x, NaN included, reads inside it)
-MF_HD double pdf_xfx_v(const PdfTable& T, double x, double v) {
-  const double* tab = T.tab;
+// x f(x, Q^2) of table flavour f (0 = gluon) with v = pdf_qcoord(T, q2),
+// FP64 (the indices are clamped to the table, so any x, NaN included, reads
+// inside it)
+MF_HD double pdf_xfx_fv(const PdfTable& T, int f, double x, double v) {
+  const double* tab = T.tab + (int64_t)f * T.nq * T.nx;
   double u = (log(x) - T.lx0) / T.dlx;
   int iu = (int)floor(u), iv = (int)floor(v);
   double fu = u - iu, fv = v - iv;
@@ -306,4 +317,15 @@ MF_HD double pdf_xfx_v(const PdfTable& T, double x, double v) {
   }
   return s > 0.0 ? s : 0.0;  // the cubic can overshoot below zero next to x = 1
 }
+// the gluon
+MF_HD double pdf_xfx_v(const PdfTable& T, double x, double v) { return pdf_xfx_fv(T, 0, x, v); }
 MF_HD double pdf_xfx(const PdfTable& T, double x, double q2) { return pdf_xfx_v(T, x, pdf_qcoord(T, q2)); }
+// Light-quark luminosity of q q~ > t t~ as madflow sums it: the initial
+// states (q, q~) and their mirror images (q~, q), q = d u s c, times 1/(x1 x2)
+// (scripts/madflow_exec.py:450-455, utilities.py:25-39)
+MF_HD double pdf_qq_luminosity(const PdfTable& T, double x1, double x2, double v) {
+  double s = 0.0;
+  for (int q = 1; q <= 4; ++q)
+    s += pdf_xfx_fv(T, q, x1, v) * pdf_xfx_fv(T, q + 4, x2, v) + pdf_xfx_fv(T, q + 4, x1, v) * pdf_xfx_fv(T, q, x2, v);
+  return s / x1 / x2;
+}

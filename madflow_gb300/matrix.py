@@ -170,6 +170,43 @@ class Matrix_1_gg_ttxggg(MatrixTTNG):
 PROCESSES = {2: Matrix_1_gg_ttx, 3: Matrix_1_gg_ttxg, 4: Matrix_1_gg_ttxgg, 5: Matrix_1_gg_ttxggg}
 
 
+class Matrix_1_uux_ttx:
+    """q q~ > t t~ (1 diagram, 2 colour flows, 16 helicities): the
+    light-quark processes of madflow's p p > t t~ run, one module for the
+    flavours d u s c as MadGraph groups them (initial states and their mirror
+    images).  smatrix(all_ps, mdl_MT, mdl_WT, GC_11) with all_ps (N, 4, 4)
+    ordered q, q~, t, t~ (C ABI mf_smatrix_qq_ttx)."""
+
+    process_string = "1_uux_ttx"
+    initial_states = [(2, -2), (4, -4), (1, -1), (3, -3)]
+    mirror_initial_states = True
+    nexternal = 4.0
+    ndiags = 1.0
+    ncomb = 16.0
+    denominator = 36.0
+
+    def __init__(self, precision=None):
+        self.precision = default_precision() if precision is None else precision
+        h = [[a, b, c, d] for a in (-1, 1) for b in (-1, 1) for c in (-1, 1) for d in (-1, 1)]
+        self.helicities = torch.tensor(h, dtype=DTYPE)
+
+    def __str__(self):
+        return self.process_string
+
+    def smatrix(self, all_ps, mdl_MT, mdl_WT, GC_11):
+        """|M|^2 averaged over the initial spins (4) and colours (9)."""
+        ps = to_device(all_ps)
+        if ps.dim() != 3 or ps.shape[1] != 4 or ps.shape[2] != 4:
+            raise ValueError(f"all_ps must have shape (N, 4, 4), got {tuple(ps.shape)}")
+        N = ps.shape[0]
+        soa = ps.permute(1, 2, 0).contiguous()
+        coup, stride = MatrixTTNG._couplings(self, N, None, GC_11, None)
+        out = torch.empty(N, dtype=DTYPE, device=device())
+        _lib.call("mf_smatrix_qq_ttx", int(self.precision), soa.data_ptr(), N, float(mdl_MT), float(mdl_WT),
+                  coup.data_ptr(), stride, out.data_ptr(), stream_ptr())
+        return out
+
+
 def smatrix_multi(batches, mdl_MT, mdl_WT, GC_10, GC_11, GC_12=None):
     """|M|^2 of several processes in one persistent launch (C ABI
     ``mf_smatrix_multi``): batches is a list of (matrix, all_ps) with distinct

@@ -45,13 +45,19 @@ def one_matrix_integration(matrix, model_params, sqrts=7e3, n_events=int(1e5), n
     return vegas_wrapper(cross_section, ndim, n_iter, n_events, seed=seed)
 
 
-def synthetic_pdf(x, q2):
-    """The synthetic gluon PDF x g(x) = A x^-0.2 (1-x)^5 (GPU table lookup)."""
+def synthetic_pdf(x, q2, pdg=21):
+    """x f(x) of the synthetic density of flavour pdg (GPU table lookup): the
+    gluon x g(x) = A x^-0.2 (1-x)^5 (pdg 21) or a light quark or antiquark
+    (pdg +-1..+-4, see mf_pdf_xfx_flavour)."""
     from .config import stream_ptr, to_device
 
     xv = to_device(x).reshape(-1)
     out = torch.empty_like(xv)
-    _lib.call("mf_pdf_xfx", xv.data_ptr(), xv.numel(), float(q2), out.data_ptr(), stream_ptr())
+    if pdg == 21:
+        _lib.call("mf_pdf_xfx", xv.data_ptr(), xv.numel(), float(q2), out.data_ptr(), stream_ptr())
+    else:
+        _lib.call("mf_pdf_xfx_flavour", int(pdg), xv.data_ptr(), xv.numel(), float(q2), out.data_ptr(),
+                  stream_ptr())
     return out.reshape(torch.as_tensor(x).shape) if not isinstance(x, torch.Tensor) else out.reshape(x.shape)
 
 

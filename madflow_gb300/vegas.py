@@ -46,14 +46,23 @@ class FusedIntegrand:
     kind 1: hadronic sqrt(S): ramboflow over 4(n-2)+2 uniforms, synthetic gluon
             PDF at Q^2 = q2, cuts on the outgoing gluons,
             f = |M|^2 * lum * weight (madflow_exec.py:436-458).
+    initial_states "gg": the g g process alone; "pp" (kind 1, n_gluons = 2):
+            p p > t t~ at leading order, the g g channel plus the light-quark
+            channels q q~ and q~ q (q = d u s c) with the synthetic quark
+            densities, summed per event as madflow sums its processes.
     """
 
     def __init__(self, n_gluons, kind=1, sqrts=13000.0, mt=173.0, wt=1.4915000200271606, alpha_s=0.118, ptmin=0.0,
-                 etamax=0.0, drmin=0.0, q2=None, newton_rule=_lib.MF_NEWTON_BATCH, precision=None):
+                 etamax=0.0, drmin=0.0, q2=None, newton_rule=_lib.MF_NEWTON_BATCH, precision=None,
+                 initial_states="gg"):
+        if initial_states not in ("gg", "pp"):
+            raise ValueError(f"initial_states must be 'gg' or 'pp', not {initial_states!r}")
         self.matrix = PROCESSES[n_gluons](precision=precision)
+        self.initial_states = initial_states
         self.cfg = dict(kind=kind, sqrts=float(sqrts), mt=float(mt), wt=float(wt), alpha_s=float(alpha_s),
                         ptmin=float(ptmin), etamax=float(etamax), drmin=float(drmin),
-                        q2=float(mt * mt if q2 is None else q2), newton_rule=int(newton_rule))
+                        q2=float(mt * mt if q2 is None else q2), newton_rule=int(newton_rule),
+                        initial_states=_lib.MF_INITIAL_PP if initial_states == "pp" else _lib.MF_INITIAL_GG)
         self._cs = _cfg_struct(self.cfg)
         nd = ctypes.c_int()
         _lib.call("mf_integrand_ndim", self.matrix.handle, ctypes.byref(self._cs), ctypes.byref(nd))

@@ -739,6 +739,38 @@ extern "C" void orc_colour_string(int k, const int* labels_in_order, int i, int 
 // ---------------------------------------------------------------------------
 static const int kNX = 100, kNQ = 50;
 static double pdf_A() { return 0.5 / std::exp(std::lgamma(0.8) + std::lgamma(6.0) - std::lgamma(6.8)); }
+// q q~ > t t~ (one diagram, an s-channel gluon), the light-quark channel of
+// p p > t t~ at leading order.  No instance exists in the reference's tests;
+// the evaluation follows the HELAS calls MadGraph makes for it (wavefunctions
+// of wavefunctions_flow.py, FFV1P0_3 and FFV1_0 above) and the colour
+// algebra T^a_ij T^a_kl = (d_il d_kj - d_ij d_kl / 3) / 2, which gives the
+// colour sum 2 |amp|^2.  p [N][4][4] (q, q~, t, t~), prm = {MT, WT, GC_11 re,
+// im}; out [N] = |M|^2 averaged over the initial spins (4) and colours (9).
+template <class R> static R smatrix_uux_ttx(const R* p, const double* prm) {
+  const R mt = R(prm[0]);
+  const Cx<R> g11{R(prm[2]), R(prm[3])};
+  R tot = R(0);
+  for (int h0 = -1; h0 <= 1; h0 += 2)
+    for (int h1 = -1; h1 <= 1; h1 += 2)
+      for (int h2 = -1; h2 <= 1; h2 += 2)
+        for (int h3 = -1; h3 <= 1; h3 += 2) {
+          WF<R> wq, wqb, wt, wtb, g;
+          ixxxxx<R>(p + 0, R(0), R(h0), R(1), wq);
+          oxxxxx<R>(p + 4, R(0), R(h1), R(-1), wqb);
+          oxxxxx<R>(p + 8, mt, R(h2), R(1), wt);
+          ixxxxx<R>(p + 12, mt, R(h3), R(-1), wtb);
+          FFV1P0_3<R>(wq, wqb, g11, R(0), R(0), g);
+          Cx<R> amp = FFV1_0<R>(wtb, wt, g, g11);
+          tot += amp.re * amp.re + amp.im * amp.im;
+        }
+  return tot * R(2.0) / R(36.0);
+}
+
+extern "C" void orc_smatrix_uux_ttx(const double* p, int64_t N, const double* prm, double* out) {
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < N; ++e) out[e] = smatrix_uux_ttx<double>(p + 16 * e, prm);
+}
+
 extern "C" void orc_pdf_table(double* table /*[kNQ][kNX]*/, double* lx0, double* dlx, double* lq0, double* dlq) {
   double A = pdf_A();
   *lx0 = std::log(1e-6); *dlx = (0.0 - *lx0) / (kNX - 1);
@@ -750,31 +782,83 @@ extern "C" void orc_pdf_table(double* table /*[kNQ][kNX]*/, double* lx0, double*
       table[iq * kNX + ix] = A * std::pow(x, -0.2) * std::pow(1.0 - x, 5.0);
     }
 }
+// Synthetic quark densities beside the gluon (the configurations define only
+// the gluon; p p > t t~ needs the light quarks too), x f(x) independent of Q:
+//   valence  x u_v = A x^0.5 (1-x)^3 with int u_v = 2,
+//            x d_v = A x^0.5 (1-x)^4 with int d_v = 1;
+//   sea      x qbar = A x^-0.2 (1-x)^7 with momentum fractions int x qbar =
+//            0.03 (ubar, dbar), 0.015 (s = sbar), 0.005 (c = cbar);
+//   u = u_v + ubar, d = d_v + dbar.
+// pdg: 21 gluon, 1..4 d u s c, -1..-4 their antiquarks.
+static double beta_fn(double a, double b) { return std::exp(std::lgamma(a) + std::lgamma(b) - std::lgamma(a + b)); }
+static double synth_xfx(int pdg, double x) {
+  if (x >= 1.0) return 0.0;
+  if (pdg == 21) return pdf_A() * std::pow(x, -0.2) * std::pow(1.0 - x, 5.0);
+  const int a = pdg < 0 ? -pdg : pdg;
+  const double frac = a <= 2 ? 0.03 : (a == 3 ? 0.015 : 0.005);
+  double v = frac / beta_fn(0.8, 8.0) * std::pow(x, -0.2) * std::pow(1.0 - x, 7.0);
+  if (pdg == 2) v += 2.0 / beta_fn(0.5, 4.0) * std::pow(x, 0.5) * std::pow(1.0 - x, 3.0);
+  if (pdg == 1) v += 1.0 / beta_fn(0.5, 5.0) * std::pow(x, 0.5) * std::pow(1.0 - x, 4.0);
+  return v;
+}
+extern "C" void orc_pdf_table_flavour(int pdg, double* table /*[kNQ][kNX]*/) {
+  double lx0 = std::log(1e-6), dlx = (0.0 - lx0) / (kNX - 1);
+  for (int iq = 0; iq < kNQ; ++iq)
+    for (int ix = 0; ix < kNX; ++ix) {
+      double x = std::exp(lx0 + ix * dlx);
+      if (ix == kNX - 1) x = 1.0;
+      table[iq * kNX + ix] = synth_xfx(pdg, x);
+    }
+}
+
 static double keys_w(double t) {  // cubic convolution kernel, a = -1/2
   t = std::fabs(t);
   if (t <= 1.0) return (1.5 * t - 2.5) * t * t + 1.0;
   if (t < 2.0) return ((-0.5 * t + 2.5) * t - 4.0) * t + 2.0;
   return 0.0;
 }
-extern "C" void orc_pdf_xfx(const double* x, int64_t N, double q2, double* out) {
-  static std::vector<double> tab;
-  static double lx0, dlx, lq0, dlq;
-  if (tab.empty()) { tab.resize(kNX * kNQ); orc_pdf_table(tab.data(), &lx0, &dlx, &lq0, &dlq); }
-  for (int64_t e = 0; e < N; ++e) {
-    double u = (std::log(x[e]) - lx0) / dlx, v = (std::log(q2) - lq0) / dlq;
-    int iu = (int)std::floor(u), iv = (int)std::floor(v);
-    double fu = u - iu, fv = v - iv;
-    double s = 0.0;
-    for (int a = -1; a <= 2; ++a) {
-      int qi = std::min(std::max(iv + a, 0), kNQ - 1);
-      double wv = keys_w(fv - a);
-      for (int b = -1; b <= 2; ++b) {
-        int xi = std::min(std::max(iu + b, 0), kNX - 1);
-        s += wv * keys_w(fu - b) * tab[qi * kNX + xi];
-      }
+// bicubic lookup (Keys 1981, a = -1/2, clamped edge nodes) of a [kNQ][kNX] table
+static double pdf_lookup(const double* tab, double x, double q2) {
+  const double lx0 = std::log(1e-6), dlx = (0.0 - lx0) / (kNX - 1);
+  const double lq0 = std::log(1.0), dlq = (std::log(1e10) - lq0) / (kNQ - 1);
+  double u = (std::log(x) - lx0) / dlx, v = (std::log(q2) - lq0) / dlq;
+  int iu = (int)std::floor(u), iv = (int)std::floor(v);
+  double fu = u - iu, fv = v - iv;
+  double s = 0.0;
+  for (int a = -1; a <= 2; ++a) {
+    int qi = std::min(std::max(iv + a, 0), kNQ - 1);
+    double wv = keys_w(fv - a);
+    for (int b = -1; b <= 2; ++b) {
+      int xi = std::min(std::max(iu + b, 0), kNX - 1);
+      s += wv * keys_w(fu - b) * tab[qi * kNX + xi];
     }
-    out[e] = s > 0.0 ? s : 0.0;
   }
+  return s > 0.0 ? s : 0.0;
+}
+extern "C" void orc_pdf_xfx(const double* x, int64_t N, double q2, double* out) {
+  static const std::vector<double> tab = [] {
+    std::vector<double> t(kNX * kNQ);
+    double a, b, c, d;
+    orc_pdf_table(t.data(), &a, &b, &c, &d);
+    return t;
+  }();
+  for (int64_t e = 0; e < N; ++e) out[e] = pdf_lookup(tab.data(), x[e], q2);
+}
+// x f(x, Q^2) of flavour pdg (21, +-1..+-4) from its table
+extern "C" int orc_pdf_xfx_flavour(int pdg, const double* x, int64_t N, double q2, double* out) {
+  static const std::map<int, std::vector<double>> tabs = [] {
+    std::map<int, std::vector<double>> m;
+    for (int f : {21, 1, 2, 3, 4, -1, -2, -3, -4}) {
+      std::vector<double> t(kNX * kNQ);
+      orc_pdf_table_flavour(f, t.data());
+      m[f] = t;
+    }
+    return m;
+  }();
+  auto it = tabs.find(pdg);
+  if (it == tabs.end()) return 1;
+  for (int64_t e = 0; e < N; ++e) out[e] = pdf_lookup(it->second.data(), x[e], q2);
+  return 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -893,6 +977,7 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
   IntegrandCfg cfg;
   cfg.kind = (int)cfgv[0]; cfg.k = (int)cfgv[1]; cfg.sqrts = cfgv[2]; cfg.mt = cfgv[3]; cfg.wt = cfgv[4];
   cfg.alphas = cfgv[5]; cfg.ptmin = cfgv[6]; cfg.etamax = cfgv[7]; cfg.drmin = cfgv[8]; cfg.newton_rule = (int)cfgv[9];
+  const int initial_states = (int)cfgv[10];  // 0: g g; 1: p p (g g + q q~ + q~ q, q = d u s c), k = 2 only
   double gs = 2.0 * std::sqrt(M_PI * cfg.alphas);
   // MT, WT, GC_10 = -g, GC_11 = i g, GC_12 = i g^2, c3 = -i, c4 = -1
   double prm[12] = {cfg.mt, cfg.wt, -gs, 0.0, 0.0, gs, 0.0, gs * gs, 0.0, -1.0, -1.0, 0.0};
@@ -941,6 +1026,26 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
     int64_t e = idx[i];
     double lum = g1[e] * g2[e] / x1[e] / x2[e];
     f[e] = mep[i] * lum * w[e];
+  }
+  if (initial_states == 1 && cfg.k == 2 && !idx.empty()) {
+    // madflow's integrand: sum over the processes of luminosity x |M|^2, the
+    // luminosity summed over each process's initial states and their mirror
+    // images (scripts/madflow_exec.py:444-458, utilities.py:25-39)
+    std::vector<double> meq(idx.size()), qa((size_t)N), qb((size_t)N), qc((size_t)N), qd((size_t)N);
+    double prmq[4] = {cfg.mt, cfg.wt, 0.0, gs};
+    orc_smatrix_uux_ttx(pp.data(), (int64_t)idx.size(), prmq, meq.data());
+    std::vector<double> lumq((size_t)N, 0.0);
+    for (int q = 1; q <= 4; ++q) {
+      orc_pdf_xfx_flavour(q, x1.data(), N, q2, qa.data());
+      orc_pdf_xfx_flavour(-q, x2.data(), N, q2, qb.data());
+      orc_pdf_xfx_flavour(-q, x1.data(), N, q2, qc.data());
+      orc_pdf_xfx_flavour(q, x2.data(), N, q2, qd.data());
+      for (int64_t e = 0; e < N; ++e) lumq[e] += qa[e] * qb[e] + qc[e] * qd[e];
+    }
+    for (size_t i = 0; i < idx.size(); ++i) {
+      int64_t e = idx[i];
+      f[e] += meq[i] * (lumq[e] / x1[e] / x2[e]) * w[e];
+    }
   }
 }
 

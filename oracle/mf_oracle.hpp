@@ -545,6 +545,28 @@ template <class R> inline void VVV1P0_1(const WF<R>& V2, const WF<R>& V3, Cx<R> 
   Cx<R> c = mul_i(den);
   for (int k = 0; k < 4; ++k) V1.w[2 + k] = c * (v23 * Cx<R>(P3[k] - P2[k]) + a[k] * c2 + b[k] * c3);
 }
+// Off-shell vector from a fermion pair (the ALOHA routine MadGraph names
+// FFV1P0_3; no instance in the reference's mock-up, restated from the same
+// Dirac algebra): with c_mu = F1^T S(e_mu) F2, so that F1^T S(V) F2 =
+// sum_mu c_mu V^mu, V3^mu = i denom g^{mu mu} c_mu, P3 = -(p_F1 + p_F2).
+template <class R> inline void FFV1P0_3(const WF<R>& F1, const WF<R>& F2, Cx<R> coup, R M3, R W3, WF<R>& V3) {
+  V3.w[0] = F1.w[0] + F2.w[0];
+  V3.w[1] = F1.w[1] + F2.w[1];
+  R P3[4];
+  mom_of<R>(V3, P3);
+  for (int k = 0; k < 4; ++k) P3[k] = -P3[k];
+  Cx<R> den = prop_denom<R>(coup, P3, M3, W3);
+  Cx<R> c = mul_i(den);
+  for (int mu = 0; mu < 4; ++mu) {
+    Cx<R> e[4];
+    e[mu] = Cx<R>(R(1));
+    Cx<R> y[4];
+    s_apply<R>(e, F2.w + 2, y);
+    Cx<R> cm = F1.w[2] * y[0] + F1.w[3] * y[1] + F1.w[4] * y[2] + F1.w[5] * y[3];
+    V3.w[2 + mu] = c * (mu == 0 ? cm : -cm);
+  }
+}
+
 // Colour-ordered four-gluon contact current (no reference instance exists:
 // derived from the QCD Feynman rules).  For the cyclic order (1,2,3,4) the
 // colour-ordered vertex is proportional to 2 g13 g24 - g12 g34 - g14 g23, so

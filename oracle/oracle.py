@@ -282,10 +282,29 @@ def ggttx_flops(p, prm6):
     return lib().orc_ggttx_flops(_p(_c64(p)), _p(_c64(prm6)))
 
 
+def smatrix_uux_ttx(all_ps, mdl_MT, mdl_WT, GC_11):
+    """q q~ > t t~ |M|^2 (averaged) for momenta (N, 4, 4) ordered q, q~, t, t~."""
+    p = _c64(all_ps)
+    out = np.empty(p.shape[0])
+    prm = _c64([mdl_MT, mdl_WT, complex(GC_11).real, complex(GC_11).imag])
+    lib().orc_smatrix_uux_ttx(_p(p), ctypes.c_int64(p.shape[0]), _p(prm), _p(out))
+    return out
+
+
 def pdf_xfx(x, q2):
     x = _c64(x)
     out = np.empty_like(x)
     lib().orc_pdf_xfx(_p(x), ctypes.c_int64(x.size), ctypes.c_double(q2), _p(out))
+    return out
+
+
+def pdf_xfx_flavour(pdg, x, q2):
+    """x f(x, Q^2) of the synthetic density of flavour pdg (21 gluon, 1..4 d u s
+    c, negative: antiquarks)."""
+    x = _c64(x)
+    out = np.empty_like(x)
+    if lib().orc_pdf_xfx_flavour(ctypes.c_int(pdg), _p(x), ctypes.c_int64(x.size), ctypes.c_double(q2), _p(out)):
+        raise ValueError(f"no synthetic density for flavour {pdg}")
     return out
 
 
@@ -334,10 +353,12 @@ def pass_cuts(plab, ptmin, etamax, drmin):
 
 
 def integrand(cfg, x, plan=None, fast=False):
-    """cfg: [kind, k, sqrts, mt, wt, alphas, ptmin, etamax, drmin, newton_rule].
-    fast: the timing build (plan, if given, must come from the same build)."""
+    """cfg: [kind, k, sqrts, mt, wt, alphas, ptmin, etamax, drmin, newton_rule
+    (, initial_states: 0 g g, 1 p p)].  fast: the timing build (plan, if
+    given, must come from the same build)."""
     if plan is not None:
         fast = plan.fast
+    cfg = list(cfg) + [0] * (11 - len(cfg))
     x = _c64(x)
     f = np.empty(x.shape[0])
     lib(fast).orc_integrand(_p(_c64(cfg)), ctypes.c_void_p(plan.h if plan is not None else None), _p(x),
