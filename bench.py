@@ -61,9 +61,9 @@ REC_BYTES = {4: 1536}
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max clock
 # DRAM bytes (read + write) of the g g > t t~ g g matrix-element kernel per
 # passing event: one ncu capture of 10^6 points
-# (profiles/me_rec_kernel_ggttxgg_mixed.md, 1.2143 GB over 760,841 events);
+# (profiles/me_rec_kernel_ggttxgg_mixed.md, 811.1 MB over 514,487 events);
 # the kernel's traffic is its records, so it scales with the events of a launch
-ME_DRAM_BYTES_PER_EVENT = 1596.0
+ME_DRAM_BYTES_PER_EVENT = 1576.0
 
 C3_CUTS = dict(ptmin=60.0, etamax=2.5, drmin=0.4)
 PDF = "synthetic gluon PDF x g=A x^-0.2 (1-x)^5 (100x50 bicubic), Q=mt"
