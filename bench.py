@@ -209,9 +209,11 @@ def _prec_code(name):
     return _lib.MF_PREC_MIXED if name == "mixed" else _lib.MF_PREC_FP64
 
 
-def fused_steps(cfg, prec_name, N, steps, warmup, seed, dist=None, rank=0, local=0, sample_clocks=True):
-    """W untimed and K timed fused VEGAS iterations (L2 flushed before each);
-    returns the timing record of the steps."""
+def fused_steps(cfg, prec_name, N, steps, warmup, seed, dist=None, rank=0, local=0, sample_clocks=True,
+                events_limit=None):
+    """W untimed and K timed fused VEGAS iterations (L2 flushed before each),
+    in slices of events_limit events if given; returns the timing record of
+    the steps (stage times for one-slice steps only)."""
     import torch
 
     from madflow_gb300 import _lib
@@ -225,7 +227,8 @@ def fused_steps(cfg, prec_name, N, steps, warmup, seed, dist=None, rank=0, local
     npass = torch.zeros(steps, dtype=torch.int64, device="cuda")
 
     def step():
-        integ.iteration(vegas.grid, vegas.seed, vegas.stream_id, vegas.iteration, N, vegas.results, f_out=f_out)
+        integ.iteration(vegas.grid, vegas.seed, vegas.stream_id, vegas.iteration, N, vegas.results, f_out=f_out,
+                        events_limit=events_limit)
         if dist:
             # one grid over all ranks: the iteration sums are summed before the refinement
             reduce_results(vegas.results)
@@ -241,7 +244,8 @@ def fused_steps(cfg, prec_name, N, steps, warmup, seed, dist=None, rank=0, local
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     # the pipeline records events between its stages (same stream), read after each step
-    integ.set_timing(True)
+    timing = events_limit is None or events_limit >= N
+    integ.set_timing(timing)
     stage_ms = []
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
@@ -253,7 +257,8 @@ def fused_steps(cfg, prec_name, N, steps, warmup, seed, dist=None, rank=0, local
             ends[i].record()
             npass[i] = torch.count_nonzero(f_out)
             ends[i].synchronize()
-            stage_ms.append(integ.stage_ms())
+            if timing:
+                stage_ms.append(integ.stage_ms())
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
@@ -405,6 +410,16 @@ def extras(args, cfg, prec_name, out):
             o = fused_steps(cfg, other, cfg["events"], 3, 2, args.seed, sample_clocks=False)
             out["other_precision"] = {"precision": other, "value": sum(o["npass"]) / o["step_s"],
                                       "unit": "|M|^2 evals/s", "ms_per_step": 1000.0 * o["step_s"] / 3}
+    if name == "c3" and args.integration:
+        # the same iteration in slices of events_limit events (scratch of one
+        # slice): 10^6, and 5*10^4, the reference's own default for six
+        # particles on a GPU with 13 GB or more (config.py:168-176)
+        out["events_limit"] = {}
+        for lim in (1_000_000, 50_000):
+            o = fused_steps(cfg, prec_name, cfg["events"], 3, 2, args.seed, sample_clocks=False, events_limit=lim)
+            out["events_limit"][str(lim)] = {"value": sum(o["npass"]) / o["step_s"], "unit": "|M|^2 evals/s",
+                                             "ms_per_step": 1000.0 * o["step_s"] / 3,
+                                             "scratch_bytes": o["integ"].scratch_bytes()}
     if name == "c3" and args.time_to_target:
         out["time_to_1e-3"] = time_to_target(args, cfg)
     if name == "c4":

@@ -136,6 +136,17 @@ typedef struct {
    * (scripts/madflow_exec.py:444-458, utilities.py:25-39).  Other
    * multiplicities with MF_INITIAL_PP: MF_ERR_UNSUPPORTED. */
   int initial_states;
+  /* > 0: mf_integrand, mf_vegas_iteration and mf_vegas_events run their
+   * events in consecutive slices of at most events_limit events, as
+   * vegasflow's VegasFlow(events_limit=...) hands the integrand one slice per
+   * call (scripts/madflow_exec.py:474-487, config.py:121-176).  The handle's
+   * scratch then holds one slice instead of the call (1.8 KB per event for
+   * four gluons, mixed; mf_process_scratch_bytes), the batch Newton rule of
+   * the massive phase space runs per slice, and the slices' sums add up in
+   * results.  Uniforms and the per-event outputs do not depend on the
+   * slicing.  0: one slice.  < 0: MF_ERR_ARG.  Stage timing
+   * (mf_process_set_timing) records one-slice calls only. */
+  int64_t events_limit;
 } mf_integrand_config;
 
 /* Number of integration dimensions of a configuration (8 for kind 0,
@@ -248,6 +259,13 @@ int mf_process_nonfinite(mf_process* proc, int64_t* count, int clear);
  * counterpart in the reference. */
 int mf_process_set_wait_limit(mf_process* proc, int tries);
 int mf_process_stage_ms(const mf_process* proc, float* ms);
+
+/* Device bytes the handle holds as scratch of the fused pipeline and of
+ * mf_smatrix (per-event records and state, sized to the largest slice or
+ * call so far, block partials, the global workspace of five gluons); freed
+ * by mf_process_destroy.  No counterpart in the reference (TensorFlow owns
+ * its memory). */
+int mf_process_scratch_bytes(const mf_process* proc, int64_t* bytes);
 
 /* VEGAS accumulation for an integrand evaluated by the caller: f [N], jac
  * [N], bins [ndim][N] (from mf_vegas_sample); results (device)

@@ -55,6 +55,7 @@ class IntegrandConfig(ctypes.Structure):
         ("q2", c_double),
         ("newton_rule", c_int),
         ("initial_states", c_int),
+        ("events_limit", c_int64),
     ]
 
 
@@ -98,6 +99,7 @@ _SIGS = {
                                   ctypes.POINTER(ctypes.c_float)]),
     "mf_process_set_tuning": (c_int, [c_void_p, c_int, c_int]),
     "mf_process_stage_ms": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "mf_process_scratch_bytes": (c_int, [c_void_p, ctypes.POINTER(c_int64)]),
     "mf_vegas_accumulate_noalloc": (c_int, [c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_double, c_dp, c_void_p]),
     "mf_vegas_refine": (c_int, [c_dp, c_dp, c_int, c_int, c_double, c_void_p]),
     "mf_vegas_sample": (c_int, [c_dp, c_int, c_int, c_dp, c_int64, c_dp, c_dp, c_dp, c_void_p]),

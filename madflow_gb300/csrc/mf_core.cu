@@ -381,14 +381,15 @@ __global__ void vegas_refine_kernel(double* __restrict__ div, const double* __re
   for (int j = 0; j <= nb; ++j) g[j] = nd[j];
 }
 
-// Fixed-order sum of the per-block partials: out[i] = sum_b partials[b][i].
+// Fixed-order sum of the per-block partials: out[i] = sum_b partials[b][i]
+// (add: out[i] += that sum, for the later slices of an iteration).
 __global__ void reduce_partials_kernel(const double* __restrict__ partials, int nblocks, int width,
-                                       double* __restrict__ out) {
+                                       double* __restrict__ out, int add = 0) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= width) return;
   double s = 0.0;
   for (int b = 0; b < nblocks; ++b) s += partials[(int64_t)b * width + i];
-  out[i] = s;
+  out[i] = add ? out[i] + s : s;
 }
 
 // Deterministic VEGAS accumulation for integrands evaluated outside the fused
@@ -961,24 +962,17 @@ static int ensure_events(mf_process* p, int64_t N) {
   return MF_OK;
 }
 
-// One pass of the pipeline over A.N events: phase-space first pass (with the
-// batch Newton minimum), phase space, |M|^2, accumulation.  results (optional) [2 + ndim*nb]; f_out (optional) [N].
-static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, double* results, double* f_out,
-                     void* stream) {
-  int st = ensure_events(p, A.N);
-  if (st) return st;
+// One pass of the pipeline over n events, the slice [A.e0, A.e0 + n) of the
+// call: phase-space first pass (with the batch Newton minimum of the slice),
+// phase space, |M|^2, accumulation.  results (optional) [2 + ndim*nb]
+// (add_results: added to, for the later slices); f_out (optional) [n].
+static int run_slice(mf_process* p, IterArgs A, int64_t n, const mf_integrand_config* c, double* results,
+                     int add_results, double* f_out, bool timed, void* stream) {
+  A.N = n;
   A.prep = p->d_prep;
   A.state = p->d_state;
   A.pref = p->d_pref;
   A.me = p->d_me;
-  if (A.qq && p->extra_cap < A.N) {
-    cudaFree(p->d_extra);
-    p->d_extra = nullptr;
-    p->extra_cap = 0;
-    st = cuda_status(cudaMalloc(&p->d_extra, sizeof(double) * (size_t)A.N));
-    if (st) return st;
-    p->extra_cap = A.N;
-  }
   A.extra = A.qq ? p->d_extra : nullptr;
   A.bins = A.x_in ? nullptr : p->d_bins;
   int accum_grid = 8 * 152;
@@ -987,28 +981,13 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     accum_grid = 8 * (sms > 0 ? sms : 152);
-    if (accum_grid > A.N) accum_grid = (int)A.N;
+    if (accum_grid > n) accum_grid = (int)n;
   }
-  int width = 2 + A.ndim * A.nb;
-  st = ensure_partials(p, (size_t)accum_grid * width);
+  const int width = 2 + A.ndim * A.nb;
+  int st = ensure_partials(p, (size_t)accum_grid * width);
   if (st) return st;
-  if (!p->d_kmin) {
-    st = cuda_status(cudaMalloc(&p->d_kmin, sizeof(int)));
-    if (st) return st;
-  }
   A.newton_iters = p->d_kmin;
-  bool per_event = c->newton_rule == MF_NEWTON_PER_EVENT;
-  // stage timing: not while the stream is being captured into a graph
-  bool timed = false;
-  if (p->timing) {
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(S(stream), &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
-      timed = true;
-      for (cudaEvent_t& e : p->tev)
-        if (!e && cudaEventCreate(&e) != cudaSuccess) timed = false;
-    }
-  }
-  p->timed_last = timed;
+  const bool per_event = c->newton_rule == MF_NEWTON_PER_EVENT;
   auto mark = [&](int i) {
     if (timed) cudaEventRecord(p->tev[i], S(stream));
   };
@@ -1018,24 +997,74 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   mark(1);
   if (mf_launch_ps(p->k, p->prec, A, S(stream))) return last_launch();
   mark(2);
-  if (autotune_wanted(p, A.N, stream)) {
-    st = autotune_me(p, A.prep, A.N, A.pref, A.me, stream);
+  if (autotune_wanted(p, n, stream)) {
+    st = autotune_me(p, A.prep, n, A.pref, A.me, stream);
     if (st) return st;
   }
-  if (mf_launch_me(p->k, p->prec, A.prep, A.N, A.pref, A.me, nullptr, p->d_err, p->tune, p->d_ws, S(stream)))
+  if (mf_launch_me(p->k, p->prec, A.prep, n, A.pref, A.me, nullptr, p->d_err, p->tune, p->d_ws, S(stream)))
     return last_launch();
   mark(3);
   size_t shm = (size_t)(A.ndim * A.nb + 3 * 256) * sizeof(double);
   static bool attr_done[64] = {false};
   st = smem_attr_once((const void*)accum_kernel, attr_done);
   if (st) return st;
-  accum_kernel<<<accum_grid, 256, shm, S(stream)>>>(A.pref, A.me, A.qq ? A.extra : nullptr, A.bins, A.N, A.ndim,
+  accum_kernel<<<accum_grid, 256, shm, S(stream)>>>(A.pref, A.me, A.qq ? A.extra : nullptr, A.bins, n, A.ndim,
                                                      A.nb, A.inv_n, f_out,
                                                      results ? p->d_partials : nullptr, p->d_err, p->d_nonfinite);
   if (results)
-    reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(p->d_partials, accum_grid, width, results);
+    reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(p->d_partials, accum_grid, width, results,
+                                                                       add_results);
   mark(4);
   return last_launch();
+}
+
+// The pipeline over the A.N events of a call, in consecutive slices of at
+// most c->events_limit events (0: one slice), as the reference's integrator
+// hands its integrand one slice of events_limit events per call
+// (scripts/madflow_exec.py:474-487): the scratch holds one slice, the batch
+// Newton rule runs per slice, the slices' sums add up in results.  The
+// Philox event index, x_in, u_out, f_out and ps_out run over the whole call.
+static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, double* results, double* f_out,
+                     void* stream) {
+  if (c->events_limit < 0) return MF_ERR_ARG;
+  const int64_t total = A.N;
+  const int64_t slice = (c->events_limit > 0 && c->events_limit < total) ? c->events_limit : total;
+  int st = ensure_events(p, slice);
+  if (st) return st;
+  if (A.qq && p->extra_cap < slice) {
+    cudaFree(p->d_extra);
+    p->d_extra = nullptr;
+    p->extra_cap = 0;
+    st = cuda_status(cudaMalloc(&p->d_extra, sizeof(double) * (size_t)slice));
+    if (st) return st;
+    p->extra_cap = slice;
+  }
+  if (!p->d_kmin) {
+    st = cuda_status(cudaMalloc(&p->d_kmin, sizeof(int)));
+    if (st) return st;
+  }
+  // stage timing: one slice, and not while the stream is being captured into a graph
+  bool timed = false;
+  if (p->timing && slice == total) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(S(stream), &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
+      timed = true;
+      for (cudaEvent_t& e : p->tev)
+        if (!e && cudaEventCreate(&e) != cudaSuccess) timed = false;
+    }
+  }
+  p->timed_last = timed;
+  A.ld = total;
+  const int npart = p->k + 2;
+  double* ps_out = A.ps_out;
+  for (int64_t off = 0; off < total; off += slice) {
+    const int64_t n = total - off < slice ? total - off : slice;
+    A.e0 = off;
+    A.ps_out = ps_out ? ps_out + off * npart * 4 : nullptr;
+    st = run_slice(p, A, n, c, results, off > 0, f_out ? f_out + off : nullptr, timed, stream);
+    if (st) return st;
+  }
+  return MF_OK;
 }
 
 int mf_process_tuning(const mf_process* p, int* colour, int* waves, int* tuned, float* ms) {
@@ -1096,6 +1125,17 @@ int mf_process_stage_ms(const mf_process* p, float* ms) {
     int st = cuda_status(cudaEventElapsedTime(&ms[i], p->tev[i], p->tev[i + 1]));
     if (st) return st;
   }
+  return MF_OK;
+}
+
+int mf_process_scratch_bytes(const mf_process* p, int64_t* bytes) {
+  if (!p || !bytes) return MF_ERR_ARG;
+  const int64_t per_event = mf_prep_bytes(p->k, p->prec) + (int64_t)sizeof(double) * (mf_state_words(p->k) + 2) +
+                            MF_MAX_DIM;
+  int64_t b = p->event_cap * per_event + p->extra_cap * (int64_t)sizeof(double) +
+              (int64_t)p->partial_cap * (int64_t)sizeof(double);
+  if (p->d_ws) b += mf_ws_bytes(p->k, p->prec);
+  *bytes = b;
   return MF_OK;
 }
 

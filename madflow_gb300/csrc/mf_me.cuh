@@ -40,8 +40,10 @@ struct IterArgs {
   double q2;
   const int* newton_iters;  // device: iterations of the batch Newton rule (<= 0: per event)
   int f32q;
-  const double* x_in;  // optional [ndim][N] points (integrand API): no Philox / VEGAS map, jac = 1
-  float* u_out;        // optional [ndim][N] uniforms
+  const double* x_in;  // optional [ndim][ld] points (integrand API): no Philox / VEGAS map, jac = 1
+  float* u_out;        // optional [ndim][ld] uniforms
+  int64_t e0, ld;      // the slice's first event in the call (Philox event index, x_in / u_out column)
+                       // and the call's event count (x_in / u_out row length)
   double* ps_out;      // optional [N][K+2][4] lab-frame momenta of the passing events (event output)
   int qq;              // p p > t t~: add the light-quark channels q q~ and q~ q (K = 2 only)
   double* extra;       // [N] with qq: jac x weight x quark luminosity x |M|^2(q q~ > t t~)
@@ -98,20 +100,21 @@ MF_DO P vegas_map(const P* __restrict__ div, int ndim, int nb, const P* u, P* x,
   return jac;
 }
 
-// The point of event e: the caller's x (integrand API, jac = 1) or Philox
+// The point of event e of the slice: the caller's x (integrand API, jac = 1) or Philox
 // uniforms through the VEGAS grid (sdiv: the grid in P).
 template <class P>
 MF_DO void event_point(const IterArgs& A, int64_t e, int it, const P* sdiv, P* x, P& jac, bool store) {
+  const int64_t g = A.e0 + e;  // the event's index in the call
   if (A.x_in) {
-    for (int d = 0; d < A.ndim; ++d) x[d] = (P)A.x_in[(int64_t)d * A.N + e];
+    for (int d = 0; d < A.ndim; ++d) x[d] = (P)A.x_in[(int64_t)d * A.ld + g];
     jac = P(1);
     return;
   }
   P u[MF_MAX_DIM];
-  for (int d = 0; d < A.ndim; d += 2) uniform_pair<P>(A.seed, A.stream, (uint32_t)it, (uint64_t)e, d / 2, u[d], u[d + 1]);
+  for (int d = 0; d < A.ndim; d += 2) uniform_pair<P>(A.seed, A.stream, (uint32_t)it, (uint64_t)g, d / 2, u[d], u[d + 1]);
   jac = vegas_map<P>(sdiv, A.ndim, A.nb, u, x, store ? A.bins + e : nullptr, A.N);
   if (store && A.u_out)
-    for (int d = 0; d < A.ndim; ++d) A.u_out[(int64_t)d * A.N + e] = (float)u[d];
+    for (int d = 0; d < A.ndim; ++d) A.u_out[(int64_t)d * A.ld + g] = (float)u[d];
 }
 
 // First part of the phase space of one event (phasespace.py:257-300 up to

@@ -31,6 +31,15 @@ BINS_MAX = 50
 ALPHA = 1.5
 
 
+def _limit(events_limit):
+    """events_limit for the C configuration: 0 = one slice."""
+    if events_limit is None:
+        return 0
+    if int(events_limit) <= 0:
+        raise ValueError(f"events_limit must be positive, not {events_limit}")
+    return int(events_limit)
+
+
 def _cfg_struct(cfg):
     s = _lib.IntegrandConfig()
     for k, _ in _lib.IntegrandConfig._fields_:
@@ -50,11 +59,16 @@ class FusedIntegrand:
             p p > t t~ at leading order, the g g channel plus the light-quark
             channels q q~ and q~ q (q = d u s c) with the synthetic quark
             densities, summed per event as madflow sums its processes.
+    events_limit: run calls in slices of at most this many events (the
+            handle's scratch holds one slice; the batch Newton rule runs per
+            slice, as madflow's integrand sees one vegasflow slice per call);
+            None: one slice.  VegasFlow(events_limit=...) overrides it for
+            its iterations.
     """
 
     def __init__(self, n_gluons, kind=1, sqrts=13000.0, mt=173.0, wt=1.4915000200271606, alpha_s=0.118, ptmin=0.0,
                  etamax=0.0, drmin=0.0, q2=None, newton_rule=_lib.MF_NEWTON_BATCH, precision=None,
-                 initial_states="gg"):
+                 initial_states="gg", events_limit=None):
         if initial_states not in ("gg", "pp"):
             raise ValueError(f"initial_states must be 'gg' or 'pp', not {initial_states!r}")
         self.matrix = PROCESSES[n_gluons](precision=precision)
@@ -62,7 +76,8 @@ class FusedIntegrand:
         self.cfg = dict(kind=kind, sqrts=float(sqrts), mt=float(mt), wt=float(wt), alpha_s=float(alpha_s),
                         ptmin=float(ptmin), etamax=float(etamax), drmin=float(drmin),
                         q2=float(mt * mt if q2 is None else q2), newton_rule=int(newton_rule),
-                        initial_states=_lib.MF_INITIAL_PP if initial_states == "pp" else _lib.MF_INITIAL_GG)
+                        initial_states=_lib.MF_INITIAL_PP if initial_states == "pp" else _lib.MF_INITIAL_GG,
+                        events_limit=_limit(events_limit))
         self._cs = _cfg_struct(self.cfg)
         nd = ctypes.c_int()
         _lib.call("mf_integrand_ndim", self.matrix.handle, ctypes.byref(self._cs), ctypes.byref(nd))
@@ -78,8 +93,14 @@ class FusedIntegrand:
                   stream_ptr())
         return f
 
-    def iteration(self, grid, seed, stream_id, iteration_dev, n_events, results, f_out=None, u_out=None):
-        _lib.call("mf_vegas_iteration", self.matrix.handle, ctypes.byref(self._cs), grid.data_ptr(),
+    def iteration(self, grid, seed, stream_id, iteration_dev, n_events, results, f_out=None, u_out=None,
+                  events_limit=None):
+        """One fused VEGAS iteration (mf_vegas_iteration); events_limit (if
+        given) replaces the integrand's own for this call."""
+        cs = self._cs
+        if events_limit is not None:
+            cs = _cfg_struct(dict(self.cfg, events_limit=_limit(events_limit)))
+        _lib.call("mf_vegas_iteration", self.matrix.handle, ctypes.byref(cs), grid.data_ptr(),
                   grid.shape[1] - 1, int(seed), int(stream_id), iteration_dev.data_ptr(), int(n_events),
                   results.data_ptr(), f_out.data_ptr() if f_out is not None else None,
                   u_out.data_ptr() if u_out is not None else None, stream_ptr())
@@ -100,6 +121,12 @@ class FusedIntegrand:
             raise _lib.DeviceError("a bounded wait on the tensor cores ran out in the matrix-element kernel; "
                                    "the affected events were set to NaN")
         return int(count.value)
+
+    def scratch_bytes(self):
+        """Device bytes of scratch the handle holds (mf_process_scratch_bytes)."""
+        b = ctypes.c_int64()
+        _lib.call("mf_process_scratch_bytes", self.matrix.handle, ctypes.byref(b))
+        return int(b.value)
 
     def set_wait_limit(self, tries):
         """Tries (~1 ms each) of each bounded tensor-core wait (default 1000)."""
@@ -250,15 +277,20 @@ class VegasFlow:
         _lib.call("mf_vegas_refine", self.grid.data_ptr(), self.results[2:].data_ptr(), self.n_dim, self.nbins,
                   self.alpha, stream_ptr())
 
+    def _fused_limit(self):
+        return self.events_per_run if self.events_per_run < self.n_events else None
+
     def _iteration_fused_body(self):
-        self.integrand.iteration(self.grid, self.seed, self.stream_id, self.iteration, self.n_events, self.results)
+        self.integrand.iteration(self.grid, self.seed, self.stream_id, self.iteration, self.n_events, self.results,
+                                 events_limit=self._fused_limit())
         if self.train:
             self._refine()
         self.iteration += 1
 
     def _iteration_sharded(self):
         if isinstance(self.integrand, FusedIntegrand):
-            self.integrand.iteration(self.grid, self.seed, self.stream_id, self.iteration, self.n_events, self.results)
+            self.integrand.iteration(self.grid, self.seed, self.stream_id, self.iteration, self.n_events, self.results,
+                                     events_limit=self._fused_limit())
         else:
             train, self.train = self.train, False
             self._iteration_python()

@@ -329,14 +329,16 @@ extern "C" void orc_colour_matrix(int k, double* Cout) {
   do perms.push_back(sig);
   while (std::next_permutation(sig.begin(), sig.end()));
   int np = (int)perms.size();
-  std::vector<double> row(np, 0.0);
   int nb = 1;
   for (int i = 0; i < k; ++i) nb *= 8;
-#pragma omp parallel
-  {
-    std::vector<double> rowp(np, 0.0);
-#pragma omp for schedule(static)
-    for (int bi = 0; bi < nb; ++bi) {
+  // partial rows over fixed blocks of colour assignments, summed in block
+  // order: the same matrix for any number of threads
+  constexpr int kBlocks = 64;
+  std::vector<double> part((size_t)kBlocks * np, 0.0);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int blk = 0; blk < kBlocks; ++blk) {
+    double* rowp = &part[(size_t)blk * np];
+    for (int bi = blk; bi < nb; bi += kBlocks) {
       int b[8];
       int t = bi;
       for (int i = 0; i < k; ++i) { b[i] = t % 8; t /= 8; }
@@ -364,9 +366,10 @@ extern "C" void orc_colour_matrix(int k, double* Cout) {
         rowp[pi] += tr.real();
       }
     }
-#pragma omp critical
-    for (int pi = 0; pi < np; ++pi) row[pi] += rowp[pi];
   }
+  std::vector<double> row(np, 0.0);
+  for (int blk = 0; blk < kBlocks; ++blk)
+    for (int pi = 0; pi < np; ++pi) row[pi] += part[(size_t)blk * np + pi];
   // index of sigma^-1 tau
   std::map<std::vector<int>, int> idx;
   for (int i = 0; i < np; ++i) idx[perms[i]] = i;

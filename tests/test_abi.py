@@ -61,3 +61,29 @@ def test_library_is_in_tree():
     import os
 
     assert os.path.commonpath([build.LIB_PATH, build.HERE]) == build.HERE
+
+
+def test_integrand_config_layout_matches_header(tmp_path):
+    """The ctypes mirror of mf_integrand_config has the C struct's size and
+    field offsets (compiled from the header with the host C compiler)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    import pytest
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = [f for f, _ in _lib.IntegrandConfig._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"madflow_gb300.h\"\nint main(void) {\n"
+                   + "  printf(\"%zu\\n\", sizeof(mf_integrand_config));\n"
+                   + "".join(f"  printf(\"%zu\\n\", offsetof(mf_integrand_config, {f}));\n" for f in fields)
+                   + "  return 0;\n}\n")
+    inc = Path(__file__).resolve().parents[1] / "include"
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got[0] == ctypes.sizeof(_lib.IntegrandConfig)
+    assert got[1:] == [getattr(_lib.IntegrandConfig, f).offset for f in fields]

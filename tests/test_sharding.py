@@ -130,7 +130,8 @@ def _cpu_vegasflow(group):
         def __init__(self):
             self.n_dim = SH_NDIM
 
-        def iteration(self, grid, seed, stream_id, iteration_dev, n_events, results, f_out=None, u_out=None):
+        def iteration(self, grid, seed, stream_id, iteration_dev, n_events, results, f_out=None, u_out=None,
+                      events_limit=None):
             r = _stub_results(grid.numpy(), seed, stream_id, int(iteration_dev.item()), n_events)
             results.copy_(torch.tensor(r))
 
