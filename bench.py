@@ -93,6 +93,16 @@ CONFIGS["pp"] = dict(k=2, kind=1, sqrts=13000.0, cuts={}, events=10_000_000, ite
                      workload=f"p p > t t~ (g g + q q~ + q~ q, q = d u s c), sqrt(S)=13 TeV, {PDF} and synthetic "
                               "quark densities, no cuts, 10-dim ramboflow, VEGAS 50 bins/dim",
                      process="gg_ttx (3 diagrams) + uux_ttx (1 diagram, 4 flavours and their mirror images)")
+# p p > t t~ j at leading order: g g > t t~ g and the light-quark channels
+# q q~ > t t~ g, q g > t t~ q, q~ g > t t~ q~ (and mirror images); the jet
+# cuts of c2 on particle 4 whatever its flavour
+CONFIGS["ppj"] = dict(k=3, kind=1, sqrts=13000.0, cuts=dict(ptmin=30.0, etamax=4.0, drmin=0.0), events=10_000_000,
+                      iterations=10, precision="mixed", initial_states="pp",
+                      workload=f"p p > t t~ j (g g > t t~ g + q q~ > t t~ g + q g > t t~ q + q~ g > t t~ q~, "
+                               f"q = d u s c, mirror images), sqrt(S)=13 TeV, {PDF} and synthetic quark densities, "
+                               "pT(j)>30, |eta(j)|<4, 14-dim ramboflow, VEGAS 50 bins/dim",
+                      process="gg_ttxg (16 diagrams) + uux_ttxg, ug_ttxu, uxg_ttxux (5 diagrams each, one thread "
+                              "per event, in the phase-space stage)")
 KERNELS = {2: "me_rec_multi_kernel<2,{T}>", 3: "me_rec_multi_kernel<3,{T}>", 4: "me_rec_kernel<4,{T},{C}>",
            5: "me_gws_kernel<5,{T},{C}>"}
 
@@ -394,10 +404,10 @@ def extras(args, cfg, prec_name, out):
     if args.precision_points and cfg["k"] > 2:
         n = args.precision_points if k < 5 else min(args.precision_points, 100_000)
         out["mixed_vs_fp64"] = precision_study(cfg, n, args.seed + 2)
-    if name in ("c1", "c2", "c5", "pp") and args.integration:
+    if name in ("c1", "c2", "c5", "pp", "ppj") and args.integration:
         out["integration"] = {p: integration(cfg, p, cfg["events"], cfg["iterations"], args.seed + 5)
-                              for p in (("fp64", "mixed") if name in ("c2", "pp") else (prec_name,))}
-        if name == "pp":
+                              for p in (("fp64", "mixed") if name in ("c2", "pp", "ppj") else (prec_name,))}
+        if name in ("pp", "ppj"):
             # the g g channel alone on the same points: the quark channels' share
             gg = integration(dict(cfg, initial_states="gg"), "mixed", cfg["events"], cfg["iterations"],
                              args.seed + 5)

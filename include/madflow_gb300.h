@@ -128,13 +128,17 @@ typedef struct {
   double ptmin, etamax, drmin;
   double q2;
   int newton_rule;
-  /* MF_INITIAL_GG: the g g process alone.  MF_INITIAL_PP (kind 1, two
-   * gluons, i.e. p p > t t~ at leading order): f = weight x [L_gg |M|^2(g g >
-   * t t~) + L_qq |M|^2(q q~ > t t~)], L_qq summed over the initial states
-   * (q, q~) and their mirror images (q~, q), q = d u s c, of the synthetic
-   * quark densities (mf_pdf_xfx_flavour), as madflow sums its processes
-   * (scripts/madflow_exec.py:444-458, utilities.py:25-39).  Other
-   * multiplicities with MF_INITIAL_PP: MF_ERR_UNSUPPORTED. */
+  /* MF_INITIAL_GG: the g g process alone.  MF_INITIAL_PP (kind 1), as
+   * madflow sums the processes of a run, each over its initial states and
+   * their mirror images (scripts/madflow_exec.py:444-458, utilities.py:25-39),
+   * with the synthetic quark densities (mf_pdf_xfx_flavour), q = d u s c:
+   *   two gluons, p p > t t~: f = weight x [L_gg |M|^2(g g > t t~) +
+   *     L_qq |M|^2(q q~ > t t~)], L_qq over (q, q~) and (q~, q);
+   *   three gluons, p p > t t~ j: f = weight x [L_gg |M|^2(g g > t t~ g) +
+   *     the channels q q~ > t t~ g, q g > t t~ q, q~ g > t t~ q~ and their
+   *     mirror images (mf_smatrix_qq_ttxj)], the jet cuts on particle 4
+   *     whatever its flavour.
+   * Other multiplicities with MF_INITIAL_PP: MF_ERR_UNSUPPORTED. */
   int initial_states;
   /* > 0: mf_integrand, mf_vegas_iteration and mf_vegas_events run their
    * events in consecutive slices of at most events_limit events, as
@@ -326,6 +330,18 @@ int mf_pdf_xfx_flavour(int pdg, const double* x, int64_t n, double q2, double* o
  * and bilinears).  No scratch, no handle. */
 int mf_smatrix_qq_ttx(int precision, const double* ps, int64_t n_events, double mdl_MT, double mdl_WT,
                       const double* couplings, int64_t coupling_stride, double* out, void* stream);
+
+/* The light-quark processes of p p > t t~ j at leading order (MadGraph's
+ * u u~ > t t~ g, u g > t t~ u, u~ g > t t~ u~ modules, five diagrams each):
+ * channel 0: q(0) q~(1) > t(2) t~(3) g(4); 1: q(0) g(1) > t t~ q(4);
+ * 2: q~(0) g(1) > t t~ q~(4).  ps [5][4][N], couplings as mf_smatrix (GC_10
+ * and GC_11 are used), out [N] |M|^2 averaged over the initial spins and
+ * colours (1/36, 1/96).  precision MF_PREC_FP64 or MF_PREC_MIXED (FP32
+ * wavefunctions and amplitudes, FP64 propagator denominators).  The gluon
+ * polarisations use madflow's float32 sqrt(1/2) (wavefunctions_flow.py:10).
+ * No scratch, no handle; no counterpart in the reference's tests. */
+int mf_smatrix_qq_ttxj(int precision, int channel, const double* ps, int64_t n_events, double mdl_MT,
+                       double mdl_WT, const double* couplings, int64_t coupling_stride, double* out, void* stream);
 
 /* ---- normalizing-flow importance sampler ---------------------------------
  * No counterpart in the reference (an addition of this implementation, used as

@@ -107,6 +107,7 @@ _SIGS = {
     "mf_pdf_xfx": (c_int, [c_dp, c_int64, c_double, c_dp, c_void_p]),
     "mf_pdf_xfx_flavour": (c_int, [c_int, c_dp, c_int64, c_double, c_dp, c_void_p]),
     "mf_smatrix_qq_ttx": (c_int, [c_int, c_dp, c_int64, c_double, c_double, c_dp, c_int64, c_dp, c_void_p]),
+    "mf_smatrix_qq_ttxj": (c_int, [c_int, c_int, c_dp, c_int64, c_double, c_double, c_dp, c_int64, c_dp, c_void_p]),
     "mf_pq_forward": (c_int, [c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
     "mf_pq_inverse": (c_int, [c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),
     "mf_pq_backward": (c_int, [c_dp, c_dp, c_dp, c_dp, c_int64, c_int, c_int, c_dp, c_dp, c_void_p]),

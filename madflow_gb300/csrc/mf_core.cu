@@ -484,6 +484,20 @@ __global__ void qq_ttx_kernel(int prec, const double* __restrict__ ps, int64_t N
     out[e] = prec == MF_PREC_FP64 ? uux_ttx_me<double>(p, mt, g11sq) : uux_ttx_me<float>(p, mt, g11sq);
   }
 }
+template <class T>
+__global__ void __launch_bounds__(128) qq3_smatrix_kernel(int channel, const double* __restrict__ ps, int64_t N,
+                                                          double mt, double wt, const double* __restrict__ coup,
+                                                          int64_t cstride, double* __restrict__ out) {
+  const T sqh = (T)mf_consts(true).sqh;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double p[5][4];
+    for (int i = 0; i < 5; ++i)
+      for (int c = 0; c < 4; ++c) p[i][c] = ps[((int64_t)i * 4 + c) * N + e];
+    const double* cp = coup + 6 * cstride * e;
+    const cx<double> gc10{cp[0], cp[1]}, gc11{cp[2], cp[3]};
+    out[e] = qq3_me<T>(channel, p, 0, 1, mt, wt, gc10, gc11, sqh);
+  }
+}
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -506,8 +520,10 @@ struct mf_process {
   double* d_state = nullptr; // [state words][cap] first-pass phase-space state
   double* d_pref = nullptr; // [cap]
   double* d_me = nullptr;   // [cap]
-  double* d_extra = nullptr;  // [extra_cap] weights of further channels (p p > t t~)
+  double* d_extra = nullptr;  // [extra_cap] weights of further channels (p p > t t~ (j))
   int64_t extra_cap = 0;
+  double* d_qqin = nullptr;   // [23][qqin_cap] inputs of the light-quark channels of p p > t t~ j
+  int64_t qqin_cap = 0;
   unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
   int64_t event_cap = 0;
   int* d_err = nullptr;     // device error flags of the kernels (bit 0: a tensor-core wait ran out,
@@ -586,6 +602,7 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_err) cudaFree(p->d_err);
   if (p->d_nonfinite) cudaFree(p->d_nonfinite);
   if (p->d_extra) cudaFree(p->d_extra);
+  if (p->d_qqin) cudaFree(p->d_qqin);
   for (cudaEvent_t e : p->tev)
     if (e) cudaEventDestroy(e);
   delete p;
@@ -833,7 +850,7 @@ static int ensure_partials(mf_process* p, size_t n) {
 static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, IterArgs& A) {
   std::memset(&A, 0, sizeof(A));
   if (c->initial_states != MF_INITIAL_GG && c->initial_states != MF_INITIAL_PP) return MF_ERR_ARG;
-  if (c->initial_states == MF_INITIAL_PP && (c->kind != 1 || p->k != 2)) return MF_ERR_UNSUPPORTED;
+  if (c->initial_states == MF_INITIAL_PP && (c->kind != 1 || (p->k != 2 && p->k != 3))) return MF_ERR_UNSUPPORTED;
   A.qq = c->initial_states == MF_INITIAL_PP;
   A.kind = c->kind;
   A.sqrts = c->sqrts;
@@ -974,6 +991,7 @@ static int run_slice(mf_process* p, IterArgs A, int64_t n, const mf_integrand_co
   A.pref = p->d_pref;
   A.me = p->d_me;
   A.extra = A.qq ? p->d_extra : nullptr;
+  A.qqin = A.qq && p->k == 3 ? p->d_qqin : nullptr;
   A.bins = A.x_in ? nullptr : p->d_bins;
   int accum_grid = 8 * 152;
   {
@@ -996,6 +1014,15 @@ static int run_slice(mf_process* p, IterArgs A, int64_t n, const mf_integrand_co
   if (mf_launch_seed(p->k, p->prec, A, p->d_kmin, per_event ? 0 : 1, S(stream))) return last_launch();
   mark(1);
   if (mf_launch_ps(p->k, p->prec, A, S(stream))) return last_launch();
+  if (A.qqin) {
+    const int grid = blocks_for(n, 128);
+    if (p->prec == MF_PREC_FP64)
+      qq3_channels_kernel<double><<<grid, 128, 0, S(stream)>>>(A);
+    else
+      qq3_channels_kernel<float><<<grid, 128, 0, S(stream)>>>(A);
+    st = last_launch();
+    if (st) return st;
+  }
   mark(2);
   if (autotune_wanted(p, n, stream)) {
     st = autotune_me(p, A.prep, n, A.pref, A.me, stream);
@@ -1038,6 +1065,14 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
     st = cuda_status(cudaMalloc(&p->d_extra, sizeof(double) * (size_t)slice));
     if (st) return st;
     p->extra_cap = slice;
+  }
+  if (A.qq && p->k == 3 && p->qqin_cap < slice) {
+    cudaFree(p->d_qqin);
+    p->d_qqin = nullptr;
+    p->qqin_cap = 0;
+    st = cuda_status(cudaMalloc(&p->d_qqin, sizeof(double) * 23 * (size_t)slice));
+    if (st) return st;
+    p->qqin_cap = slice;
   }
   if (!p->d_kmin) {
     st = cuda_status(cudaMalloc(&p->d_kmin, sizeof(int)));
@@ -1133,6 +1168,7 @@ int mf_process_scratch_bytes(const mf_process* p, int64_t* bytes) {
   const int64_t per_event = mf_prep_bytes(p->k, p->prec) + (int64_t)sizeof(double) * (mf_state_words(p->k) + 2) +
                             MF_MAX_DIM;
   int64_t b = p->event_cap * per_event + p->extra_cap * (int64_t)sizeof(double) +
+              p->qqin_cap * 23 * (int64_t)sizeof(double) +
               (int64_t)p->partial_cap * (int64_t)sizeof(double);
   if (p->d_ws) b += mf_ws_bytes(p->k, p->prec);
   *bytes = b;
@@ -1381,6 +1417,19 @@ int mf_smatrix_qq_ttx(int precision, const double* ps, int64_t N, double mt, dou
     return MF_ERR_ARG;
   if (N == 0) return MF_OK;
   qq_ttx_kernel<<<blocks_for(N, 128), 128, 0, S(stream)>>>(precision, ps, N, mt, coup, cstride, out);
+  return last_launch();
+}
+
+int mf_smatrix_qq_ttxj(int precision, int channel, const double* ps, int64_t N, double mt, double wt,
+                       const double* coup, int64_t cstride, double* out, void* stream) {
+  if ((precision != MF_PREC_FP64 && precision != MF_PREC_MIXED) || channel < 0 || channel > 2 || N < 0 ||
+      (N > 0 && (!ps || !coup || !out)) || (cstride != 0 && cstride != 1))
+    return MF_ERR_ARG;
+  if (N == 0) return MF_OK;
+  if (precision == MF_PREC_FP64)
+    qq3_smatrix_kernel<double><<<blocks_for(N, 128), 128, 0, S(stream)>>>(channel, ps, N, mt, wt, coup, cstride, out);
+  else
+    qq3_smatrix_kernel<float><<<blocks_for(N, 128), 128, 0, S(stream)>>>(channel, ps, N, mt, wt, coup, cstride, out);
   return last_launch();
 }
 

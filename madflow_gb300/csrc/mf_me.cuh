@@ -21,6 +21,7 @@
 #pragma once
 #include "mf_me_rec.cuh"
 #include "mf_qq.cuh"
+#include "mf_qq3.cuh"
 
 struct IterArgs {
   const double* div;  // VEGAS grid [ndim][nb+1]
@@ -45,8 +46,10 @@ struct IterArgs {
   int64_t e0, ld;      // the slice's first event in the call (Philox event index, x_in / u_out column)
                        // and the call's event count (x_in / u_out row length)
   double* ps_out;      // optional [N][K+2][4] lab-frame momenta of the passing events (event output)
-  int qq;              // p p > t t~: add the light-quark channels q q~ and q~ q (K = 2 only)
-  double* extra;       // [N] with qq: jac x weight x quark luminosity x |M|^2(q q~ > t t~)
+  int qq;              // p p > t t~ (K = 2) or p p > t t~ j (K = 3): add the light-quark channels
+  double* extra;       // [N] with qq: their weight, jac x weight x luminosity x |M|^2 summed
+  double* qqin;        // [23][N] with qq and K = 3: the event's momenta [5][4] (partonic frame), the
+                       // weight before the luminosities (0: the event failed the cuts), x1, x2
   // pipeline buffers (scratch)
   double* state;            // [4K+16][N] first-pass state (ps_state_words)
   int4* prep;              // [N] per-event records (PrepRec), passing events only
@@ -275,6 +278,20 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
         A.extra[e] = ex;
       }
     }
+    if constexpr (K == 3) {
+      // the light-quark channels of p p > t t~ j: their inputs, for
+      // qq3_channels_kernel
+      if (A.qq) {
+        double* q = A.qqin + e;
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) q[(int64_t)(4 * i + c) * N] = p[i][c];
+        q[(int64_t)20 * N] = ok ? jac * wps : 0.0;
+        q[(int64_t)21 * N] = x1;
+        q[(int64_t)22 * N] = x2;
+      }
+    }
     if (A.ps_out) {
       // madflow's all_ps (com_output=False): lab frame, FP64
       double* q = A.ps_out + (int64_t)e * NPART * 4;
@@ -291,6 +308,55 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
       int4* dst = A.prep + e * NW;
       for (int w = 0; w < NW; ++w) dst[w] = src[w];
     }
+  }
+}
+
+// The light-quark channels of p p > t t~ j, one thread per event (madflow
+// sums the processes of a run, each over its initial states and their
+// mirror images, scripts/madflow_exec.py:444-458, utilities.py:25-39):
+//   extra = w / (x1 x2) [ |M|^2(q q~ > t t~ g)(p1, p2) sum_q q(x1) q~(x2)
+//                        + |M|^2(q q~ > t t~ g)(p2, p1) sum_q q~(x1) q(x2)
+//                        + |M|^2(q g > t t~ q)(p1, p2) Q(x1) g(x2) + mirror
+//                        + |M|^2(q~ g > t t~ q~)(p1, p2) Qb(x1) g(x2) + mirror ],
+// Q, Qb the sums of x f over q = d u s c and their antiquarks.
+template <class T> __global__ void __launch_bounds__(128) qq3_channels_kernel(IterArgs A) {
+  const int64_t N = A.N;
+  const double v = pdf_qcoord(A.pdf, A.q2);
+  const T sqh = (T)mf_consts(A.f32q != 0).sqh;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    const double* q = A.qqin + e;
+    const double w = q[(int64_t)20 * N];
+    double ex = 0.0;
+    if (w != 0.0) {
+      double p[5][4];
+#pragma unroll
+      for (int i = 0; i < 5; ++i)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) p[i][c] = q[(int64_t)(4 * i + c) * N];
+      const double x1 = q[(int64_t)21 * N], x2 = q[(int64_t)22 * N];
+      double qq = 0.0, qbq = 0.0, Q1 = 0.0, Qb1 = 0.0, Q2 = 0.0, Qb2 = 0.0;
+      for (int f = 1; f <= 4; ++f) {
+        const double a = pdf_xfx_fv(A.pdf, f, x1, v), ab = pdf_xfx_fv(A.pdf, f + 4, x1, v);
+        const double b = pdf_xfx_fv(A.pdf, f, x2, v), bb = pdf_xfx_fv(A.pdf, f + 4, x2, v);
+        qq += a * bb;
+        qbq += ab * b;
+        Q1 += a;
+        Qb1 += ab;
+        Q2 += b;
+        Qb2 += bb;
+      }
+      const double g1 = pdf_xfx_fv(A.pdf, 0, x1, v), g2 = pdf_xfx_fv(A.pdf, 0, x2, v);
+      const double lum[6] = {qq, qbq, Q1 * g2, g1 * Q2, Qb1 * g2, g1 * Qb2};
+      double s = 0.0;
+      // one copy of the evaluation, the channel a run-time argument
+#pragma unroll 1
+      for (int j = 0; j < 6; ++j) {
+        const int m = j & 1;
+        s += lum[j] * qq3_me<T>(j >> 1, p, m, 1 - m, A.mt, A.wt, A.gc10, A.gc11, sqh);
+      }
+      ex = w * s / x1 / x2;
+    }
+    A.extra[e] = ex;
   }
 }
 

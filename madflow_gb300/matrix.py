@@ -207,6 +207,71 @@ class Matrix_1_uux_ttx:
         return out
 
 
+class _MatrixQQ3:
+    """A light-quark process of p p > t t~ j (5 diagrams, 32 helicities; one
+    module for the flavours d u s c as MadGraph groups them, initial states
+    and their mirror images).  smatrix(all_ps, mdl_MT, mdl_WT, GC_10, GC_11)
+    with all_ps (N, 5, 4) in MadGraph's particle order (C ABI
+    mf_smatrix_qq_ttxj)."""
+
+    channel = None
+    mirror_initial_states = True
+    nexternal = 5.0
+    ndiags = 5.0
+    ncomb = 32.0
+
+    def __init__(self, precision=None):
+        self.precision = default_precision() if precision is None else precision
+        h = [[a, b, c, d, e] for a in (-1, 1) for b in (-1, 1) for c in (-1, 1) for d in (-1, 1) for e in (-1, 1)]
+        self.helicities = torch.tensor(h, dtype=DTYPE)
+
+    def __str__(self):
+        return self.process_string
+
+    def smatrix(self, all_ps, mdl_MT, mdl_WT, GC_10, GC_11):
+        """|M|^2 averaged over the initial spins and colours."""
+        ps = to_device(all_ps)
+        if ps.dim() != 3 or ps.shape[1] != 5 or ps.shape[2] != 4:
+            raise ValueError(f"all_ps must have shape (N, 5, 4), got {tuple(ps.shape)}")
+        N = ps.shape[0]
+        soa = ps.permute(1, 2, 0).contiguous()
+        coup, stride = MatrixTTNG._couplings(self, N, GC_10, GC_11, None)
+        out = torch.empty(N, dtype=DTYPE, device=device())
+        _lib.call("mf_smatrix_qq_ttxj", int(self.precision), int(self.channel), soa.data_ptr(), N, float(mdl_MT),
+                  float(mdl_WT), coup.data_ptr(), stride, out.data_ptr(), stream_ptr())
+        return out
+
+
+class Matrix_1_uux_ttxg(_MatrixQQ3):
+    """q q~ > t t~ g, particles q, q~, t, t~, g; averaged over 4 spins and 9
+    colours."""
+
+    process_string = "1_uux_ttxg"
+    channel = 0
+    initial_states = [(2, -2), (4, -4), (1, -1), (3, -3)]
+    denominator = 36.0
+
+
+class Matrix_1_ug_ttxu(_MatrixQQ3):
+    """q g > t t~ q, particles q, g, t, t~, q; averaged over 4 spins and 24
+    colours."""
+
+    process_string = "1_ug_ttxu"
+    channel = 1
+    initial_states = [(2, 21), (4, 21), (1, 21), (3, 21)]
+    denominator = 96.0
+
+
+class Matrix_1_uxg_ttxux(_MatrixQQ3):
+    """q~ g > t t~ q~, particles q~, g, t, t~, q~; averaged over 4 spins and
+    24 colours."""
+
+    process_string = "1_uxg_ttxux"
+    channel = 2
+    initial_states = [(-2, 21), (-4, 21), (-1, 21), (-3, 21)]
+    denominator = 96.0
+
+
 def smatrix_multi(batches, mdl_MT, mdl_WT, GC_10, GC_11, GC_12=None):
     """|M|^2 of several processes in one persistent launch (C ABI
     ``mf_smatrix_multi``): batches is a list of (matrix, all_ps) with distinct

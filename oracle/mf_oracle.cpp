@@ -774,6 +774,107 @@ extern "C" void orc_smatrix_uux_ttx(const double* p, int64_t N, const double* pr
   for (int64_t e = 0; e < N; ++e) out[e] = smatrix_uux_ttx<double>(p + 16 * e, prm);
 }
 
+// ---------------------------------------------------------------------------
+// p p > t t~ j at leading order: the channels with one light-quark line,
+// q q~ > t t~ g, q g > t t~ q and q~ g > t t~ q~ (MadGraph's u u~ > t t~ g,
+// u g > t t~ u, u~ g > t t~ u~ modules of a p p > t t~ j run; no instance in
+// the reference's tests).  Five diagrams each, with the HELAS wavefunctions
+// of wavefunctions_flow.py and the ALOHA routines above.  The light line runs
+// from its i-type end I (ixxxxx: incoming quark or outgoing antiquark) to its
+// o-type end O (oxxxxx: outgoing quark or incoming antiquark), the top line
+// from the t~ (I_tb) to the t (O_t):
+//   a1: gluon on the light line at I      colour (T^b T^a)_{O I} T^b_{t tb}
+//   a2: gluon on the light line at O      colour (T^a T^b)_{O I} T^b_{t tb}
+//   a3: gluon on the top line at the t    colour T^b_{O I} (T^a T^b)_{t tb}
+//   a4: gluon on the top line at the t~   colour T^b_{O I} (T^b T^a)_{t tb}
+//   a5: three-gluon vertex               colour f^{bac} T^b_{O I} T^c_{t tb}
+// The colour matrix of these tensors, CM[d][d'] = sum over colours of
+// C_d conj(C_d') (Gell-Mann generators, T^a = lambda^a / 2), is
+//   [8/3 -1/3 7/3 -2/3 -3i; -1/3 8/3 -2/3 7/3 3i; 7/3 -2/3 8/3 -1/3 -3i;
+//    -2/3 7/3 -1/3 8/3 3i; 3i -3i 3i -3i 6],
+// with a5 = FFV1_0(I_tb, O_t, VVV1P0_1(V_light, G, GC_10), GC_11) as it
+// stands (the sum agrees with an evaluation of the textbook Feynman rules,
+// test).  Averages: 1/36 for q q~, 1/96 for q g and q~ g.
+static const double kQQ3CmRe[5][5] = {{8.0 / 3, -1.0 / 3, 7.0 / 3, -2.0 / 3, 0},
+                                      {-1.0 / 3, 8.0 / 3, -2.0 / 3, 7.0 / 3, 0},
+                                      {7.0 / 3, -2.0 / 3, 8.0 / 3, -1.0 / 3, 0},
+                                      {-2.0 / 3, 7.0 / 3, -1.0 / 3, 8.0 / 3, 0},
+                                      {0, 0, 0, 0, 6}};
+static const double kQQ3CmIm[5][5] = {{0, 0, 0, 0, -3}, {0, 0, 0, 0, 3}, {0, 0, 0, 0, -3}, {0, 0, 0, 0, 3},
+                                      {3, -3, 3, -3, 0}};
+
+template <class R>
+static R qq3_helicity_sum(const WF<R> I[2], const WF<R> O[2], const WF<R> Ot[2], const WF<R> Itb[2],
+                          const WF<R> G[2], Cx<R> gc10, Cx<R> gc11, R mt, R wt) {
+  R tot = R(0);
+  for (int hi = 0; hi < 2; ++hi)
+    for (int ho = 0; ho < 2; ++ho) {
+      WF<R> vs0;
+      FFV1P0_3<R>(I[hi], O[ho], gc11, R(0), R(0), vs0);
+      for (int hg = 0; hg < 2; ++hg) {
+        WF<R> i1, o2, vs1, vs2, vs5;
+        FFV1_2<R>(I[hi], G[hg], gc11, R(0), R(0), i1);
+        FFV1P0_3<R>(i1, O[ho], gc11, R(0), R(0), vs1);
+        FFV1_1<R>(O[ho], G[hg], gc11, R(0), R(0), o2);
+        FFV1P0_3<R>(I[hi], o2, gc11, R(0), R(0), vs2);
+        VVV1P0_1<R>(vs0, G[hg], gc10, R(0), R(0), vs5);
+        for (int ht = 0; ht < 2; ++ht)
+          for (int hb = 0; hb < 2; ++hb) {
+            WF<R> ot3, itb4;
+            FFV1_1<R>(Ot[ht], G[hg], gc11, mt, wt, ot3);
+            FFV1_2<R>(Itb[hb], G[hg], gc11, mt, wt, itb4);
+            Cx<R> a[5] = {FFV1_0<R>(Itb[hb], Ot[ht], vs1, gc11), FFV1_0<R>(Itb[hb], Ot[ht], vs2, gc11),
+                          FFV1_0<R>(Itb[hb], ot3, vs0, gc11), FFV1_0<R>(itb4, Ot[ht], vs0, gc11),
+                          FFV1_0<R>(Itb[hb], Ot[ht], vs5, gc11)};
+            for (int d = 0; d < 5; ++d) {
+              Cx<R> z;
+              for (int e = 0; e < 5; ++e) z += Cx<R>{R(kQQ3CmRe[d][e]), R(kQQ3CmIm[d][e])} * conj(a[e]);
+              tot += (a[d] * z).re;
+            }
+          }
+      }
+    }
+  return tot;
+}
+
+// channel 0: q(p0) q~(p1) > t(p2) t~(p3) g(p4); 1: q(p0) g(p1) > t t~ q(p4);
+// 2: q~(p0) g(p1) > t t~ q~(p4).  prm: mt, wt, GC_10 (re, im), GC_11 (re, im).
+template <class R> static R smatrix_qq3(int channel, const R* p, const double* prm, double sqh_d) {
+  const R mt = R(prm[0]), wt = R(prm[1]), sqh = R(sqh_d);
+  const Cx<R> gc10{R(prm[2]), R(prm[3])}, gc11{R(prm[4]), R(prm[5])};
+  WF<R> I[2], O[2], Ot[2], Itb[2], G[2];
+  for (int b = 0; b < 2; ++b) {
+    const R h = b ? R(1) : R(-1);
+    oxxxxx<R>(p + 8, mt, h, R(1), Ot[b]);
+    ixxxxx<R>(p + 12, mt, h, R(-1), Itb[b]);
+    if (channel == 0) {
+      ixxxxx<R>(p + 0, R(0), h, R(1), I[b]);
+      oxxxxx<R>(p + 4, R(0), h, R(-1), O[b]);
+      vxxxxx<R>(p + 16, R(0), h, R(1), sqh, G[b]);
+    } else if (channel == 1) {
+      ixxxxx<R>(p + 0, R(0), h, R(1), I[b]);
+      oxxxxx<R>(p + 16, R(0), h, R(1), O[b]);
+      vxxxxx<R>(p + 4, R(0), h, R(-1), sqh, G[b]);
+    } else {
+      oxxxxx<R>(p + 0, R(0), h, R(-1), O[b]);
+      ixxxxx<R>(p + 16, R(0), h, R(-1), I[b]);
+      vxxxxx<R>(p + 4, R(0), h, R(-1), sqh, G[b]);
+    }
+  }
+  const R tot = qq3_helicity_sum<R>(I, O, Ot, Itb, G, gc10, gc11, mt, wt);
+  return tot / R(channel == 0 ? 36.0 : 96.0);
+}
+
+// f32q: madflow's float32-rounded sqrt(1/2) in the gluon polarisations
+// (wavefunctions_flow.py:10), else the exact value
+extern "C" int orc_smatrix_qq3(int channel, const double* p, int64_t N, const double* prm, int f32q, double* out) {
+  if (channel < 0 || channel > 2) return 1;
+  const double sqh = ref_consts(f32q != 0).sqh;
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < N; ++e) out[e] = smatrix_qq3<double>(channel, p + 20 * e, prm, sqh);
+  return 0;
+}
+
 extern "C" void orc_pdf_table(double* table /*[kNQ][kNX]*/, double* lx0, double* dlx, double* lq0, double* dlq) {
   double A = pdf_A();
   *lx0 = std::log(1e-6); *dlx = (0.0 - *lx0) / (kNX - 1);
@@ -1048,6 +1149,54 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
     for (size_t i = 0; i < idx.size(); ++i) {
       int64_t e = idx[i];
       f[e] += meq[i] * (lumq[e] / x1[e] / x2[e]) * w[e];
+    }
+  }
+  if (initial_states == 1 && cfg.k == 3 && !idx.empty()) {
+    // p p > t t~ j: q q~ > t t~ g, q g > t t~ q, q~ g > t t~ q~ and their
+    // mirror images (the initial states swapped), q = d u s c
+    const size_t M = idx.size();
+    std::vector<double> swapped(pp);
+    for (size_t i = 0; i < M; ++i)
+      for (int c = 0; c < 4; ++c) std::swap(swapped[20 * i + c], swapped[20 * i + 4 + c]);
+    double prm3[6] = {cfg.mt, cfg.wt, -gs, 0.0, 0.0, gs};
+    std::vector<double> me[6];
+    for (int ch = 0; ch < 3; ++ch) {
+      me[2 * ch].resize(M);
+      me[2 * ch + 1].resize(M);
+      orc_smatrix_qq3(ch, pp.data(), (int64_t)M, prm3, 1, me[2 * ch].data());
+      orc_smatrix_qq3(ch, swapped.data(), (int64_t)M, prm3, 1, me[2 * ch + 1].data());
+    }
+    std::vector<double> q1((size_t)N, 0.0), qb1((size_t)N, 0.0), t((size_t)N);
+    for (int q = 1; q <= 4; ++q) {
+      orc_pdf_xfx_flavour(q, x1.data(), N, q2, t.data());
+      for (int64_t e = 0; e < N; ++e) q1[e] += t[e];
+      orc_pdf_xfx_flavour(-q, x1.data(), N, q2, t.data());
+      for (int64_t e = 0; e < N; ++e) qb1[e] += t[e];
+    }
+    double lq[6];
+    for (size_t i = 0; i < M; ++i) {
+      const int64_t e = idx[i];
+      double s_qq = 0.0, s_qbq = 0.0, q_2 = 0.0, qb_2 = 0.0;
+      for (int q = 1; q <= 4; ++q) {
+        double a, b, c, d;
+        orc_pdf_xfx_flavour(q, &x1[e], 1, q2, &a);
+        orc_pdf_xfx_flavour(-q, &x2[e], 1, q2, &b);
+        orc_pdf_xfx_flavour(-q, &x1[e], 1, q2, &c);
+        orc_pdf_xfx_flavour(q, &x2[e], 1, q2, &d);
+        s_qq += a * b;
+        s_qbq += c * d;
+        q_2 += d;
+        qb_2 += b;
+      }
+      lq[0] = s_qq;               // q(x1) q~(x2)
+      lq[1] = s_qbq;              // q~(x1) q(x2): q q~ mirrored
+      lq[2] = q1[e] * g2[e];      // q(x1) g(x2)
+      lq[3] = g1[e] * q_2;        // g(x1) q(x2)
+      lq[4] = qb1[e] * g2[e];     // q~(x1) g(x2)
+      lq[5] = g1[e] * qb_2;       // g(x1) q~(x2)
+      double sum = 0.0;
+      for (int c = 0; c < 6; ++c) sum += me[c][i] * lq[c];
+      f[e] += sum / x1[e] / x2[e] * w[e];
     }
   }
 }

@@ -291,6 +291,23 @@ def smatrix_uux_ttx(all_ps, mdl_MT, mdl_WT, GC_11):
     return out
 
 
+QQ3_CHANNELS = {"uux_ttxg": 0, "ug_ttxu": 1, "uxg_ttxux": 2}
+
+
+def smatrix_qq3(channel, all_ps, mdl_MT, mdl_WT, GC_10, GC_11, f32q=True):
+    """|M|^2 (averaged) of the light-quark channels of p p > t t~ j for
+    momenta (N, 5, 4): "uux_ttxg" (q q~ > t t~ g), "ug_ttxu" (q g > t t~ q),
+    "uxg_ttxux" (q~ g > t t~ q~), MadGraph's particle order.  f32q: madflow's
+    float32 sqrt(1/2) in the gluon polarisations."""
+    p = _c64(all_ps)
+    out = np.empty(p.shape[0])
+    prm = _c64([mdl_MT, mdl_WT, complex(GC_10).real, complex(GC_10).imag, complex(GC_11).real, complex(GC_11).imag])
+    if lib().orc_smatrix_qq3(ctypes.c_int(QQ3_CHANNELS[channel]), _p(p), ctypes.c_int64(p.shape[0]), _p(prm),
+                             ctypes.c_int(int(bool(f32q))), _p(out)):
+        raise ValueError(channel)
+    return out
+
+
 def pdf_xfx(x, q2):
     x = _c64(x)
     out = np.empty_like(x)
