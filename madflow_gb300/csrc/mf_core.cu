@@ -488,14 +488,19 @@ template <class T>
 __global__ void __launch_bounds__(128) qq3_smatrix_kernel(int channel, const double* __restrict__ ps, int64_t N,
                                                           double mt, double wt, const double* __restrict__ coup,
                                                           int64_t cstride, double* __restrict__ out) {
+  // a group of four lanes per event (mfqq3)
+  const int lane = threadIdx.x & 3, base = (threadIdx.x & 31) & ~3;
+  const unsigned mask = 0xFu << base;
   const T sqh = (T)mf_consts(true).sqh;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * (blockDim.x >> 2);
+  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2; e < N; e += stride) {
     double p[5][4];
     for (int i = 0; i < 5; ++i)
       for (int c = 0; c < 4; ++c) p[i][c] = ps[((int64_t)i * 4 + c) * N + e];
     const double* cp = coup + 6 * cstride * e;
     const cx<double> gc10{cp[0], cp[1]}, gc11{cp[2], cp[3]};
-    out[e] = qq3_me<T>(channel, p, 0, 1, mt, wt, gc10, gc11, sqh);
+    const double r = qq3_me_group<T>(channel, p, mt, wt, gc10, gc11, sqh, mask, lane, base);
+    if (lane == 0) out[e] = r;
   }
 }
 }  // namespace
@@ -1015,7 +1020,7 @@ static int run_slice(mf_process* p, IterArgs A, int64_t n, const mf_integrand_co
   mark(1);
   if (mf_launch_ps(p->k, p->prec, A, S(stream))) return last_launch();
   if (A.qqin) {
-    const int grid = blocks_for(n, 128);
+    const int grid = blocks_for(4 * n, 128);  // four lanes per event
     if (p->prec == MF_PREC_FP64)
       qq3_channels_kernel<double><<<grid, 128, 0, S(stream)>>>(A);
     else
@@ -1427,9 +1432,11 @@ int mf_smatrix_qq_ttxj(int precision, int channel, const double* ps, int64_t N, 
     return MF_ERR_ARG;
   if (N == 0) return MF_OK;
   if (precision == MF_PREC_FP64)
-    qq3_smatrix_kernel<double><<<blocks_for(N, 128), 128, 0, S(stream)>>>(channel, ps, N, mt, wt, coup, cstride, out);
+    qq3_smatrix_kernel<double><<<blocks_for(4 * N, 128), 128, 0, S(stream)>>>(channel, ps, N, mt, wt, coup, cstride,
+                                                                               out);
   else
-    qq3_smatrix_kernel<float><<<blocks_for(N, 128), 128, 0, S(stream)>>>(channel, ps, N, mt, wt, coup, cstride, out);
+    qq3_smatrix_kernel<float><<<blocks_for(4 * N, 128), 128, 0, S(stream)>>>(channel, ps, N, mt, wt, coup, cstride,
+                                                                              out);
   return last_launch();
 }
 

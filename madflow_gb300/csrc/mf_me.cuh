@@ -320,10 +320,15 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
 //                        + |M|^2(q~ g > t t~ q~)(p1, p2) Qb(x1) g(x2) + mirror ],
 // Q, Qb the sums of x f over q = d u s c and their antiquarks.
 template <class T> __global__ void __launch_bounds__(128) qq3_channels_kernel(IterArgs A) {
+  // a group of four lanes per event (mfqq3): lane l also takes the
+  // densities of flavour l + 1
   const int64_t N = A.N;
+  const int lane = threadIdx.x & 3, base = (threadIdx.x & 31) & ~3;
+  const unsigned mask = 0xFu << base;
   const double v = pdf_qcoord(A.pdf, A.q2);
   const T sqh = (T)mf_consts(A.f32q != 0).sqh;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * (blockDim.x >> 2);
+  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2; e < N; e += stride) {
     const double* q = A.qqin + e;
     const double w = q[(int64_t)20 * N];
     double ex = 0.0;
@@ -334,29 +339,17 @@ template <class T> __global__ void __launch_bounds__(128) qq3_channels_kernel(It
 #pragma unroll
         for (int c = 0; c < 4; ++c) p[i][c] = q[(int64_t)(4 * i + c) * N];
       const double x1 = q[(int64_t)21 * N], x2 = q[(int64_t)22 * N];
-      double qq = 0.0, qbq = 0.0, Q1 = 0.0, Qb1 = 0.0, Q2 = 0.0, Qb2 = 0.0;
-      for (int f = 1; f <= 4; ++f) {
-        const double a = pdf_xfx_fv(A.pdf, f, x1, v), ab = pdf_xfx_fv(A.pdf, f + 4, x1, v);
-        const double b = pdf_xfx_fv(A.pdf, f, x2, v), bb = pdf_xfx_fv(A.pdf, f + 4, x2, v);
-        qq += a * bb;
-        qbq += ab * b;
-        Q1 += a;
-        Qb1 += ab;
-        Q2 += b;
-        Qb2 += bb;
-      }
+      const int f = lane + 1;
+      const double a = pdf_xfx_fv(A.pdf, f, x1, v), ab = pdf_xfx_fv(A.pdf, f + 4, x1, v);
+      const double b = pdf_xfx_fv(A.pdf, f, x2, v), bb = pdf_xfx_fv(A.pdf, f + 4, x2, v);
       const double g1 = pdf_xfx_fv(A.pdf, 0, x1, v), g2 = pdf_xfx_fv(A.pdf, 0, x2, v);
-      const double lum[6] = {qq, qbq, Q1 * g2, g1 * Q2, Qb1 * g2, g1 * Qb2};
-      double s = 0.0;
-      // one copy of the evaluation, the channel a run-time argument
-#pragma unroll 1
-      for (int j = 0; j < 6; ++j) {
-        const int m = j & 1;
-        s += lum[j] * qq3_me<T>(j >> 1, p, m, 1 - m, A.mt, A.wt, A.gc10, A.gc11, sqh);
-      }
-      ex = w * s / x1 / x2;
+      using mfqq3::group_sum;
+      const double Q1 = group_sum(a, mask), Qb1 = group_sum(ab, mask);
+      const double Q2 = group_sum(b, mask), Qb2 = group_sum(bb, mask);
+      const double lum[6] = {group_sum(a * bb, mask), group_sum(ab * b, mask), Q1 * g2, g1 * Q2, Qb1 * g2, g1 * Qb2};
+      ex = w * qq3_lum_sum<T>(p, lum, A.mt, A.wt, A.gc10, A.gc11, sqh, mask, lane, base) / x1 / x2;
     }
-    A.extra[e] = ex;
+    if (lane == 0) A.extra[e] = ex;
   }
 }
 

@@ -152,61 +152,154 @@ template <class T> MF_D QW<T> external(int kind, const double* p, double m, T h,
 
 }  // namespace mfqq3
 
-// |M|^2 averaged over the initial spins and colours of one light-quark
-// channel: channel 0 q(p[0]) q~(p[1]) > t(p[2]) t~(p[3]) g(p[4]); 1 q(p[0])
-// g(p[1]) > t t~ q(p[4]); 2 q~(p[0]) g(p[1]) > t t~ q~(p[4]).  a, b: the
-// indices of the momenta of particles 0 and 1 in p (0, 1, or 1, 0 for the
-// mirrored initial state).  gc10, gc11: GC_10, GC_11; sqh: sqrt(1/2) of the
-// gluon polarisations.
+// ---- four lanes per event --------------------------------------------------
+// The 16 helicity configurations of a channel with non-zero amplitudes (the
+// massless quark pair has one chirality: its two spinors share nhel * nsf)
+// are the products of 4 light-line states (gluon helicity x chirality) and 4
+// top-line states (t x t~ helicities).  Lane l of an event's group of four
+// builds the light-line currents of light state l and the top-line
+// bilinears of top state l; the 16 products are formed after the light
+// currents pass round the group by shuffles, so nothing is computed twice.
+// The top-line objects depend on the gluon's momentum only, so they serve
+// two of an event's six channel evaluations at once.
+namespace mfqq3 {
+
+template <class T> struct TopSide {
+  W4<T> c;        // Itb^T S(e_mu) Ot: diagrams a1, a2, a5
+  W4<T> d3[2];    // Itb^T S(e_mu) FFV1_1(Ot, G): a3, per gluon helicity
+  W4<T> d4[2];    // FFV1_2(Itb, G)^T S(e_mu) Ot: a4
+};
+template <class T> struct LightSide {
+  W4<T> vs0, vs1, vs2, vs5;
+};
+
+// kG: 4 outgoing gluon, 5 incoming gluon
 template <class T>
-MF_D double qq3_me(int channel, const double (*p)[4], int a, int b, double mt, double wt, cx<double> gc10,
-                   cx<double> gc11, T sqh) {
-  using namespace mfqq3;
-  // external kinds of (I, O, G) per channel, and their momenta
-  const int kI = channel == 2 ? 1 : 0, kO = channel == 0 ? 3 : (channel == 1 ? 2 : 3), kG = channel == 0 ? 4 : 5;
-  const double* pI = channel == 2 ? p[4] : p[a];
-  const double* pO = channel == 0 ? p[b] : (channel == 1 ? p[4] : p[a]);
-  const double* pG = channel == 0 ? p[4] : p[b];
-  QW<T> Ot[2], Itb[2];
+MF_D TopSide<T> top_side(const double (*p)[4], const double* pG, int kG, int lane, double mt, double wt,
+                         cx<double> gc11, T sqh) {
+  const QW<T> Ot = external<T>(2, p[2], mt, (lane >> 1) ? T(1) : T(-1), sqh);
+  const QW<T> Itb = external<T>(1, p[3], mt, (lane & 1) ? T(1) : T(-1), sqh);
+  TopSide<T> t;
+  t.c = bilinear(Itb.w, Ot.w);
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    Ot[h] = external<T>(2, p[2], mt, h ? T(1) : T(-1), sqh);
-    Itb[h] = external<T>(1, p[3], mt, h ? T(1) : T(-1), sqh);
-  }
-  T tot = T(0);
   for (int hg = 0; hg < 2; ++hg) {
     const QW<T> G = external<T>(kG, pG, 0.0, hg ? T(1) : T(-1), sqh);
-    QW<T> ot3[2], itb4[2];
+    t.d3[hg] = bilinear(Itb.w, ffv1_1(Ot, G, gc11, mt, wt).w);
+    t.d4[hg] = bilinear(ffv1_2(Itb, G, gc11, mt, wt).w, Ot.w);
+  }
+  return t;
+}
+
+// light state l: gluon helicity l >> 1, chirality nh = +-1 (l & 1) of the
+// quark pair, nhel = nh * nsf for each of the two
+template <class T>
+MF_D LightSide<T> light_side(int kI, const double* pI, int kO, const double* pO, int kG, const double* pG, int lane,
+                             cx<double> gc10, cx<double> gc11, T sqh) {
+  const T nh = (lane & 1) ? T(1) : T(-1);
+  const T nsfI = kI == 0 ? T(1) : T(-1), nsfO = kO == 2 ? T(1) : T(-1);
+  const QW<T> G = external<T>(kG, pG, 0.0, (lane >> 1) ? T(1) : T(-1), sqh);
+  const QW<T> I = external<T>(kI, pI, 0.0, nh * nsfI, sqh);
+  const QW<T> O = external<T>(kO, pO, 0.0, nh * nsfO, sqh);
+  LightSide<T> l;
+  const QW<T> vs0 = ffv1p0_3(I, O, gc11);
+  l.vs0 = vs0.w;
+  l.vs1 = ffv1p0_3(ffv1_2(I, G, gc11, 0.0, 0.0), O, gc11).w;
+  l.vs2 = ffv1p0_3(I, ffv1_1(O, G, gc11, 0.0, 0.0), gc11).w;
+  l.vs5 = vvv1p0_1(vs0, G, gc10).w;
+  return l;
+}
+
+template <class T> MF_D cx<T> shfl(unsigned mask, cx<T> v, int src) {
+  return cx<T>{__shfl_sync(mask, v.re, src), __shfl_sync(mask, v.im, src)};
+}
+template <class T> MF_D W4<T> shfl(unsigned mask, const W4<T>& v, int src) {
+  W4<T> r;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      ot3[h] = ffv1_1(Ot[h], G, gc11, mt, wt);
-      itb4[h] = ffv1_2(Itb[h], G, gc11, mt, wt);
-    }
-    for (int hio = 0; hio < 4; ++hio) {
-      const QW<T> I = external<T>(kI, pI, 0.0, (hio & 1) ? T(1) : T(-1), sqh);
-      const QW<T> O = external<T>(kO, pO, 0.0, (hio & 2) ? T(1) : T(-1), sqh);
-      const QW<T> vs0 = ffv1p0_3(I, O, gc11);
-      // massless quarks: the pairs of opposite chirality give an exactly
-      // zero current (and zero amplitudes)
-      if (is_zero(vs0.w)) continue;
-      const QW<T> vs1 = ffv1p0_3(ffv1_2(I, G, gc11, 0.0, 0.0), O, gc11);
-      const QW<T> vs2 = ffv1p0_3(I, ffv1_1(O, G, gc11, 0.0, 0.0), gc11);
-      const QW<T> vs5 = vvv1p0_1(vs0, G, gc10);
+  for (int k = 0; k < 4; ++k) r.v[k] = shfl(mask, v.v[k], src);
+  return r;
+}
+
+// This lane's share of the colour- and helicity-summed |M|^2 (without the
+// factor |GC_11|^2 and the average): top state `lane` times the four light
+// states of the group.  mask: the group's four lanes; base: its first lane.
+template <class T>
+MF_D T group_products(const TopSide<T>& t, const LightSide<T>& l, unsigned mask, int base) {
+  T tot = T(0);
 #pragma unroll
-      for (int ht = 0; ht < 2; ++ht)
-#pragma unroll
-        for (int hb = 0; hb < 2; ++hb) {
-          const W4<T> c = bilinear(Itb[hb].w, Ot[ht].w);
-          const cx<T> a1 = contract(c, vs1.w), a2 = contract(c, vs2.w), a5 = contract(c, vs5.w);
-          const cx<T> a3 = contract(bilinear(Itb[hb].w, ot3[ht].w), vs0.w);
-          const cx<T> a4 = contract(bilinear(itb4[hb].w, Ot[ht].w), vs0.w);
-          const cx<T> s1 = a1 + a2 + a3 + a4, s3 = a1 + a2 - a3 - a4;
-          const cx<T> s2 = a1 - a2 + a3 - a4 + cx<T>{T(-2) * a5.im, T(2) * a5.re};
-          tot += abs2(s1) + T(1.5) * abs2(s2) + abs2(s3) * T(1.0 / 6.0);
-        }
+  for (int j = 0; j < 4; ++j) {
+    const W4<T> vs0 = shfl(mask, l.vs0, base + j), vs1 = shfl(mask, l.vs1, base + j);
+    const W4<T> vs2 = shfl(mask, l.vs2, base + j), vs5 = shfl(mask, l.vs5, base + j);
+    const cx<T> a1 = contract(t.c, vs1), a2 = contract(t.c, vs2), a5 = contract(t.c, vs5);
+    const cx<T> a3 = contract(t.d3[j >> 1], vs0), a4 = contract(t.d4[j >> 1], vs0);
+    const cx<T> s1 = a1 + a2 + a3 + a4, s3 = a1 + a2 - a3 - a4;
+    const cx<T> s2 = a1 - a2 + a3 - a4 + cx<T>{T(-2) * a5.im, T(2) * a5.re};
+    tot += abs2(s1) + T(1.5) * abs2(s2) + abs2(s3) * T(1.0 / 6.0);
+  }
+  return tot;
+}
+
+// external kinds and momenta of (I, O, G) of a channel; a, b: the indices
+// of the momenta of particles 0 and 1 (1, 0 for the mirrored initial state)
+MF_D void channel_legs(int channel, int a, int b, int& kI, int& iI, int& kO, int& iO, int& kG, int& iG) {
+  if (channel == 0) {        // q q~ > t t~ g
+    kI = 0; iI = a; kO = 3; iO = b; kG = 4; iG = 4;
+  } else if (channel == 1) { // q g > t t~ q
+    kI = 0; iI = a; kO = 2; iO = 4; kG = 5; iG = b;
+  } else {                   // q~ g > t t~ q~
+    kI = 1; iI = 4; kO = 3; iO = a; kG = 5; iG = b;
+  }
+}
+
+template <class T> MF_D T group_sum(T v, unsigned mask) {
+  v += __shfl_xor_sync(mask, v, 1);
+  v += __shfl_xor_sync(mask, v, 2);
+  return v;
+}
+
+}  // namespace mfqq3
+
+// |M|^2 of one channel (C ABI mf_smatrix_qq_ttxj), evaluated by a group of
+// four lanes; every lane of the group returns the value.  channel 0
+// q(p[0]) q~(p[1]) > t(p[2]) t~(p[3]) g(p[4]); 1 q(p[0]) g(p[1]) > t t~
+// q(p[4]); 2 q~(p[0]) g(p[1]) > t t~ q~(p[4]); averaged over the initial
+// spins and colours.  All four lanes of the group (mask) must call it.
+template <class T>
+MF_D double qq3_me_group(int channel, const double (*p)[4], double mt, double wt, cx<double> gc10, cx<double> gc11,
+                         T sqh, unsigned mask, int lane, int base) {
+  using namespace mfqq3;
+  int kI, iI, kO, iO, kG, iG;
+  channel_legs(channel, 0, 1, kI, iI, kO, iO, kG, iG);
+  const TopSide<T> t = top_side<T>(p, p[iG], kG, lane, mt, wt, gc11, sqh);
+  const LightSide<T> l = light_side<T>(kI, p[iI], kO, p[iO], kG, p[iG], lane, gc10, gc11, sqh);
+  const T tot = group_sum(group_products(t, l, mask, base), mask);
+  const double g11sq = gc11.re * gc11.re + gc11.im * gc11.im;  // the FFV1_0 factor -i GC_11
+  return (double)tot * g11sq / (channel == 0 ? 36.0 : 96.0);
+}
+
+// The six channel evaluations of an event of p p > t t~ j weighted by their
+// luminosities lum[6] (q q~, q~ q, q g, g q, q~ g, g q~), summed; the three
+// gluon momenta (p[4]; p[1]; p[0]) each serve two evaluations' top lines.
+template <class T>
+MF_D double qq3_lum_sum(const double (*p)[4], const double* lum, double mt, double wt, cx<double> gc10,
+                        cx<double> gc11, T sqh, unsigned mask, int lane, int base) {
+  using namespace mfqq3;
+  double s = 0.0;
+#pragma unroll 1
+  for (int g = 0; g < 3; ++g) {
+    // g = 0: q q~ and its mirror (gluon p[4]); 1: q g, q~ g (gluon p[1]);
+    // 2: g q, g q~ (gluon p[0])
+    const int kG = g == 0 ? 4 : 5, iG = g == 0 ? 4 : (g == 1 ? 1 : 0);
+    const TopSide<T> t = top_side<T>(p, p[iG], kG, lane, mt, wt, gc11, sqh);
+#pragma unroll 1
+    for (int u = 0; u < 2; ++u) {
+      const int channel = g == 0 ? 0 : 1 + u, m = g == 0 ? u : g - 1;
+      int kI, iI, kO, iO, kGc, iGc;
+      channel_legs(channel, m, 1 - m, kI, iI, kO, iO, kGc, iGc);
+      const LightSide<T> l = light_side<T>(kI, p[iI], kO, p[iO], kGc, p[iGc], lane, gc10, gc11, sqh);
+      const int j = g == 0 ? u : (channel == 1 ? 2 + m : 4 + m);
+      s += lum[j] / (channel == 0 ? 36.0 : 96.0) * (double)group_products(t, l, mask, base);
     }
   }
-  // every amplitude carries the FFV1_0 factor -i GC_11
   const double g11sq = gc11.re * gc11.re + gc11.im * gc11.im;
-  return (double)tot * g11sq / (channel == 0 ? 36.0 : 96.0);
+  return group_sum(s, mask) * g11sq;
 }

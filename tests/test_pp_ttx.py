@@ -167,7 +167,7 @@ def test_gpu_pp_unsupported_combinations(cuda):
     from madflow_gb300.vegas import FusedIntegrand
 
     with pytest.raises(_lib.MadflowError):
-        FusedIntegrand(3, kind=1, sqrts=13000.0, precision=0, initial_states="pp")(torch.rand((10, 14)))
+        FusedIntegrand(4, kind=1, sqrts=13000.0, precision=0, initial_states="pp")(torch.rand((10, 18)))
     with pytest.raises(_lib.MadflowError):
         FusedIntegrand(2, kind=0, sqrts=1000.0, precision=0, initial_states="pp")(torch.rand((10, 8)))
     # event output names one initial state per event: one channel only
