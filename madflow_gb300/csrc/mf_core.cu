@@ -499,7 +499,10 @@ __global__ void __launch_bounds__(128) qq3_smatrix_kernel(int channel, const dou
       for (int c = 0; c < 4; ++c) p[i][c] = ps[((int64_t)i * 4 + c) * N + e];
     const double* cp = coup + 6 * cstride * e;
     const cx<double> gc10{cp[0], cp[1]}, gc11{cp[2], cp[3]};
-    const double r = qq3_me_group<T>(channel, p, mt, wt, gc10, gc11, sqh, mask, lane, base);
+    // the evaluation of the channel in qq3_weighted_sum's order (q q~, q~ q, q g, q~ g, ...)
+    double w[6] = {0, 0, 0, 0, 0, 0};
+    w[channel == 0 ? 0 : channel + 1] = 1.0;
+    const double r = qq3_weighted_sum<T>(p, w, mt, wt, gc10, gc11, sqh, mask, lane, base);
     if (lane == 0) out[e] = r;
   }
 }

@@ -317,7 +317,7 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
 //   extra = w / (x1 x2) [ |M|^2(q q~ > t t~ g)(p1, p2) sum_q q(x1) q~(x2)
 //                        + |M|^2(q q~ > t t~ g)(p2, p1) sum_q q~(x1) q(x2)
 //                        + |M|^2(q g > t t~ q)(p1, p2) Q(x1) g(x2) + mirror
-//                        + |M|^2(q~ g > t t~ q~)(p1, p2) Qb(x1) g(x2) + mirror ],
+//                        + |M|^2(q~ g > t t~ q~)(p1, p2) Qb(x1) g(x2) + mirror ]
 // Q, Qb the sums of x f over q = d u s c and their antiquarks.
 template <class T> __global__ void __launch_bounds__(128) qq3_channels_kernel(IterArgs A) {
   // a group of four lanes per event (mfqq3): lane l also takes the
@@ -346,8 +346,9 @@ template <class T> __global__ void __launch_bounds__(128) qq3_channels_kernel(It
       using mfqq3::group_sum;
       const double Q1 = group_sum(a, mask), Qb1 = group_sum(ab, mask);
       const double Q2 = group_sum(b, mask), Qb2 = group_sum(bb, mask);
-      const double lum[6] = {group_sum(a * bb, mask), group_sum(ab * b, mask), Q1 * g2, g1 * Q2, Qb1 * g2, g1 * Qb2};
-      ex = w * qq3_lum_sum<T>(p, lum, A.mt, A.wt, A.gc10, A.gc11, sqh, mask, lane, base) / x1 / x2;
+      // the evaluations' order of qq3_weighted_sum: q q~, q~ q, q g, q~ g, g q, g q~
+      const double lum[6] = {group_sum(a * bb, mask), group_sum(ab * b, mask), Q1 * g2, Qb1 * g2, g1 * Q2, g1 * Qb2};
+      ex = w * qq3_weighted_sum<T>(p, lum, A.mt, A.wt, A.gc10, A.gc11, sqh, mask, lane, base) / x1 / x2;
     }
     if (lane == 0) A.extra[e] = ex;
   }

@@ -29,52 +29,44 @@
 
 namespace mfqq3 {
 
-// a wavefunction and its HELAS slot momentum (+p for an outgoing particle,
-// -p for an incoming one, as ixxxxx / oxxxxx / vxxxxx store it)
+// a wavefunction and its HELAS slot momentum in T (+p for an outgoing
+// particle, -p for an incoming one, as ixxxxx / oxxxxx / vxxxxx store it)
 template <class T> struct QW {
   W4<T> w;
-  double q[4];
+  T q[4];
 };
 
-// i * coup / (P^2 - M^2 + i M W), the factor of the ALOHA off-shell routines
-template <class T> MF_D cx<T> offshell_factor(const double* P, double M, double W, cx<double> coup) {
-  const double p2 = P[0] * P[0] - P[1] * P[1] - P[2] * P[2] - P[3] * P[3];
-  const double dr = p2 - M * M, di = M * W;
-  const double inv = 1.0 / (dr * dr + di * di);
-  const double re = (coup.re * dr + coup.im * di) * inv, im = (coup.im * dr - coup.re * di) * inv;
-  return cx<T>{(T)(-im), (T)re};
-}
-
-template <class T> MF_D void add_q(const QW<T>& a, const QW<T>& b, double* q) {
+template <class T> MF_D void add_q(const QW<T>& a, const QW<T>& b, T* q) {
 #pragma unroll
   for (int k = 0; k < 4; ++k) q[k] = a.q[k] + b.q[k];
 }
 
+// The off-shell routines take their factor c = i * coup / (P^2 - M^2 + i M W)
+// ready-made (the invariants P^2 are FP64, computed once per event).
+
 // FFV1_1: the o-type line continued past the vertex with V,
 // c (S(Q) + M) S(V) F2 with Q the summed slot momentum
-template <class T> MF_D QW<T> ffv1_1(const QW<T>& F2, const QW<T>& V, cx<double> coup, double M, double W) {
+template <class T> MF_D QW<T> ffv1_1(const QW<T>& F2, const QW<T>& V, cx<T> c, T M) {
   QW<T> r;
   add_q(F2, V, r.q);
   W4<T> y = w4zero<T>();
   sv_add(V.w, F2.w, y);
-  const T Q[4] = {(T)r.q[0], (T)r.q[1], (T)r.q[2], (T)r.q[3]};
-  r.w = topprop(Q, (T)M, offshell_factor<T>(r.q, M, W, coup), y);
+  r.w = topprop(r.q, M, c, y);
   return r;
 }
 
 // FFV1_2: the i-type line continued past the vertex with V,
 // c (S(-Q)^T + M) S(V)^T F1
-template <class T> MF_D QW<T> ffv1_2(const QW<T>& F1, const QW<T>& V, cx<double> coup, double M, double W) {
+template <class T> MF_D QW<T> ffv1_2(const QW<T>& F1, const QW<T>& V, cx<T> c, T M) {
   QW<T> r;
   add_q(F1, V, r.q);
   const W4<T> y = sandwich_row(F1.w, V.w);
   W4<T> P;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) P.v[k] = cx<T>{(T)(-r.q[k]), T(0)};
+  for (int k = 0; k < 4; ++k) P.v[k] = cx<T>{-r.q[k], T(0)};
   const W4<T> z = sandwich_row(y, P);
-  const cx<T> c = offshell_factor<T>(r.q, M, W, coup);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) r.w.v[k] = c * (z.v[k] + (T)M * y.v[k]);
+  for (int k = 0; k < 4; ++k) r.w.v[k] = c * (z.v[k] + M * y.v[k]);
   return r;
 }
 
@@ -87,36 +79,32 @@ template <class T> MF_D W4<T> bilinear(const W4<T>& F1, const W4<T>& F2) {
 }
 
 // FFV1P0_3: the massless gluon current of a fermion pair
-template <class T> MF_D QW<T> ffv1p0_3(const QW<T>& F1, const QW<T>& F2, cx<double> coup) {
+template <class T> MF_D QW<T> ffv1p0_3(const QW<T>& F1, const QW<T>& F2, cx<T> c) {
   QW<T> r;
   add_q(F1, F2, r.q);
-  const W4<T> c = bilinear(F1.w, F2.w);
-  const cx<T> f = offshell_factor<T>(r.q, 0.0, 0.0, coup);
-  r.w.v[0] = f * c.v[0];
+  const W4<T> b = bilinear(F1.w, F2.w);
+  r.w.v[0] = c * b.v[0];
 #pragma unroll
-  for (int mu = 1; mu < 4; ++mu) r.w.v[mu] = -(f * c.v[mu]);
+  for (int mu = 1; mu < 4; ++mu) r.w.v[mu] = -(c * b.v[mu]);
   return r;
 }
 
 // VVV1P0_1: the massless gluon of the three-gluon vertex of V2 and V3
-template <class T> MF_D QW<T> vvv1p0_1(const QW<T>& V2, const QW<T>& V3, cx<double> coup) {
+template <class T> MF_D QW<T> vvv1p0_1(const QW<T>& V2, const QW<T>& V3, cx<T> c) {
   QW<T> r;
   add_q(V2, V3, r.q);
-  T P1[4], P2[4], P3[4];
+  const T* P2 = V2.q;
+  const T* P3 = V3.q;
+  T P1[4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    P1[k] = (T)(-r.q[k]);
-    P2[k] = (T)V2.q[k];
-    P3[k] = (T)V3.q[k];
-  }
+  for (int k = 0; k < 4; ++k) P1[k] = -r.q[k];
   const W4<T>& a = V2.w;
   const W4<T>& b = V3.w;
   const cx<T> v23 = mdot(b, a);
   const cx<T> c2 = mdotq(b, P2[0] - P1[0], P2[1] - P1[1], P2[2] - P1[2], P2[3] - P1[3]);
   const cx<T> c3 = mdotq(a, P1[0] - P3[0], P1[1] - P3[1], P1[2] - P3[2], P1[3] - P3[3]);
-  const cx<T> f = offshell_factor<T>(r.q, 0.0, 0.0, coup);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) r.w.v[k] = f * ((P3[k] - P2[k]) * v23 + a.v[k] * c2 + b.v[k] * c3);
+  for (int k = 0; k < 4; ++k) r.w.v[k] = c * ((P3[k] - P2[k]) * v23 + a.v[k] * c2 + b.v[k] * c3);
   return r;
 }
 
@@ -125,13 +113,6 @@ template <class T> MF_D cx<T> contract(const W4<T>& c, const W4<T>& V) {
 }
 template <class T> MF_D T abs2(cx<T> z) { return z.re * z.re + z.im * z.im; }
 
-template <class T> MF_D bool is_zero(const W4<T>& w) {
-  bool z = true;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) z = z && w.v[k].re == T(0) && w.v[k].im == T(0);
-  return z;
-}
-
 template <class T> MF_D QW<T> external(int kind, const double* p, double m, T h, T sqh) {
   // kind 0: ixxxxx incoming quark, 1: ixxxxx outgoing antiquark, 2: oxxxxx
   // outgoing quark, 3: oxxxxx incoming antiquark, 4: vxxxxx outgoing gluon,
@@ -139,18 +120,122 @@ template <class T> MF_D QW<T> external(int kind, const double* p, double m, T h,
   const T pt[4] = {(T)p[0], (T)p[1], (T)p[2], (T)p[3]};
   // nsf / nsv: +1 for an incoming fermion, an outgoing fermion or an
   // outgoing vector, -1 for antifermions and an incoming vector
-  const double ns = (kind == 0 || kind == 2 || kind == 4) ? 1.0 : -1.0;
-  const double out = (kind == 1 || kind == 2 || kind == 4) ? 1.0 : -1.0;
+  const T ns = (kind == 0 || kind == 2 || kind == 4) ? T(1) : T(-1);
+  const T out = (kind == 1 || kind == 2 || kind == 4) ? T(1) : T(-1);
   QW<T> r;
-  if (kind <= 1) r.w = ixxxxx<T>(pt, (T)m, h, (T)ns);
-  else if (kind <= 3) r.w = oxxxxx<T>(pt, (T)m, h, (T)ns);
-  else r.w = vxxxxx<T>(pt, (T)m, h, (T)ns, sqh);
+  if (kind <= 1) r.w = ixxxxx<T>(pt, (T)m, h, ns);
+  else if (kind <= 3) r.w = oxxxxx<T>(pt, (T)m, h, ns);
+  else r.w = vxxxxx<T>(pt, (T)m, h, ns, sqh);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) r.q[k] = out * p[k];
+  for (int k = 0; k < 4; ++k) r.q[k] = out * pt[k];
   return r;
 }
 
-}  // namespace mfqq3
+template <class T> MF_D cx<T> shfl(unsigned mask, cx<T> v, int src) {
+  return cx<T>{__shfl_sync(mask, v.re, src), __shfl_sync(mask, v.im, src)};
+}
+template <class T> MF_D W4<T> shfl(unsigned mask, const W4<T>& v, int src) {
+  W4<T> r;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) r.v[k] = shfl(mask, v.v[k], src);
+  return r;
+}
+template <class T> MF_D T group_sum(T v, unsigned mask) {
+  v += __shfl_xor_sync(mask, v, 1);
+  v += __shfl_xor_sync(mask, v, 2);
+  return v;
+}
+
+// external kinds and momentum indices of (I, O, G) of a channel; a, b: the
+// indices of the momenta of particles 0 and 1 (1, 0 for the mirrored
+// initial state)
+MF_D void channel_legs(int channel, int a, int b, int& kI, int& iI, int& kO, int& iO, int& kG, int& iG) {
+  if (channel == 0) {        // q q~ > t t~ g
+    kI = 0; iI = a; kO = 3; iO = b; kG = 4; iG = 4;
+  } else if (channel == 1) { // q g > t t~ q
+    kI = 0; iI = a; kO = 2; iO = 4; kG = 5; iG = b;
+  } else {                   // q~ g > t t~ q~
+    kI = 1; iI = 4; kO = 3; iO = a; kG = 5; iG = b;
+  }
+}
+MF_D double out_sign(int kind) { return (kind == 1 || kind == 2 || kind == 4) ? 1.0 : -1.0; }
+
+// ---- the propagator factors of an event ---------------------------------------
+// 1 / (P^2 - M^2 + i M W) of the event's 25 off-shell lines, P^2 in FP64
+// (massless differences such as (p_q - p_g)^2 cancel in FP32):
+//   0        the gluon of the top pair, P = p0 + p1 - p4
+//   1 + 2g   the top after the gluon of set g, P = p2 + q_g
+//   2 + 2g   the anti-top before it, P = p3 + q_g
+//   7 + 3j   evaluation j: the light line at I with the gluon, P = q_I + q_G
+//   8 + 3j   at O with the gluon, P = q_O + q_G
+//   9 + 3j   the light-line gluon, P = q_I + q_O
+// q: slot momenta; gluon sets g = 0 (p4 outgoing), 1 (p1 incoming), 2 (p0
+// incoming); evaluations j = 2g + u in the order of qq3_lum_sum.
+constexpr int kQQ3Factors = 25;
+
+MF_D void eval_channel(int j, int& channel, int& m) {
+  const int g = j >> 1, u = j & 1;
+  channel = g == 0 ? 0 : 1 + u;
+  m = g == 0 ? u : g - 1;
+}
+
+template <class T>
+MF_D cx<T> factor(int k, const double (*p)[4], double mt, double wt) {
+  double P[4];
+  double M = 0.0, W = 0.0;
+  if (k == 0) {
+    // the light side's momenta, as the off-shell routines sum them (equal to
+    // p2 + p3 up to the phase space's energy conservation)
+    for (int c = 0; c < 4; ++c) P[c] = p[0][c] + p[1][c] - p[4][c];
+  } else if (k < 7) {
+    const int g = (k - 1) >> 1, top = (k - 1) & 1;
+    const int ig = g == 0 ? 4 : 2 - g;
+    const double sg = g == 0 ? 1.0 : -1.0;
+    for (int c = 0; c < 4; ++c) P[c] = p[2 + top][c] + sg * p[ig][c];
+    M = mt;
+    W = wt;
+  } else {
+    const int j = (k - 7) / 3, r = (k - 7) % 3;
+    int channel, m, kI, iI, kO, iO, kG, iG;
+    eval_channel(j, channel, m);
+    channel_legs(channel, m, 1 - m, kI, iI, kO, iO, kG, iG);
+    const double sI = out_sign(kI), sO = out_sign(kO), sG = out_sign(kG);
+    for (int c = 0; c < 4; ++c)
+      P[c] = r == 0 ? sI * p[iI][c] + sG * p[iG][c]
+                    : (r == 1 ? sO * p[iO][c] + sG * p[iG][c] : sI * p[iI][c] + sO * p[iO][c]);
+  }
+  const double d = P[0] * P[0] - P[1] * P[1] - P[2] * P[2] - P[3] * P[3] - M * M;
+  // 1 / (d + i M W) in T
+  const T dr = (T)d, di = (T)(M * W);
+  const T inv = T(1) / (dr * dr + di * di);
+  return cx<T>{dr * inv, -di * inv};
+}
+
+// all 25 factors in every lane of the group: lane l computes those with
+// index = l (mod 4), the group exchanges them
+template <class T> struct Factors {
+  cx<T> r[kQQ3Factors];
+};
+template <class T>
+MF_D Factors<T> event_factors(const double (*p)[4], double mt, double wt, unsigned mask, int lane, int base) {
+  cx<T> mine[(kQQ3Factors + 3) / 4];
+#pragma unroll
+  for (int i = 0; i < (kQQ3Factors + 3) / 4; ++i) {
+    const int k = 4 * i + lane;
+    mine[i] = k < kQQ3Factors ? factor<T>(k, p, mt, wt) : cx<T>{T(0), T(0)};
+  }
+  Factors<T> f;
+#pragma unroll
+  for (int k = 0; k < kQQ3Factors; ++k) f.r[k] = shfl(mask, mine[k >> 2], base + (k & 3));
+  return f;
+}
+
+// i * coup * r
+template <class T> MF_D cx<T> ic(cx<double> coup, cx<T> r) {
+  const cx<T> c{(T)coup.re, (T)coup.im};
+  const cx<T> z = c * r;
+  return cx<T>{-z.im, z.re};
+}
 
 // ---- four lanes per event --------------------------------------------------
 // The 16 helicity configurations of a channel with non-zero amplitudes (the
@@ -162,8 +247,6 @@ template <class T> MF_D QW<T> external(int kind, const double* p, double m, T h,
 // currents pass round the group by shuffles, so nothing is computed twice.
 // The top-line objects depend on the gluon's momentum only, so they serve
 // two of an event's six channel evaluations at once.
-namespace mfqq3 {
-
 template <class T> struct TopSide {
   W4<T> c;        // Itb^T S(e_mu) Ot: diagrams a1, a2, a5
   W4<T> d3[2];    // Itb^T S(e_mu) FFV1_1(Ot, G): a3, per gluon helicity
@@ -173,50 +256,46 @@ template <class T> struct LightSide {
   W4<T> vs0, vs1, vs2, vs5;
 };
 
-// kG: 4 outgoing gluon, 5 incoming gluon
+// gluon set g (0: p4 outgoing, 1: p1 incoming, 2: p0 incoming)
 template <class T>
-MF_D TopSide<T> top_side(const double (*p)[4], const double* pG, int kG, int lane, double mt, double wt,
-                         cx<double> gc11, T sqh) {
+MF_D TopSide<T> top_side(const double (*p)[4], int g, int lane, double mt, cx<double> gc11, const Factors<T>& F,
+                         T sqh) {
   const QW<T> Ot = external<T>(2, p[2], mt, (lane >> 1) ? T(1) : T(-1), sqh);
   const QW<T> Itb = external<T>(1, p[3], mt, (lane & 1) ? T(1) : T(-1), sqh);
+  const int kG = g == 0 ? 4 : 5, iG = g == 0 ? 4 : 2 - g;
+  const cx<T> ct = ic<T>(gc11, F.r[1 + 2 * g]), cb = ic<T>(gc11, F.r[2 + 2 * g]);
   TopSide<T> t;
   t.c = bilinear(Itb.w, Ot.w);
 #pragma unroll
   for (int hg = 0; hg < 2; ++hg) {
-    const QW<T> G = external<T>(kG, pG, 0.0, hg ? T(1) : T(-1), sqh);
-    t.d3[hg] = bilinear(Itb.w, ffv1_1(Ot, G, gc11, mt, wt).w);
-    t.d4[hg] = bilinear(ffv1_2(Itb, G, gc11, mt, wt).w, Ot.w);
+    const QW<T> G = external<T>(kG, p[iG], 0.0, hg ? T(1) : T(-1), sqh);
+    t.d3[hg] = bilinear(Itb.w, ffv1_1(Ot, G, ct, (T)mt).w);
+    t.d4[hg] = bilinear(ffv1_2(Itb, G, cb, (T)mt).w, Ot.w);
   }
   return t;
 }
 
-// light state l: gluon helicity l >> 1, chirality nh = +-1 (l & 1) of the
-// quark pair, nhel = nh * nsf for each of the two
+// evaluation j's light state l: gluon helicity l >> 1, chirality nh = +-1
+// (l & 1) of the quark pair, nhel = nh * nsf for each of the two
 template <class T>
-MF_D LightSide<T> light_side(int kI, const double* pI, int kO, const double* pO, int kG, const double* pG, int lane,
-                             cx<double> gc10, cx<double> gc11, T sqh) {
+MF_D LightSide<T> light_side(const double (*p)[4], int j, int lane, cx<double> gc10, cx<double> gc11,
+                             const Factors<T>& F, T sqh) {
+  int channel, m, kI, iI, kO, iO, kG, iG;
+  eval_channel(j, channel, m);
+  channel_legs(channel, m, 1 - m, kI, iI, kO, iO, kG, iG);
   const T nh = (lane & 1) ? T(1) : T(-1);
   const T nsfI = kI == 0 ? T(1) : T(-1), nsfO = kO == 2 ? T(1) : T(-1);
-  const QW<T> G = external<T>(kG, pG, 0.0, (lane >> 1) ? T(1) : T(-1), sqh);
-  const QW<T> I = external<T>(kI, pI, 0.0, nh * nsfI, sqh);
-  const QW<T> O = external<T>(kO, pO, 0.0, nh * nsfO, sqh);
+  const QW<T> G = external<T>(kG, p[iG], 0.0, (lane >> 1) ? T(1) : T(-1), sqh);
+  const QW<T> I = external<T>(kI, p[iI], 0.0, nh * nsfI, sqh);
+  const QW<T> O = external<T>(kO, p[iO], 0.0, nh * nsfO, sqh);
+  const cx<T> cs = ic<T>(gc11, F.r[0]);
   LightSide<T> l;
-  const QW<T> vs0 = ffv1p0_3(I, O, gc11);
+  const QW<T> vs0 = ffv1p0_3(I, O, ic<T>(gc11, F.r[9 + 3 * j]));
   l.vs0 = vs0.w;
-  l.vs1 = ffv1p0_3(ffv1_2(I, G, gc11, 0.0, 0.0), O, gc11).w;
-  l.vs2 = ffv1p0_3(I, ffv1_1(O, G, gc11, 0.0, 0.0), gc11).w;
-  l.vs5 = vvv1p0_1(vs0, G, gc10).w;
+  l.vs1 = ffv1p0_3(ffv1_2(I, G, ic<T>(gc11, F.r[7 + 3 * j]), T(0)), O, cs).w;
+  l.vs2 = ffv1p0_3(I, ffv1_1(O, G, ic<T>(gc11, F.r[8 + 3 * j]), T(0)), cs).w;
+  l.vs5 = vvv1p0_1(vs0, G, ic<T>(gc10, F.r[0])).w;
   return l;
-}
-
-template <class T> MF_D cx<T> shfl(unsigned mask, cx<T> v, int src) {
-  return cx<T>{__shfl_sync(mask, v.re, src), __shfl_sync(mask, v.im, src)};
-}
-template <class T> MF_D W4<T> shfl(unsigned mask, const W4<T>& v, int src) {
-  W4<T> r;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) r.v[k] = shfl(mask, v.v[k], src);
-  return r;
 }
 
 // This lane's share of the colour- and helicity-summed |M|^2 (without the
@@ -238,68 +317,34 @@ MF_D T group_products(const TopSide<T>& t, const LightSide<T>& l, unsigned mask,
   return tot;
 }
 
-// external kinds and momenta of (I, O, G) of a channel; a, b: the indices
-// of the momenta of particles 0 and 1 (1, 0 for the mirrored initial state)
-MF_D void channel_legs(int channel, int a, int b, int& kI, int& iI, int& kO, int& iO, int& kG, int& iG) {
-  if (channel == 0) {        // q q~ > t t~ g
-    kI = 0; iI = a; kO = 3; iO = b; kG = 4; iG = 4;
-  } else if (channel == 1) { // q g > t t~ q
-    kI = 0; iI = a; kO = 2; iO = 4; kG = 5; iG = b;
-  } else {                   // q~ g > t t~ q~
-    kI = 1; iI = 4; kO = 3; iO = a; kG = 5; iG = b;
-  }
-}
-
-template <class T> MF_D T group_sum(T v, unsigned mask) {
-  v += __shfl_xor_sync(mask, v, 1);
-  v += __shfl_xor_sync(mask, v, 2);
-  return v;
-}
-
 }  // namespace mfqq3
 
-// |M|^2 of one channel (C ABI mf_smatrix_qq_ttxj), evaluated by a group of
-// four lanes; every lane of the group returns the value.  channel 0
-// q(p[0]) q~(p[1]) > t(p[2]) t~(p[3]) g(p[4]); 1 q(p[0]) g(p[1]) > t t~
-// q(p[4]); 2 q~(p[0]) g(p[1]) > t t~ q~(p[4]); averaged over the initial
-// spins and colours.  All four lanes of the group (mask) must call it.
+// The six channel evaluations j of an event of p p > t t~ j, |M|^2 averaged
+// over the initial spins and colours, in the order q q~, q~ q (mirrored),
+// q g, q~ g, g q, g q~; weighted by w[j] and summed (w[j] = 1 for one j
+// alone gives that evaluation).  Evaluated by a group of four lanes (mask,
+// lane 0..3, base: the group's first lane); every lane of the group must
+// call it and every lane returns the sum.  p: [5][4] momenta in FP64.
 template <class T>
-MF_D double qq3_me_group(int channel, const double (*p)[4], double mt, double wt, cx<double> gc10, cx<double> gc11,
-                         T sqh, unsigned mask, int lane, int base) {
+MF_D double qq3_weighted_sum(const double (*p)[4], const double* w, double mt, double wt, cx<double> gc10,
+                             cx<double> gc11, T sqh, unsigned mask, int lane, int base) {
   using namespace mfqq3;
-  int kI, iI, kO, iO, kG, iG;
-  channel_legs(channel, 0, 1, kI, iI, kO, iO, kG, iG);
-  const TopSide<T> t = top_side<T>(p, p[iG], kG, lane, mt, wt, gc11, sqh);
-  const LightSide<T> l = light_side<T>(kI, p[iI], kO, p[iO], kG, p[iG], lane, gc10, gc11, sqh);
-  const T tot = group_sum(group_products(t, l, mask, base), mask);
-  const double g11sq = gc11.re * gc11.re + gc11.im * gc11.im;  // the FFV1_0 factor -i GC_11
-  return (double)tot * g11sq / (channel == 0 ? 36.0 : 96.0);
-}
-
-// The six channel evaluations of an event of p p > t t~ j weighted by their
-// luminosities lum[6] (q q~, q~ q, q g, g q, q~ g, g q~), summed; the three
-// gluon momenta (p[4]; p[1]; p[0]) each serve two evaluations' top lines.
-template <class T>
-MF_D double qq3_lum_sum(const double (*p)[4], const double* lum, double mt, double wt, cx<double> gc10,
-                        cx<double> gc11, T sqh, unsigned mask, int lane, int base) {
-  using namespace mfqq3;
+  const Factors<T> F = event_factors<T>(p, mt, wt, mask, lane, base);
   double s = 0.0;
 #pragma unroll 1
   for (int g = 0; g < 3; ++g) {
-    // g = 0: q q~ and its mirror (gluon p[4]); 1: q g, q~ g (gluon p[1]);
-    // 2: g q, g q~ (gluon p[0])
-    const int kG = g == 0 ? 4 : 5, iG = g == 0 ? 4 : (g == 1 ? 1 : 0);
-    const TopSide<T> t = top_side<T>(p, p[iG], kG, lane, mt, wt, gc11, sqh);
+    if (w[2 * g] == 0.0 && w[2 * g + 1] == 0.0) continue;  // uniform across the group
+    const TopSide<T> t = top_side<T>(p, g, lane, mt, gc11, F, sqh);
 #pragma unroll 1
     for (int u = 0; u < 2; ++u) {
-      const int channel = g == 0 ? 0 : 1 + u, m = g == 0 ? u : g - 1;
-      int kI, iI, kO, iO, kGc, iGc;
-      channel_legs(channel, m, 1 - m, kI, iI, kO, iO, kGc, iGc);
-      const LightSide<T> l = light_side<T>(kI, p[iI], kO, p[iO], kGc, p[iGc], lane, gc10, gc11, sqh);
-      const int j = g == 0 ? u : (channel == 1 ? 2 + m : 4 + m);
-      s += lum[j] / (channel == 0 ? 36.0 : 96.0) * (double)group_products(t, l, mask, base);
+      const int j = 2 * g + u;
+      if (w[j] == 0.0) continue;
+      int channel, m;
+      eval_channel(j, channel, m);
+      const LightSide<T> l = light_side<T>(p, j, lane, gc10, gc11, F, sqh);
+      s += w[j] / (channel == 0 ? 36.0 : 96.0) * (double)group_products(t, l, mask, base);
     }
   }
-  const double g11sq = gc11.re * gc11.re + gc11.im * gc11.im;
+  const double g11sq = gc11.re * gc11.re + gc11.im * gc11.im;  // the FFV1_0 factor -i GC_11
   return group_sum(s, mask) * g11sq;
 }
