@@ -311,17 +311,15 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
   }
 }
 
-// The light-quark channels of p p > t t~ j, one thread per event (madflow
-// sums the processes of a run, each over its initial states and their
-// mirror images, scripts/madflow_exec.py:444-458, utilities.py:25-39):
+// The light-quark channels of p p > t t~ j, a group of four lanes per event
+// (madflow sums the processes of a run, each over its initial states and
+// their mirror images, scripts/madflow_exec.py:444-458, utilities.py:25-39):
 //   extra = w / (x1 x2) [ |M|^2(q q~ > t t~ g)(p1, p2) sum_q q(x1) q~(x2)
 //                        + |M|^2(q q~ > t t~ g)(p2, p1) sum_q q~(x1) q(x2)
 //                        + |M|^2(q g > t t~ q)(p1, p2) Q(x1) g(x2) + mirror
 //                        + |M|^2(q~ g > t t~ q~)(p1, p2) Qb(x1) g(x2) + mirror ]
 // Q, Qb the sums of x f over q = d u s c and their antiquarks.
 template <class T> __global__ void __launch_bounds__(128) qq3_channels_kernel(IterArgs A) {
-  // a group of four lanes per event (mfqq3): lane l also takes the
-  // densities of flavour l + 1
   const int64_t N = A.N;
   const int lane = threadIdx.x & 3, base = (threadIdx.x & 31) & ~3;
   const unsigned mask = 0xFu << base;
@@ -339,15 +337,27 @@ template <class T> __global__ void __launch_bounds__(128) qq3_channels_kernel(It
 #pragma unroll
         for (int c = 0; c < 4; ++c) p[i][c] = q[(int64_t)(4 * i + c) * N];
       const double x1 = q[(int64_t)21 * N], x2 = q[(int64_t)22 * N];
-      const int f = lane + 1;
-      const double a = pdf_xfx_fv(A.pdf, f, x1, v), ab = pdf_xfx_fv(A.pdf, f + 4, x1, v);
-      const double b = pdf_xfx_fv(A.pdf, f, x2, v), bb = pdf_xfx_fv(A.pdf, f + 4, x2, v);
-      const double g1 = pdf_xfx_fv(A.pdf, 0, x1, v), g2 = pdf_xfx_fv(A.pdf, 0, x2, v);
+      // densities: lanes 0, 1 at x1, lanes 2, 3 at x2; even lanes d u and
+      // their antiquarks (and the gluon), odd lanes s c and theirs
       using mfqq3::group_sum;
-      const double Q1 = group_sum(a, mask), Qb1 = group_sum(ab, mask);
-      const double Q2 = group_sum(b, mask), Qb2 = group_sum(bb, mask);
+      const PdfStencil st = pdf_stencil(A.pdf, lane < 2 ? x1 : x2, v);
+      const int f0 = (lane & 1) ? 3 : 1;
+      const double qa = pdf_xfx_st(A.pdf, f0, st), qb = pdf_xfx_st(A.pdf, f0 + 1, st);
+      const double qab = pdf_xfx_st(A.pdf, f0 + 4, st), qbb = pdf_xfx_st(A.pdf, f0 + 5, st);
+      double g = 0.0;
+      if (!(lane & 1)) g = pdf_xfx_st(A.pdf, 0, st);
+      const double g1 = __shfl_sync(mask, g, base), g2 = __shfl_sync(mask, g, base + 2);
+      // lanes 0, 1 pair their flavours at x1 with the same flavours at x2
+      const int partner = base + ((lane + 2) & 3);
+      const double ra = __shfl_sync(mask, qa, partner), rb = __shfl_sync(mask, qb, partner);
+      const double rab = __shfl_sync(mask, qab, partner), rbb = __shfl_sync(mask, qbb, partner);
+      const bool at1 = lane < 2;
+      const double qq = group_sum(at1 ? qa * rab + qb * rbb : 0.0, mask);
+      const double qbq = group_sum(at1 ? qab * ra + qbb * rb : 0.0, mask);
+      const double Q1 = group_sum(at1 ? qa + qb : 0.0, mask), Qb1 = group_sum(at1 ? qab + qbb : 0.0, mask);
+      const double Q2 = group_sum(at1 ? 0.0 : qa + qb, mask), Qb2 = group_sum(at1 ? 0.0 : qab + qbb, mask);
       // the evaluations' order of qq3_weighted_sum: q q~, q~ q, q g, q~ g, g q, g q~
-      const double lum[6] = {group_sum(a * bb, mask), group_sum(ab * b, mask), Q1 * g2, Qb1 * g2, g1 * Q2, g1 * Qb2};
+      const double lum[6] = {qq, qbq, Q1 * g2, Qb1 * g2, g1 * Q2, g1 * Qb2};
       ex = w * qq3_weighted_sum<T>(p, lum, A.mt, A.wt, A.gc10, A.gc11, sqh, mask, lane, base) / x1 / x2;
     }
     if (lane == 0) A.extra[e] = ex;

@@ -317,6 +317,35 @@ MF_HD double pdf_xfx_fv(const PdfTable& T, int f, double x, double v) {
   }
   return s > 0.0 ? s : 0.0;  // the cubic can overshoot below zero next to x = 1
 }
+// The same interpolation split in two, for several flavours at one x: the
+// stencil of x (clamped nodes, weights) once, then 16 products per flavour
+// in pdf_xfx_fv's order (so the values are the same to the bit).
+struct PdfStencil {
+  int xi[4], qi[4];
+  double wu[4], wv[4];
+};
+MF_HD PdfStencil pdf_stencil(const PdfTable& T, double x, double v) {
+  PdfStencil st;
+  const double u = (log(x) - T.lx0) / T.dlx;
+  const int iu = (int)floor(u), iv = (int)floor(v);
+  const double fu = u - iu, fv = v - iv;
+  for (int b = -1; b <= 2; ++b) {
+    st.wu[b + 1] = keys_w<double>(fu - b);
+    st.xi[b + 1] = min(max(iu + b, 0), T.nx - 1);
+  }
+  for (int a = -1; a <= 2; ++a) {
+    st.wv[a + 1] = keys_w<double>(fv - a);
+    st.qi[a + 1] = min(max(iv + a, 0), T.nq - 1);
+  }
+  return st;
+}
+MF_HD double pdf_xfx_st(const PdfTable& T, int f, const PdfStencil& st) {
+  const double* tab = T.tab + (int64_t)f * T.nq * T.nx;
+  double s = 0.0;
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b) s += st.wv[a] * st.wu[b] * tab[st.qi[a] * T.nx + st.xi[b]];
+  return s > 0.0 ? s : 0.0;
+}
 // the gluon
 MF_HD double pdf_xfx_v(const PdfTable& T, double x, double v) { return pdf_xfx_fv(T, 0, x, v); }
 MF_HD double pdf_xfx(const PdfTable& T, double x, double q2) { return pdf_xfx_v(T, x, pdf_qcoord(T, q2)); }

@@ -113,19 +113,18 @@ template <class T> MF_D cx<T> contract(const W4<T>& c, const W4<T>& V) {
 }
 template <class T> MF_D T abs2(cx<T> z) { return z.re * z.re + z.im * z.im; }
 
-template <class T> MF_D QW<T> external(int kind, const double* p, double m, T h, T sqh) {
+template <class T> MF_D QW<T> external(int kind, const T* pt, T m, T h, T sqh) {
   // kind 0: ixxxxx incoming quark, 1: ixxxxx outgoing antiquark, 2: oxxxxx
   // outgoing quark, 3: oxxxxx incoming antiquark, 4: vxxxxx outgoing gluon,
-  // 5: vxxxxx incoming gluon
-  const T pt[4] = {(T)p[0], (T)p[1], (T)p[2], (T)p[3]};
+  // 5: vxxxxx incoming gluon; pt the momentum in T
   // nsf / nsv: +1 for an incoming fermion, an outgoing fermion or an
   // outgoing vector, -1 for antifermions and an incoming vector
   const T ns = (kind == 0 || kind == 2 || kind == 4) ? T(1) : T(-1);
   const T out = (kind == 1 || kind == 2 || kind == 4) ? T(1) : T(-1);
   QW<T> r;
-  if (kind <= 1) r.w = ixxxxx<T>(pt, (T)m, h, ns);
-  else if (kind <= 3) r.w = oxxxxx<T>(pt, (T)m, h, ns);
-  else r.w = vxxxxx<T>(pt, (T)m, h, ns, sqh);
+  if (kind <= 1) r.w = ixxxxx<T>(pt, m, h, ns);
+  else if (kind <= 3) r.w = oxxxxx<T>(pt, m, h, ns);
+  else r.w = vxxxxx<T>(pt, m, h, ns, sqh);
 #pragma unroll
   for (int k = 0; k < 4; ++k) r.q[k] = out * pt[k];
   return r;
@@ -258,8 +257,7 @@ template <class T> struct LightSide {
 
 // gluon set g (0: p4 outgoing, 1: p1 incoming, 2: p0 incoming)
 template <class T>
-MF_D TopSide<T> top_side(const double (*p)[4], int g, int lane, double mt, cx<double> gc11, const Factors<T>& F,
-                         T sqh) {
+MF_D TopSide<T> top_side(const T (*p)[4], int g, int lane, T mt, cx<double> gc11, const Factors<T>& F, T sqh) {
   const QW<T> Ot = external<T>(2, p[2], mt, (lane >> 1) ? T(1) : T(-1), sqh);
   const QW<T> Itb = external<T>(1, p[3], mt, (lane & 1) ? T(1) : T(-1), sqh);
   const int kG = g == 0 ? 4 : 5, iG = g == 0 ? 4 : 2 - g;
@@ -268,9 +266,9 @@ MF_D TopSide<T> top_side(const double (*p)[4], int g, int lane, double mt, cx<do
   t.c = bilinear(Itb.w, Ot.w);
 #pragma unroll
   for (int hg = 0; hg < 2; ++hg) {
-    const QW<T> G = external<T>(kG, p[iG], 0.0, hg ? T(1) : T(-1), sqh);
-    t.d3[hg] = bilinear(Itb.w, ffv1_1(Ot, G, ct, (T)mt).w);
-    t.d4[hg] = bilinear(ffv1_2(Itb, G, cb, (T)mt).w, Ot.w);
+    const QW<T> G = external<T>(kG, p[iG], T(0), hg ? T(1) : T(-1), sqh);
+    t.d3[hg] = bilinear(Itb.w, ffv1_1(Ot, G, ct, mt).w);
+    t.d4[hg] = bilinear(ffv1_2(Itb, G, cb, mt).w, Ot.w);
   }
   return t;
 }
@@ -278,16 +276,16 @@ MF_D TopSide<T> top_side(const double (*p)[4], int g, int lane, double mt, cx<do
 // evaluation j's light state l: gluon helicity l >> 1, chirality nh = +-1
 // (l & 1) of the quark pair, nhel = nh * nsf for each of the two
 template <class T>
-MF_D LightSide<T> light_side(const double (*p)[4], int j, int lane, cx<double> gc10, cx<double> gc11,
-                             const Factors<T>& F, T sqh) {
+MF_D LightSide<T> light_side(const T (*p)[4], int j, int lane, cx<double> gc10, cx<double> gc11, const Factors<T>& F,
+                             T sqh) {
   int channel, m, kI, iI, kO, iO, kG, iG;
   eval_channel(j, channel, m);
   channel_legs(channel, m, 1 - m, kI, iI, kO, iO, kG, iG);
   const T nh = (lane & 1) ? T(1) : T(-1);
   const T nsfI = kI == 0 ? T(1) : T(-1), nsfO = kO == 2 ? T(1) : T(-1);
-  const QW<T> G = external<T>(kG, p[iG], 0.0, (lane >> 1) ? T(1) : T(-1), sqh);
-  const QW<T> I = external<T>(kI, p[iI], 0.0, nh * nsfI, sqh);
-  const QW<T> O = external<T>(kO, p[iO], 0.0, nh * nsfO, sqh);
+  const QW<T> G = external<T>(kG, p[iG], T(0), (lane >> 1) ? T(1) : T(-1), sqh);
+  const QW<T> I = external<T>(kI, p[iI], T(0), nh * nsfI, sqh);
+  const QW<T> O = external<T>(kO, p[iO], T(0), nh * nsfO, sqh);
   const cx<T> cs = ic<T>(gc11, F.r[0]);
   LightSide<T> l;
   const QW<T> vs0 = ffv1p0_3(I, O, ic<T>(gc11, F.r[9 + 3 * j]));
@@ -330,18 +328,23 @@ MF_D double qq3_weighted_sum(const double (*p)[4], const double* w, double mt, d
                              cx<double> gc11, T sqh, unsigned mask, int lane, int base) {
   using namespace mfqq3;
   const Factors<T> F = event_factors<T>(p, mt, wt, mask, lane, base);
+  T pt[5][4];
+#pragma unroll
+  for (int i = 0; i < 5; ++i)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) pt[i][c] = (T)p[i][c];
   double s = 0.0;
 #pragma unroll 1
   for (int g = 0; g < 3; ++g) {
     if (w[2 * g] == 0.0 && w[2 * g + 1] == 0.0) continue;  // uniform across the group
-    const TopSide<T> t = top_side<T>(p, g, lane, mt, gc11, F, sqh);
+    const TopSide<T> t = top_side<T>(pt, g, lane, (T)mt, gc11, F, sqh);
 #pragma unroll 1
     for (int u = 0; u < 2; ++u) {
       const int j = 2 * g + u;
       if (w[j] == 0.0) continue;
       int channel, m;
       eval_channel(j, channel, m);
-      const LightSide<T> l = light_side<T>(p, j, lane, gc10, gc11, F, sqh);
+      const LightSide<T> l = light_side<T>(pt, j, lane, gc10, gc11, F, sqh);
       s += w[j] / (channel == 0 ? 36.0 : 96.0) * (double)group_products(t, l, mask, base);
     }
   }
