@@ -530,7 +530,7 @@ struct mf_process {
   double* d_me = nullptr;   // [cap]
   double* d_extra = nullptr;  // [extra_cap] weights of further channels (p p > t t~ (j))
   int64_t extra_cap = 0;
-  double* d_qqin = nullptr;   // [23][qqin_cap] inputs of the light-quark channels of p p > t t~ j
+  double* d_qqin = nullptr;   // [26][qqin_cap] inputs of the light-quark channels of p p > t t~ j
   int64_t qqin_cap = 0;
   unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
   int64_t event_cap = 0;
@@ -1078,7 +1078,7 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
     cudaFree(p->d_qqin);
     p->d_qqin = nullptr;
     p->qqin_cap = 0;
-    st = cuda_status(cudaMalloc(&p->d_qqin, sizeof(double) * 23 * (size_t)slice));
+    st = cuda_status(cudaMalloc(&p->d_qqin, sizeof(double) * 26 * (size_t)slice));
     if (st) return st;
     p->qqin_cap = slice;
   }
@@ -1176,7 +1176,7 @@ int mf_process_scratch_bytes(const mf_process* p, int64_t* bytes) {
   const int64_t per_event = mf_prep_bytes(p->k, p->prec) + (int64_t)sizeof(double) * (mf_state_words(p->k) + 2) +
                             MF_MAX_DIM;
   int64_t b = p->event_cap * per_event + p->extra_cap * (int64_t)sizeof(double) +
-              p->qqin_cap * 23 * (int64_t)sizeof(double) +
+              p->qqin_cap * 26 * (int64_t)sizeof(double) +
               (int64_t)p->partial_cap * (int64_t)sizeof(double);
   if (p->d_ws) b += mf_ws_bytes(p->k, p->prec);
   *bytes = b;

@@ -48,8 +48,9 @@ struct IterArgs {
   double* ps_out;      // optional [N][K+2][4] lab-frame momenta of the passing events (event output)
   int qq;              // p p > t t~ (K = 2) or p p > t t~ j (K = 3): add the light-quark channels
   double* extra;       // [N] with qq: their weight, jac x weight x luminosity x |M|^2 summed
-  double* qqin;        // [23][N] with qq and K = 3: the event's momenta [5][4] (partonic frame), the
-                       // weight before the luminosities (0: the event failed the cuts), x1, x2
+  double* qqin;        // [26][N] with qq and K = 3: the event's momenta [5][4] (partonic frame) and
+                       // its weight times each channel evaluation's luminosity (qq3_weighted_sum's
+                       // order; all 0: the event failed the cuts)
   // pipeline buffers (scratch)
   double* state;            // [4K+16][N] first-pass state (ps_state_words)
   int4* prep;              // [N] per-event records (PrepRec), passing events only
@@ -287,9 +288,33 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
         for (int i = 0; i < 5; ++i)
 #pragma unroll
           for (int c = 0; c < 4; ++c) q[(int64_t)(4 * i + c) * N] = p[i][c];
-        q[(int64_t)20 * N] = ok ? jac * wps : 0.0;
-        q[(int64_t)21 * N] = x1;
-        q[(int64_t)22 * N] = x2;
+        double lw[6] = {0, 0, 0, 0, 0, 0};
+        if (ok) {
+          // the densities at x1 and x2 from one interpolation stencil each
+          const PdfStencil s1 = pdf_stencil(A.pdf, x1, v), s2 = pdf_stencil(A.pdf, x2, v);
+          double qq = 0.0, qbq = 0.0, Q1 = 0.0, Qb1 = 0.0, Q2 = 0.0, Qb2 = 0.0;
+          for (int f = 1; f <= 4; ++f) {
+            const double a = pdf_xfx_st(A.pdf, f, s1), ab = pdf_xfx_st(A.pdf, f + 4, s1);
+            const double b = pdf_xfx_st(A.pdf, f, s2), bb = pdf_xfx_st(A.pdf, f + 4, s2);
+            qq += a * bb;
+            qbq += ab * b;
+            Q1 += a;
+            Qb1 += ab;
+            Q2 += b;
+            Qb2 += bb;
+          }
+          const double g1 = pdf_xfx_st(A.pdf, 0, s1), g2 = pdf_xfx_st(A.pdf, 0, s2);
+          const double c = jac * wps / x1 / x2;
+          // qq3_weighted_sum's order: q q~, q~ q, q g, q~ g, g q, g q~
+          lw[0] = c * qq;
+          lw[1] = c * qbq;
+          lw[2] = c * (Q1 * g2);
+          lw[3] = c * (Qb1 * g2);
+          lw[4] = c * (g1 * Q2);
+          lw[5] = c * (g1 * Qb2);
+        }
+#pragma unroll
+        for (int j = 0; j < 6; ++j) q[(int64_t)(20 + j) * N] = lw[j];
       }
     }
     if (A.ps_out) {
@@ -323,42 +348,25 @@ template <class T> __global__ void __launch_bounds__(128) qq3_channels_kernel(It
   const int64_t N = A.N;
   const int lane = threadIdx.x & 3, base = (threadIdx.x & 31) & ~3;
   const unsigned mask = 0xFu << base;
-  const double v = pdf_qcoord(A.pdf, A.q2);
   const T sqh = (T)mf_consts(A.f32q != 0).sqh;
   const int64_t stride = (int64_t)gridDim.x * (blockDim.x >> 2);
   for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2; e < N; e += stride) {
     const double* q = A.qqin + e;
-    const double w = q[(int64_t)20 * N];
+    double lw[6];
+    bool any = false;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      lw[j] = q[(int64_t)(20 + j) * N];
+      any = any || lw[j] != 0.0;
+    }
     double ex = 0.0;
-    if (w != 0.0) {
+    if (any) {
       double p[5][4];
 #pragma unroll
       for (int i = 0; i < 5; ++i)
 #pragma unroll
         for (int c = 0; c < 4; ++c) p[i][c] = q[(int64_t)(4 * i + c) * N];
-      const double x1 = q[(int64_t)21 * N], x2 = q[(int64_t)22 * N];
-      // densities: lanes 0, 1 at x1, lanes 2, 3 at x2; even lanes d u and
-      // their antiquarks (and the gluon), odd lanes s c and theirs
-      using mfqq3::group_sum;
-      const PdfStencil st = pdf_stencil(A.pdf, lane < 2 ? x1 : x2, v);
-      const int f0 = (lane & 1) ? 3 : 1;
-      const double qa = pdf_xfx_st(A.pdf, f0, st), qb = pdf_xfx_st(A.pdf, f0 + 1, st);
-      const double qab = pdf_xfx_st(A.pdf, f0 + 4, st), qbb = pdf_xfx_st(A.pdf, f0 + 5, st);
-      double g = 0.0;
-      if (!(lane & 1)) g = pdf_xfx_st(A.pdf, 0, st);
-      const double g1 = __shfl_sync(mask, g, base), g2 = __shfl_sync(mask, g, base + 2);
-      // lanes 0, 1 pair their flavours at x1 with the same flavours at x2
-      const int partner = base + ((lane + 2) & 3);
-      const double ra = __shfl_sync(mask, qa, partner), rb = __shfl_sync(mask, qb, partner);
-      const double rab = __shfl_sync(mask, qab, partner), rbb = __shfl_sync(mask, qbb, partner);
-      const bool at1 = lane < 2;
-      const double qq = group_sum(at1 ? qa * rab + qb * rbb : 0.0, mask);
-      const double qbq = group_sum(at1 ? qab * ra + qbb * rb : 0.0, mask);
-      const double Q1 = group_sum(at1 ? qa + qb : 0.0, mask), Qb1 = group_sum(at1 ? qab + qbb : 0.0, mask);
-      const double Q2 = group_sum(at1 ? 0.0 : qa + qb, mask), Qb2 = group_sum(at1 ? 0.0 : qab + qbb, mask);
-      // the evaluations' order of qq3_weighted_sum: q q~, q~ q, q g, q~ g, g q, g q~
-      const double lum[6] = {qq, qbq, Q1 * g2, Qb1 * g2, g1 * Q2, g1 * Qb2};
-      ex = w * qq3_weighted_sum<T>(p, lum, A.mt, A.wt, A.gc10, A.gc11, sqh, mask, lane, base) / x1 / x2;
+      ex = qq3_weighted_sum<T>(p, lw, A.mt, A.wt, A.gc10, A.gc11, sqh, mask, lane, base);
     }
     if (lane == 0) A.extra[e] = ex;
   }

@@ -345,7 +345,8 @@ MF_D double qq3_weighted_sum(const double (*p)[4], const double* w, double mt, d
       int channel, m;
       eval_channel(j, channel, m);
       const LightSide<T> l = light_side<T>(pt, j, lane, gc10, gc11, F, sqh);
-      s += w[j] / (channel == 0 ? 36.0 : 96.0) * (double)group_products(t, l, mask, base);
+      // the averages over the initial spins and colours: 1/36, 1/96
+      s += w[j] * (channel == 0 ? 1.0 / 36.0 : 1.0 / 96.0) * (double)group_products(t, l, mask, base);
     }
   }
   const double g11sq = gc11.re * gc11.re + gc11.im * gc11.im;  // the FFV1_0 factor -i GC_11
