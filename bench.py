@@ -605,7 +605,7 @@ def _flow_leg(args, integ, target, layers, bins, bf16, vegas_iters, vegas_events
         return adaptive_flow_integration(flow, integ, target_rel_error=target_, batch_size=batch,
                                          max_batches=max_b, lr=args.flow_lr, train_batches=train_b,
                                          minibatch=args.flow_minibatch, grid=grid, prior=prior,
-                                         resample=args.flow_resample)
+                                         resample=args.flow_resample, train_steps=args.flow_train_steps)
 
     # untimed warm-up of the flow's kernels and GEMM shapes, the launch autotuner and the allocations
     run(_flow(args, integ, layers, bins, bf16), None, None, 0.0, 2, 1)
@@ -629,7 +629,8 @@ def _flow_leg(args, integ, target, layers, bins, bf16, vegas_iters, vegas_events
             "flow": f"{layers} piecewise-quadratic coupling layers, {bins} bins, MLP 2x{args.flow_hidden} "
                     f"({_flow_kernels(flow)}), "
                     f"lr {args.flow_lr}, on a frozen VEGAS grid, trained on {args.flow_resample} events per batch "
-                    "resampled with probability w^2 (one Adam step, a captured CUDA graph)",
+                    f"resampled with probability w^2 ({args.flow_train_steps} Adam step(s) per batch, each on its "
+                    "own resample, a captured CUDA graph)",
             "last_std_over_mean": info["last_rel_std"]}, flow, v.grid
 
 
@@ -905,6 +906,7 @@ def parse_args(argv=None):
     ap.add_argument("--flow-resample", type=int, default=50_000)
     ap.add_argument("--flow-lr", type=float, default=1e-2)
     ap.add_argument("--flow-train-batches", type=int, default=20)
+    ap.add_argument("--flow-train-steps", type=int, default=1, help="optimiser steps per trained flow batch")
     ap.add_argument("--flow-vegas-iters", type=int, default=5)
     ap.add_argument("--flow-vegas-events", type=int, default=2_000_000)
     ap.add_argument("--precision-points", type=int, default=1_000_000)

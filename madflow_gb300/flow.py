@@ -329,7 +329,7 @@ class _GraphedStep:
         self.graph.replay()
 
 
-def _train_step(flow, opt, x, w, minibatch, resample=0, step=None):
+def _train_step(flow, opt, x, w, minibatch, resample=0, step=None, steps=1):
     """Variance-loss updates on one batch (x, w = f/q) drawn from the flow.
 
     The gradient of Var(f/q) is -E_q[w^2 d log q] (score function).  With
@@ -337,30 +337,19 @@ def _train_step(flow, opt, x, w, minibatch, resample=0, step=None):
     probability w^2 / sum w^2 (systematic resampling), as
     -(sum w^2) mean(d log q) over them: unbiased, and only the resampled
     events go through the flow's log-density and its backward pass.
-    step (optional): a _GraphedStep for `resample` points (one minibatch)."""
+    step (optional): a _GraphedStep for `resample` points (one minibatch).
+    steps: optimiser steps on the batch, each on its own resample."""
     if resample > 0:
         w2 = (w * w).double()
         total = float(w2.sum())
         if total <= 0.0:
             return
         cdf = torch.cumsum(w2, 0) / total
-        u = (torch.arange(resample, device=w.device, dtype=torch.float64) + torch.rand(1, device=w.device,
-                                                                                      dtype=torch.float64)) / resample
-        idx = torch.clamp(torch.searchsorted(cdf, u), max=w.numel() - 1)
-        xs = x[idx]
-        if step is not None:
-            step(xs)
-            return
-        for s in range(0, resample, minibatch):
-            xm = xs[s: s + minibatch]
-            if flow.native:
-                flow.native_backward(xm, torch.full((xm.shape[0],), -1.0 / xm.shape[0], dtype=torch.float32,
-                                                    device=xm.device))
-            else:
-                loss = -flow.log_prob(xm).mean()
-                opt.zero_grad(set_to_none=True)
-                _backward(flow, loss)
-            opt.step()
+        for _ in range(int(steps)):
+            u = (torch.arange(resample, device=w.device, dtype=torch.float64)
+                 + torch.rand(1, device=w.device, dtype=torch.float64)) / resample
+            idx = torch.clamp(torch.searchsorted(cdf, u), max=w.numel() - 1)
+            _resampled_step(flow, opt, x[idx], minibatch, resample, step)
         return
     mean_w = w.mean()
     scale = (mean_w * mean_w).clamp_min(1e-300)
@@ -373,6 +362,23 @@ def _train_step(flow, opt, x, w, minibatch, resample=0, step=None):
         else:
             lq = flow.log_prob(x[s: s + minibatch])
             loss = -(coef * lq).mean()
+            opt.zero_grad(set_to_none=True)
+            _backward(flow, loss)
+        opt.step()
+
+
+def _resampled_step(flow, opt, xs, minibatch, resample, step):
+    """One optimiser step of -mean log q over resampled points xs."""
+    if step is not None:
+        step(xs)
+        return
+    for s in range(0, resample, minibatch):
+        xm = xs[s: s + minibatch]
+        if flow.native:
+            flow.native_backward(xm, torch.full((xm.shape[0],), -1.0 / xm.shape[0], dtype=torch.float32,
+                                                device=xm.device))
+        else:
+            loss = -flow.log_prob(xm).mean()
             opt.zero_grad(set_to_none=True)
             _backward(flow, loss)
         opt.step()
@@ -410,7 +416,7 @@ def _vegas_map(grid, z):
 
 def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size=1_000_000, max_batches=200,
                               train_batches=30, minibatch=100_000, lr=2e-3, seed=99, grid=None, prior=None,
-                              resample=0, graph=True):
+                              resample=0, graph=True, train_steps=1):
     """Integrate while training: every batch is drawn from the current (frozen)
     flow, so mean(f/q) over it is an unbiased estimate with variance
     var(f/q)/n; the estimates of all batches are combined with
@@ -425,7 +431,8 @@ def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size
     the same inverse-variance form.  resample > 0: train on that many events
     resampled with probability w^2 (see _train_step).  graph: with
     resample > 0 and resample <= minibatch, the training step runs as a
-    captured CUDA graph (_GraphedStep).
+    captured CUDA graph (_GraphedStep); train_steps optimiser steps per
+    trained batch, each on its own resample.
 
     Returns (result, error, info)."""
     graphed = bool(graph and 0 < resample <= minibatch and train_batches > 0)
@@ -452,7 +459,7 @@ def adaptive_flow_integration(flow, integrand, target_rel_error=1e-3, batch_size
             if cur != 0 and (1.0 / math.sqrt(wsum)) / abs(cur) <= target_rel_error:
                 break
         if b < train_batches:
-            _train_step(flow, opt, z, w, minibatch, resample, step)
+            _train_step(flow, opt, z, w, minibatch, resample, step, train_steps)
     info = {"batches": b + 1, "trained": min(b + 1, int(train_batches)), "last_rel_std": rel_std}
     if wsum == 0:
         return 0.0, 0.0, info
