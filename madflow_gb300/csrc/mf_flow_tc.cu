@@ -13,7 +13,11 @@
 // (K/4) x 128 bytes between 8-row groups), loaded once per block; the A
 // operands (the conditioning inputs 2z - 1, padded to K = 16, and the hidden
 // activations, K = 64); the biases.  Tensor memory: 256 columns (D1 at 0,
-// D2 at 64, D3 at 0 once D1 and D2 have been read).  Every wait on the MMA
+// D2 at 64, D3 at 0 once D1 and D2 have been read).  A layer with more than
+// 256 MLP outputs runs the third GEMM in two column chunks of whole
+// dimensions (each at most 256 columns, the second after the first one's
+// epilogue has read its accumulator), with the rows of W3 stored in the
+// two chunks' padded blocks.  Every wait on the MMA
 // completion is bounded (1000 tries of <= 1 ms); one that runs out sets *err,
 // the block stops and frees its tensor memory.
 #include <cstdint>
@@ -28,7 +32,18 @@ constexpr int FH = 64;        // hidden units
 constexpr int FTILE = 128;    // points per tile (MMA M)
 constexpr int FK1 = 16;       // padded conditioning inputs (GEMM1 K)
 constexpr int FTMEM = 256;    // tensor-memory columns per block
-constexpr int FMAXN3 = 256;   // nb (2K+1) padded to 16, at most
+constexpr int FMAXN3 = 256;   // one chunk of the third GEMM: at most 256 columns
+
+__host__ __device__ inline int pad16(int n) { return (n + 15) / 16 * 16; }
+// The column chunks of the third GEMM for nb dimensions of np = 2K+1
+// parameters: da dimensions in the first, nb - da in the second, padded to
+// n3ap and n3bp columns (n3bp = 0: one chunk).  false: more than two chunks.
+__host__ __device__ inline bool flow_tc_chunks(int nb, int np, int& da, int& n3ap, int& n3bp) {
+  da = nb < FMAXN3 / np ? nb : FMAXN3 / np;
+  n3ap = pad16(da * np);
+  n3bp = pad16((nb - da) * np);
+  return n3bp <= FMAXN3;
+}
 
 // float offset of element (r, k) in a K-major canonical operand with kdim
 // columns
@@ -39,10 +54,10 @@ __host__ __device__ __forceinline__ int canon(int r, int k, int kdim) {
 struct FlowTcSmem {
   float* B1;  // [64][16]
   float* B2;  // [64][64]
-  float* B3;  // [n3p][64]
+  float* B3;  // [n3ap + n3bp][64]: the chunks' rows of W3, each block padded
   float* A1;  // [128][16]
   float* A2;  // [128][64]
-  float* bias;  // b1[64] b2[64] b3[n3p]
+  float* bias;  // b1[64] b2[64] b3[n3ap + n3bp] (b3 by output column)
   int* idx;     // ia[16] ib[16]
   unsigned long long* mbar;
   uint32_t* tmem;
@@ -137,21 +152,24 @@ __global__ void __launch_bounds__(FTILE) flow_inv_layer_tc_kernel(float* __restr
                                                                   const float* __restrict__ W2,
                                                                   const float* __restrict__ b2,
                                                                   const float* __restrict__ W3,
-                                                                  const float* __restrict__ b3, int n3p,
+                                                                  const float* __restrict__ b3,
                                                                   float* __restrict__ logq, int* __restrict__ err) {
 #if MF_TCGEN05
   constexpr int NP = 2 * K + 1;
   const int n3 = nb * NP;
+  int da, n3ap, n3bp;
+  flow_tc_chunks(nb, NP, da, n3ap, n3bp);
+  const int n3a = da * NP, n3b = n3 - n3a;
   extern __shared__ __align__(1024) unsigned char fsm[];
   uintptr_t base = (reinterpret_cast<uintptr_t>(fsm) + 1023) & ~(uintptr_t)1023;
   FlowTcSmem S;
   S.B1 = reinterpret_cast<float*>(base);
   S.B2 = S.B1 + FH * FK1;
   S.B3 = S.B2 + FH * FH;
-  S.A1 = S.B3 + n3p * FH;
+  S.A1 = S.B3 + (n3ap + n3bp) * FH;
   S.A2 = S.A1 + FTILE * FK1;
   S.bias = S.A2 + FTILE * FH;
-  S.idx = reinterpret_cast<int*>(S.bias + 2 * FH + n3p);
+  S.idx = reinterpret_cast<int*>(S.bias + 2 * FH + n3ap + n3bp);
   S.mbar = reinterpret_cast<unsigned long long*>(S.idx + 32);
   S.tmem = reinterpret_cast<uint32_t*>(S.mbar + 1);
   S.bad = reinterpret_cast<int*>(S.tmem + 1);
@@ -163,15 +181,17 @@ __global__ void __launch_bounds__(FTILE) flow_inv_layer_tc_kernel(float* __restr
     S.B1[canon(r, k, FK1)] = k < na ? W1[r * na + k] : 0.f;
   }
   for (int i = tid; i < FH * FH; i += FTILE) S.B2[canon(i / FH, i % FH, FH)] = W2[i];
-  for (int i = tid; i < n3p * FH; i += FTILE) {
+  for (int i = tid; i < (n3ap + n3bp) * FH; i += FTILE) {
     const int r = i / FH, k = i % FH;
-    S.B3[canon(r, k, FH)] = r < n3 ? W3[r * FH + k] : 0.f;
+    // row r of the chunk blocks: output column src of W3 (-1: padding)
+    const int src = r < n3ap ? (r < n3a ? r : -1) : (r - n3ap < n3b ? n3a + r - n3ap : -1);
+    S.B3[canon(r, k, FH)] = src >= 0 ? W3[src * FH + k] : 0.f;
   }
   for (int i = tid; i < FH; i += FTILE) {
     S.bias[i] = b1[i];
     S.bias[FH + i] = b2[i];
   }
-  for (int i = tid; i < n3p; i += FTILE) S.bias[2 * FH + i] = i < n3 ? b3[i] : 0.f;
+  for (int i = tid; i < n3ap + n3bp; i += FTILE) S.bias[2 * FH + i] = i < n3 ? b3[i] : 0.f;
   if (tid < 16) {
     S.idx[tid] = tid < na ? ia[tid] : 0;
     S.idx[16 + tid] = tid < nb ? ib[tid] : 0;
@@ -190,7 +210,10 @@ __global__ void __launch_bounds__(FTILE) flow_inv_layer_tc_kernel(float* __restr
   const uint32_t a1 = tc_smem_u32(S.A1), a2 = tc_smem_u32(S.A2);
   const uint32_t w1 = tc_smem_u32(S.B1), w2 = tc_smem_u32(S.B2), w3 = tc_smem_u32(S.B3);
   constexpr uint32_t L = 128, SB1 = (FK1 / 4) * 128, SB2 = (FH / 4) * 128;
-  const uint32_t id64 = tc_idesc_tf32(FTILE, FH), id3 = tc_idesc_tf32(FTILE, n3p);
+  const uint32_t id64 = tc_idesc_tf32(FTILE, FH), id3a = tc_idesc_tf32(FTILE, n3ap);
+  const uint32_t id3b = tc_idesc_tf32(FTILE, n3bp > 0 ? n3bp : 16);
+  // the second chunk's rows start n3ap rows (n3ap / 8 core-matrix groups) in
+  const uint32_t w3b = w3 + (uint32_t)n3ap * FH * 4;
   uint32_t phase = 0;
   const int64_t ntiles = (n + FTILE - 1) / FTILE;
 
@@ -271,32 +294,49 @@ __global__ void __launch_bounds__(FTILE) flow_inv_layer_tc_kernel(float* __restr
     tc_fence_proxy_async();
     tc_fence_before();
     __syncthreads();
-    // GEMM3: D3 [128][n3p] (columns 0..n3p-1) = A2 B3^T
-    if (tid == 0) {
-      tc_fence_after();
-#pragma unroll
-      for (int s = 0; s < FH / 8; ++s)
-        tc_mma_tf32(tm, tc_smem_desc(a2 + 256 * s, L, SB2), tc_smem_desc(w3 + 256 * s, L, SB2), id3, s > 0);
-      tc_commit(S.mbar);
-    }
-    if (!flow_tc_wait(S.mbar, phase, S.bad)) break;
-    phase ^= 1u;
-    tc_fence_after();
-    // epilogue: the inverse transform of each transformed dimension
+    // GEMM3 by column chunks: D3 [128][n3ap] (columns 0..) = A2 B3a^T, its
+    // epilogue, then the same for the second chunk (if any) into the same
+    // columns; the epilogue is the inverse transform of each dimension
     float ld = 0.f;
-    for (int d = 0; d < nb; ++d) {
-      float p[NP];
+    bool stop = false;
+    for (int ch = 0; ch < 2; ++ch) {
+      const int d0 = ch ? da : 0, d1 = ch ? nb : da;
+      if (d0 >= d1) break;
+      if (ch) {
+        // the first chunk's accumulator has been read by every thread
+        tc_fence_before();
+        __syncthreads();
+      }
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t wb = ch ? w3b : w3;
+        const uint32_t id3 = ch ? id3b : id3a;
 #pragma unroll
-      for (int j = 0; j < NP; ++j) tc_ld_x1(lane_base + d * NP + j, p[j]);
-      tc_wait_ld();
+        for (int s = 0; s < FH / 8; ++s)
+          tc_mma_tf32(tm, tc_smem_desc(a2 + 256 * s, L, SB2), tc_smem_desc(wb + 256 * s, L, SB2), id3, s > 0);
+        tc_commit(S.mbar);
+      }
+      if (!flow_tc_wait(S.mbar, phase, S.bad)) {
+        stop = true;
+        break;
+      }
+      phase ^= 1u;
+      tc_fence_after();
+      for (int d = d0; d < d1; ++d) {
+        float p[NP];
 #pragma unroll
-      for (int j = 0; j < NP; ++j) p[j] += S.bias[2 * FH + d * NP + j];
-      const int col = S.idx[16 + d];
-      float lp;
-      const float x = pq_inverse_one<K>(p, valid ? zr[col] : 0.5f, lp);
-      if (valid) zr[col] = x;
-      ld += lp;
+        for (int j = 0; j < NP; ++j) tc_ld_x1(lane_base + (d - d0) * NP + j, p[j]);
+        tc_wait_ld();
+#pragma unroll
+        for (int j = 0; j < NP; ++j) p[j] += S.bias[2 * FH + d * NP + j];
+        const int col = S.idx[16 + d];
+        float lp;
+        const float x = pq_inverse_one<K>(p, valid ? zr[col] : 0.5f, lp);
+        if (valid) zr[col] = x;
+        ld += lp;
+      }
     }
+    if (stop) break;
     if (valid) logq[e] += ld;
     tc_fence_before();
     __syncthreads();
@@ -323,8 +363,9 @@ template <int K>
 int launch_flow_tc(float* z, int64_t n, int dim, const int* ia, int na, const int* ib, int nb, const float* W1,
                    const float* b1, const float* W2, const float* b2, const float* W3, const float* b3, float* logq,
                    int* err, cudaStream_t st) {
-  const int n3 = nb * (2 * K + 1), n3p = (n3 + 15) / 16 * 16;
-  const size_t smem = flow_tc_smem_bytes(n3p);
+  int da, n3ap, n3bp;
+  flow_tc_chunks(nb, 2 * K + 1, da, n3ap, n3bp);
+  const size_t smem = flow_tc_smem_bytes(n3ap + n3bp);
   auto fn = flow_inv_layer_tc_kernel<K>;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return MF_ERR_CUDA;
@@ -333,7 +374,7 @@ int launch_flow_tc(float* z, int64_t n, int dim, const int* ia, int na, const in
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int64_t tiles = (n + FTILE - 1) / FTILE, grid = (int64_t)(sms > 0 ? sms : 152) * 2;
   if (grid > tiles) grid = tiles;
-  fn<<<(int)grid, FTILE, smem, st>>>(z, n, dim, ia, na, ib, nb, W1, b1, W2, b2, W3, b3, n3p, logq, err);
+  fn<<<(int)grid, FTILE, smem, st>>>(z, n, dim, ia, na, ib, nb, W1, b1, W2, b2, W3, b3, logq, err);
   return cudaPeekAtLastError() == cudaSuccess ? MF_OK : MF_ERR_CUDA;
 }
 
@@ -343,7 +384,8 @@ extern "C" int mf_flow_inv_layer_tc(float* z, int64_t n, int dim, const int* ia,
                                     const float* W1, const float* b1, const float* W2, const float* b2,
                                     const float* W3, const float* b3, float* logq, int* err, void* stream) {
   if (n < 0 || dim <= 0 || na < 1 || na > 16 || nb < 1 || nb > 16 || na + nb > dim) return MF_ERR_ARG;
-  if (!(K == 4 || K == 8 || K == 16) || ((nb * (2 * K + 1) + 15) / 16) * 16 > FMAXN3) return MF_ERR_ARG;
+  int da, n3ap, n3bp;
+  if (!(K == 4 || K == 8 || K == 16) || !flow_tc_chunks(nb, 2 * K + 1, da, n3ap, n3bp)) return MF_ERR_ARG;
   if (n == 0) return MF_OK;
   if (!z || !ia || !ib || !W1 || !b1 || !W2 || !b2 || !W3 || !b3 || !logq || !err) return MF_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;

@@ -15,8 +15,9 @@ dimensions per half):
     a fixed order); Adam updates the weights;
   * sampling runs one tcgen05 kernel per coupling layer (``mf_flow_tc.cu``:
     the MLP as three TF32 GEMMs with tensor-memory accumulators, the inverse
-    transform in the epilogue) when the layer fits it (at most 256 MLP
-    outputs) and TF32 is chosen, else the hand-written FP32 layer kernel.
+    transform in the epilogue) when the layer fits it (its MLP outputs in at
+    most two chunks of whole dimensions, 256 columns each) and TF32 is
+    chosen, else the hand-written FP32 layer kernel.
 Other shapes, and ``bf16=True``, run the conditioner through torch (cuBLAS,
 BF16 under autocast) with the hand-written transform kernels of
 ``mf_flow.cu`` (forward, inverse, log-Jacobian, backward).
@@ -93,6 +94,14 @@ def _masks(dim, n_layers, seed):
     return masks[:n_layers]
 
 
+def _tc_chunks_fit(nb, np_):
+    """Whether nb dimensions of np_ parameters fit the tensor-core sampling
+    layer's third GEMM: at most 256 columns in its first chunk of whole
+    dimensions, the rest (padded to 16) at most 256 in a second."""
+    da = min(nb, 256 // np_)
+    return ((nb - da) * np_ + 15) // 16 * 16 <= 256
+
+
 class NormalizingFlow(torch.nn.Module):
     def __init__(self, dim, n_layers=6, bins=16, hidden=64, n_hidden=2, seed=0, bf16=False, tf32=False, fused=None,
                  native=None):
@@ -104,7 +113,8 @@ class NormalizingFlow(torch.nn.Module):
         (cuBLAS) instead.  fused: sample with one tensor-core kernel per
         coupling layer (mf_flow_inv_layer_tc: the MLP in TF32 and the inverse
         transform); by default whenever tf32 is set and the shapes fit it
-        (also nb (2K+1) <= 256).  Reduced-precision GEMMs leave the estimates
+        (also the MLP outputs in at most two chunks of whole dimensions, 256
+        columns each).  Reduced-precision GEMMs leave the estimates
         unbiased (the sampled log-density is the exact density of the map as
         evaluated); they perturb the training gradients."""
         super().__init__()
@@ -127,11 +137,11 @@ class NormalizingFlow(torch.nn.Module):
                      for m in self.masks]
         self._idx32 = [(ib.int().contiguous(), ia.int().contiguous()) for ib, ia in self._idx]
         fits = (hidden == 64 and n_hidden == 2 and bins in (4, 8, 16)
-                and all(0 < len(ia) <= 16 and 0 < len(ib) <= 16 and len(ib) * (2 * bins + 1) <= 256
+                and all(0 < len(ia) <= 16 and 0 < len(ib) <= 16 and _tc_chunks_fit(len(ib), 2 * bins + 1)
                         for ib, ia in self._idx))
         if fused and not fits:
             raise ValueError("the fused sampling kernel needs 64 hidden units, 2 hidden layers, 4/8/16 bins, "
-                             "at most 16 dimensions per half")
+                             "at most 16 dimensions per half and two chunks of at most 256 MLP outputs")
         self.fused = bool(fits and (tf32 and not bf16) if fused is None else fused)
         nfits = (hidden == 64 and n_hidden == 2 and bins in (4, 8, 16)
                  and all(0 < len(ia) <= 16 and 0 < len(ib) <= 16 and len(ib) * (2 * bins + 1) <= 320

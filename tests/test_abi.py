@@ -41,7 +41,7 @@ def test_flow_layer_argument_checks():
     assert call(10, 18, 0, 9, 8) == _lib.MF_ERR_ARG      # no conditioning inputs
     assert call(10, 40, 20, 20, 8) == _lib.MF_ERR_ARG    # more than 16 per half
     assert call(10, 10, 9, 9, 8) == _lib.MF_ERR_ARG      # na + nb > dim
-    assert call(10, 32, 16, 16, 8) == _lib.MF_ERR_ARG    # nb (2K+1) = 272 > 256
+    assert call(10, 32, 16, 16, 16) == _lib.MF_ERR_ARG   # 7 dimensions in the first chunk, 9 x 33 > 256 after
     assert call(10, 18, 9, 9, 8) == _lib.MF_ERR_ARG      # null buffers
 
 

@@ -164,7 +164,7 @@ def test_adaptive_flow_on_vegas_grid(cuda):
     assert abs(res - 1.0) < 4 * err
 
 
-@pytest.mark.parametrize("dim,bins", [(18, 8), (18, 4), (7, 16)])
+@pytest.mark.parametrize("dim,bins", [(18, 8), (18, 4), (7, 16), (18, 16), (32, 8)])
 def test_fused_tensor_core_sampling(cuda, dim, bins):
     """mf_flow_inv_layer_tc (conditioner MLP as three tcgen05 TF32 GEMMs and
     the inverse transform in one kernel per layer) against the layer-by-layer
@@ -173,7 +173,9 @@ def test_fused_tensor_core_sampling(cuda, dim, bins):
     map is far from the identity).  The MLP inputs and weights are rounded to
     TF32 (10-bit mantissa) in the fused kernel: points agree to 2e-3 and
     log-densities to 2e-2 absolute; and the fused sampler's log density is
-    its map's own (against the FP32 forward log_prob, same tolerance)."""
+    its map's own (against the FP32 forward log_prob, same tolerance).
+    (18, 16) and (32, 8) have more than 256 MLP outputs per layer (297, 272):
+    the third GEMM runs in two column chunks."""
     import torch
 
     from madflow_gb300.flow import NormalizingFlow
