@@ -178,6 +178,51 @@ MF_D void rec_load(RecWS<T, K>& ws, PrepRec<T, K>& pr, const int4* __restrict__ 
   }
 }
 
+// rec_load in two halves, so that the global loads of the next event's
+// record overlap the current event's colour stage: rec_fetch reads this
+// thread's 16-byte words of the record into registers, rec_store puts them
+// where rec_load would.
+template <class T, int K, int NT> struct RecFetch {
+  static constexpr int NW = (int)(sizeof(PrepRec<T, K>) / 16);
+  static constexpr int PER = (NW + NT - 1) / NT;
+  int4 v[PER];
+};
+template <class T, int K, int NT>
+MF_D void rec_fetch(RecFetch<T, K, NT>& f, const int4* __restrict__ src, int tid) {
+#pragma unroll
+  for (int i = 0; i < RecFetch<T, K, NT>::PER; ++i) {
+    const int w = tid + i * NT;
+    if (w < RecFetch<T, K, NT>::NW) f.v[i] = src[w];
+  }
+}
+template <class T, int K, int NT>
+MF_D void rec_store(RecWS<T, K>& ws, PrepRec<T, K>& pr, const RecFetch<T, K, NT>& f, int tid) {
+  using R = RecTraits<K>;
+  using P = PrepRec<T, K>;
+  constexpr int NW = (int)(sizeof(P) / 16), NPL = (int)(sizeof(W4<T>) / 16);
+  constexpr int OG = (int)(offsetof(P, G) / 16), OWT = (int)(offsetof(P, WT) / 16);
+  constexpr int OWTB = (int)(offsetof(P, WTB) / 16), OEND = OWTB + 2 * NPL;
+  int4* dpr = reinterpret_cast<int4*>(&pr);
+  int4* dwt = reinterpret_cast<int4*>(ws.WT);
+  int4* dwtb = reinterpret_cast<int4*>(ws.WTB);
+#pragma unroll
+  for (int i = 0; i < RecFetch<T, K, NT>::PER; ++i) {
+    const int w = tid + i * NT;
+    if (w >= NW) break;
+    const int4 v = f.v[i];
+    if (w < OG || w >= OEND) {
+      dpr[w] = v;
+    } else if (w < OWT) {
+      const int idx = w - OG, wv = idx / NPL;
+      ws.J.pl[idx % NPL][R::jo_ext(wv >> 1) + (wv & 1)] = v;
+    } else if (w < OWTB) {
+      dwt[w - OWT] = v;
+    } else {
+      dwtb[w - OWTB] = v;
+    }
+  }
+}
+
 // colour-ordered gluon current from a record (see codegen.emit_program):
 // group i (1..L-1) of the record is split i, then one group per triple of the
 // contact term; m is the subset of the whole sequence
@@ -854,6 +899,12 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     const int64_t en = next_event(e + gridDim.x);
     T part = T(0);
     bool bad = false;
+    // SIMT colour sum: the next event's record into registers first, so its
+    // loads overlap the colour stage (the tensor-core variant loads it while
+    // the MMA runs)
+    RecFetch<T, K, nt> nf;
+    if constexpr (!TC)
+      if (en < N) rec_fetch<T, K, nt>(nf, prep + en * NW, tid);
 #if MF_TCGEN05
     if constexpr (TC) {
       constexpr int NP = R::NPERM, NC = 1 << (K + 2);
@@ -932,7 +983,7 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
       break;
     }
     if constexpr (!TC)
-      if (en < N) load_ext(en);
+      if (en < N) rec_store<T, K, nt>(S.ws, S.pr, nf, tid);
     e = en;
   }
 #if MF_TCGEN05
@@ -957,6 +1008,43 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
 // the block's sequence that need work; a sub-group left without one only
 // takes part in the barriers.
 template <int K> constexpr int events_per_block() { return K == 2 ? 6 : (K == 3 ? 3 : 1); }
+
+// Warp 0 of a block: the next EPB events of the block's sequence c, c + G,
+// c + 2G, ... (G = gridDim.x) that need work, 32 candidates per round (one
+// load each, in parallel); the skipped ones before the last event taken get
+// out = 0.  Returns the new cursor; ev[j] = -1 for missing events.
+template <int EPB>
+MF_DO int64_t gather_events(int64_t c, int64_t N, const double* __restrict__ skip, double* __restrict__ out,
+                           int64_t* ev, int lane) {
+  const int64_t G = gridDim.x;
+  int taken = 0;
+  while (taken < EPB) {
+    const int64_t cand = c + (int64_t)lane * G;
+    const bool inrange = cand < N;
+    const bool need = inrange && !(skip && (__double_as_longlong(skip[cand]) << 1) == 0);
+    const unsigned nm = __ballot_sync(0xffffffffu, need);
+    if (__ballot_sync(0xffffffffu, inrange) == 0) break;
+    const int want = EPB - taken;
+    int last = 31;  // the last candidate consumed this round
+    if (__popc(nm) >= want) {
+      unsigned m = nm;
+      for (int i = 1; i < want; ++i) m &= m - 1;
+      last = __ffs(m) - 1;
+    }
+    if (lane <= last) {
+      if (need)
+        ev[taken + __popc(nm & ((1u << lane) - 1u))] = cand;
+      else if (inrange)
+        out[cand] = 0.0;
+    }
+    taken += __popc(nm) < want ? __popc(nm) : want;
+    c += (int64_t)(last + 1) * G;
+  }
+  __syncwarp();
+  if (lane < EPB && lane >= taken) ev[lane] = -1;
+  return c;
+}
+
 template <int K, class T>
 __global__ void __launch_bounds__(MF_REC_NT, 4)
     me_rec_multi_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
@@ -966,34 +1054,27 @@ __global__ void __launch_bounds__(MF_REC_NT, 4)
   static_assert(TPE % 32 == 0, "whole warps per event");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   RecSmem<T, K>* Sall = reinterpret_cast<RecSmem<T, K>*>(smem_raw);
-  __shared__ int64_t ev[EPB];
-  __shared__ int64_t cursor;
+  __shared__ int64_t evs[2][EPB];  // this round's events and the next round's
   const int tid = threadIdx.x, sub = tid / TPE, lt = tid % TPE;
   RecSmem<T, K>& S = Sall[sub];
-  if (tid == 0) cursor = blockIdx.x;
+  int64_t cursor = blockIdx.x;  // warp 0's
+  if (tid < 32) cursor = gather_events<EPB>(cursor, N, skip, out, evs[0], tid);
   __syncthreads();
-  for (;;) {
-    if (tid == 0) {
-      int64_t c = cursor;
-      for (int j = 0; j < EPB; ++j) {
-        while (c < N && skip && (__double_as_longlong(skip[c]) << 1) == 0) {
-          out[c] = 0.0;
-          c += gridDim.x;
-        }
-        ev[j] = c < N ? c : -1;
-        if (c < N) c += gridDim.x;
-      }
-      cursor = c;
-    }
+  int64_t e = evs[0][sub];
+  if (e >= 0) rec_load<T, K, TPE>(S.ws, S.pr, prep + e * NW, lt);
+  int buf = 0;
+  while (evs[buf][0] >= 0) {
     __syncthreads();
-    if (ev[0] < 0) break;
-    const int64_t e = ev[sub];
+    // warp 0 looks up the next round's events while the stages run
+    if (tid < 32) cursor = gather_events<EPB>(cursor, N, skip, out, evs[buf ^ 1], tid);
     const bool on = e >= 0;
-    if (on) rec_load<T, K, TPE>(S.ws, S.pr, prep + e * NW, lt);
-    __syncthreads();
     rec_stages_c<T, K, 1, TPE>(S.ws, S.pr.ev, lt, on);
     if (on) rec_st_A<T, K>(S.ws, lt, TPE);
     __syncthreads();
+    // the next round's records into registers: their loads overlap the colour stage
+    const int64_t en = evs[buf ^ 1][sub];
+    RecFetch<T, K, TPE> nf;
+    if (en >= 0) rec_fetch<T, K, TPE>(nf, prep + en * NW, lt);
     T part = on ? rec_st_colour<T, K>(S.ws, lt, TPE) : T(0);
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((tid & 31) == 0) S.red[lt >> 5] = part;
@@ -1007,6 +1088,9 @@ __global__ void __launch_bounds__(MF_REC_NT, 4)
       for (int w = 0; w < TPE / 32; ++w) tot += S.red[w];
       out[e] = (double)tot * sc;
     }
+    if (en >= 0) rec_store<T, K, TPE>(S.ws, S.pr, nf, lt);
+    e = en;
+    buf ^= 1;
   }
 }
 #endif
