@@ -899,12 +899,7 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
     const int64_t en = next_event(e + gridDim.x);
     T part = T(0);
     bool bad = false;
-    // SIMT colour sum: the next event's record into registers first, so its
-    // loads overlap the colour stage (the tensor-core variant loads it while
-    // the MMA runs)
-    RecFetch<T, K, nt> nf;
-    if constexpr (!TC)
-      if (en < N) rec_fetch<T, K, nt>(nf, prep + en * NW, tid);
+
 #if MF_TCGEN05
     if constexpr (TC) {
       constexpr int NP = R::NPERM, NC = 1 << (K + 2);
@@ -983,7 +978,7 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
       break;
     }
     if constexpr (!TC)
-      if (en < N) rec_store<T, K, nt>(S.ws, S.pr, nf, tid);
+      if (en < N) load_ext(en);
     e = en;
   }
 #if MF_TCGEN05
