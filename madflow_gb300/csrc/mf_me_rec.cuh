@@ -408,13 +408,17 @@ MF_D void rec_stage_c(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid) {
   constexpr bool PAIR = K >= 4 && rec_part_items<K, P0, P1>() > NT;
   rec_stage_parts<T, K, P0, P1, NT, PAIR>(ws, ev, tid, 0);
 }
-// stages STAGE..K-1, each followed by a block barrier; a thread with on =
-// false only takes part in the barriers
+// stages STAGE..K-1, each followed by a block barrier (a warp barrier when
+// one warp evaluates the event, NT = 32); a thread with on = false only
+// takes part in the barriers
 template <class T, int K, int STAGE, int NT>
 MF_DO void rec_stages_c(RecWS<T, K>& ws, const EvData<T, K>& ev, int tid, bool on = true) {
   if constexpr (STAGE < K) {
     if (on) rec_stage_c<T, K, STAGE, NT>(ws, ev, tid);
-    __syncthreads();
+    if constexpr (NT == 32)
+      __syncwarp();
+    else
+      __syncthreads();
     rec_stages_c<T, K, STAGE + 1, NT>(ws, ev, tid, on);
   }
 }
@@ -1086,6 +1090,71 @@ __global__ void __launch_bounds__(MF_REC_NT, 4)
     if (en >= 0) rec_store<T, K, TPE>(S.ws, S.pr, nf, lt);
     e = en;
     buf ^= 1;
+  }
+}
+
+// One warp per event (two and three gluons): every warp of the grid follows
+// its own sequence of events (warp w of the grid takes w, w + W, w + 2W, ...,
+// W the warps in the grid), with its own record in shared memory and only
+// warp barriers between the stages, so no warp waits for another.  The
+// warp looks for its next event and fetches its record into registers
+// before the colour stage, which hides their loads.
+// Warp-uniform: the warp's next event at or after cursor c (stride G) that
+// needs work (e, -1 if none); the skipped ones before it get out = 0.
+MF_DO int64_t next_warp_event(int64_t c, int64_t G, int64_t N, const double* __restrict__ skip,
+                              double* __restrict__ out, int lane, int64_t& e) {
+  for (;;) {
+    const int64_t cand = c + (int64_t)lane * G;
+    const bool inrange = cand < N;
+    const bool need = inrange && !(skip && (__double_as_longlong(skip[cand]) << 1) == 0);
+    const unsigned nm = __ballot_sync(0xffffffffu, need);
+    if (__ballot_sync(0xffffffffu, inrange) == 0) {
+      e = -1;
+      return c;
+    }
+    if (nm) {
+      const int first = __ffs(nm) - 1;
+      if (lane < first && inrange) out[cand] = 0.0;
+      e = c + (int64_t)first * G;
+      return c + (int64_t)(first + 1) * G;
+    }
+    if (inrange) out[cand] = 0.0;
+    c += 32 * G;
+  }
+}
+
+template <int K, class T>
+__global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
+    me_rec_warp_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
+                       double* __restrict__ out, double* __restrict__ hel_out) {
+  using R = RecTraits<K>;
+  constexpr int WPB = MF_REC_NT / 32, NW = prep_words<T, K>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  RecSmem<T, K>& S = reinterpret_cast<RecSmem<T, K>*>(smem_raw)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int64_t G = (int64_t)gridDim.x * WPB;
+  int64_t e;
+  int64_t c = next_warp_event((int64_t)blockIdx.x * WPB + (threadIdx.x >> 5), G, N, skip, out, lane, e);
+  if (e >= 0) rec_load<T, K, 32>(S.ws, S.pr, prep + e * NW, lane);
+  while (e >= 0) {
+    __syncwarp();
+    rec_stages_c<T, K, 1, 32>(S.ws, S.pr.ev, lane);
+    rec_st_A<T, K>(S.ws, lane, 32);
+    __syncwarp();
+    int64_t en;
+    c = next_warp_event(c, G, N, skip, out, lane, en);
+    RecFetch<T, K, 32> nf;
+    if (en >= 0) rec_fetch<T, K, 32>(nf, prep + en * NW, lane);
+    T part = rec_st_colour<T, K>(S.ws, lane, 32);
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    const double sc = S.pr.scale;
+    if (hel_out)
+      for (int cc = lane; cc < (1 << (K + 2)); cc += 32)
+        hel_out[(int64_t)R::cfg_to_mg(cc) * N + e] = rec_colour_one<T, K>(S.ws, cc) * sc * R::DENOMINATOR;
+    if (lane == 0) out[e] = (double)part * sc;
+    __syncwarp();
+    if (en >= 0) rec_store<T, K, 32>(S.ws, S.pr, nf, lane);
+    e = en;
   }
 }
 #endif

@@ -43,18 +43,19 @@ static int sm_count() {
   static int me_rec_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out, double* hel_out, \
                                  int* err, int waves, uint32_t tries, cudaStream_t st) {                                       \
     if constexpr (events_per_block<KK>() > 1) {                                                                \
-      /* several events per block (few helicities and colour flows) */                                        \
-      const void* fm = (const void*)me_rec_multi_kernel<KK, T>;                                                \
-      int mb = (int)sizeof(RecSmem<T, KK>) * events_per_block<KK>();                                           \
+      /* one warp per event (few helicities and colour flows) */                                              \
+      constexpr int WPB = MF_REC_NT / 32;                                                                      \
+      const void* fm = (const void*)me_rec_warp_kernel<KK, T>;                                                 \
+      int mb = (int)sizeof(RecSmem<T, KK>) * WPB;                                                              \
       cudaFuncSetAttribute(fm, cudaFuncAttributeMaxDynamicSharedMemorySize, mb);                               \
       int pm = 0;                                                                                              \
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pm, fm, MF_REC_NT, mb);                                   \
       if (pm < 1) pm = 1;                                                                                      \
       int64_t gm = (int64_t)sm_count() * pm * (waves > 0 ? waves : 1);                                         \
-      int64_t need = (N + events_per_block<KK>() - 1) / events_per_block<KK>();                                \
+      int64_t need = (N + WPB - 1) / WPB;                                                                      \
       if (gm > need) gm = need;                                                                                \
       if (gm < 1) gm = 1;                                                                                      \
-      me_rec_multi_kernel<KK, T><<<(int)gm, MF_REC_NT, mb, st>>>(prep, N, skip, out, hel_out);                \
+      me_rec_warp_kernel<KK, T><<<(int)gm, MF_REC_NT, mb, st>>>(prep, N, skip, out, hel_out);                 \
       return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                     \
     } else {                                                                                                   \
       const void* fn = (const void*)me_rec_kernel<KK, T, COLOUR>;                                              \
