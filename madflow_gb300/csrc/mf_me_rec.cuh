@@ -1000,98 +1000,9 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
   }
 #endif
 }
-// Processes with few helicities and colour flows (two or three gluons) run
-// EPB events per block, TPE = MF_REC_NT / EPB threads each (a multiple of a
-// warp), every event in its own RecSmem; the block keeps the events in step
-// (stage barriers are block-wide).  Thread 0 gathers the next EPB events of
-// the block's sequence that need work; a sub-group left without one only
-// takes part in the barriers.
-template <int K> constexpr int events_per_block() { return K == 2 ? 6 : (K == 3 ? 3 : 1); }
-
-// Warp 0 of a block: the next EPB events of the block's sequence c, c + G,
-// c + 2G, ... (G = gridDim.x) that need work, 32 candidates per round (one
-// load each, in parallel); the skipped ones before the last event taken get
-// out = 0.  Returns the new cursor; ev[j] = -1 for missing events.
-template <int EPB>
-MF_DO int64_t gather_events(int64_t c, int64_t N, const double* __restrict__ skip, double* __restrict__ out,
-                           int64_t* ev, int lane) {
-  const int64_t G = gridDim.x;
-  int taken = 0;
-  while (taken < EPB) {
-    const int64_t cand = c + (int64_t)lane * G;
-    const bool inrange = cand < N;
-    const bool need = inrange && !(skip && (__double_as_longlong(skip[cand]) << 1) == 0);
-    const unsigned nm = __ballot_sync(0xffffffffu, need);
-    if (__ballot_sync(0xffffffffu, inrange) == 0) break;
-    const int want = EPB - taken;
-    int last = 31;  // the last candidate consumed this round
-    if (__popc(nm) >= want) {
-      unsigned m = nm;
-      for (int i = 1; i < want; ++i) m &= m - 1;
-      last = __ffs(m) - 1;
-    }
-    if (lane <= last) {
-      if (need)
-        ev[taken + __popc(nm & ((1u << lane) - 1u))] = cand;
-      else if (inrange)
-        out[cand] = 0.0;
-    }
-    taken += __popc(nm) < want ? __popc(nm) : want;
-    c += (int64_t)(last + 1) * G;
-  }
-  __syncwarp();
-  if (lane < EPB && lane >= taken) ev[lane] = -1;
-  return c;
-}
-
-template <int K, class T>
-__global__ void __launch_bounds__(MF_REC_NT, 4)
-    me_rec_multi_kernel(const int4* __restrict__ prep, int64_t N, const double* __restrict__ skip,
-                        double* __restrict__ out, double* __restrict__ hel_out) {
-  using R = RecTraits<K>;
-  constexpr int EPB = events_per_block<K>(), TPE = MF_REC_NT / EPB, NW = prep_words<T, K>();
-  static_assert(TPE % 32 == 0, "whole warps per event");
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  RecSmem<T, K>* Sall = reinterpret_cast<RecSmem<T, K>*>(smem_raw);
-  __shared__ int64_t evs[2][EPB];  // this round's events and the next round's
-  const int tid = threadIdx.x, sub = tid / TPE, lt = tid % TPE;
-  RecSmem<T, K>& S = Sall[sub];
-  int64_t cursor = blockIdx.x;  // warp 0's
-  if (tid < 32) cursor = gather_events<EPB>(cursor, N, skip, out, evs[0], tid);
-  __syncthreads();
-  int64_t e = evs[0][sub];
-  if (e >= 0) rec_load<T, K, TPE>(S.ws, S.pr, prep + e * NW, lt);
-  int buf = 0;
-  while (evs[buf][0] >= 0) {
-    __syncthreads();
-    // warp 0 looks up the next round's events while the stages run
-    if (tid < 32) cursor = gather_events<EPB>(cursor, N, skip, out, evs[buf ^ 1], tid);
-    const bool on = e >= 0;
-    rec_stages_c<T, K, 1, TPE>(S.ws, S.pr.ev, lt, on);
-    if (on) rec_st_A<T, K>(S.ws, lt, TPE);
-    __syncthreads();
-    // the next round's records into registers: their loads overlap the colour stage
-    const int64_t en = evs[buf ^ 1][sub];
-    RecFetch<T, K, TPE> nf;
-    if (en >= 0) rec_fetch<T, K, TPE>(nf, prep + en * NW, lt);
-    T part = on ? rec_st_colour<T, K>(S.ws, lt, TPE) : T(0);
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if ((tid & 31) == 0) S.red[lt >> 5] = part;
-    const double sc = S.pr.scale;
-    if (on && hel_out)
-      for (int c = lt; c < (1 << (K + 2)); c += TPE)
-        hel_out[(int64_t)R::cfg_to_mg(c) * N + e] = rec_colour_one<T, K>(S.ws, c) * sc * R::DENOMINATOR;
-    __syncthreads();
-    if (on && lt == 0) {
-      T tot = T(0);
-      for (int w = 0; w < TPE / 32; ++w) tot += S.red[w];
-      out[e] = (double)tot * sc;
-    }
-    if (en >= 0) rec_store<T, K, TPE>(S.ws, S.pr, nf, lt);
-    e = en;
-    buf ^= 1;
-  }
-}
+// Processes with few helicities and colour flows (two and three gluons) run
+// one event per warp; four and five gluons one event per block.
+template <int K> constexpr bool one_warp_per_event() { return K <= 3; }
 
 // One warp per event (two and three gluons): every warp of the grid follows
 // its own sequence of events (warp w of the grid takes w, w + W, w + 2W, ...,

@@ -42,7 +42,7 @@ static int sm_count() {
   template <class T, int COLOUR>                                                                               \
   static int me_rec_launch_k##KK(const int4* prep, int64_t N, const double* skip, double* out, double* hel_out, \
                                  int* err, int waves, uint32_t tries, cudaStream_t st) {                                       \
-    if constexpr (events_per_block<KK>() > 1) {                                                                \
+    if constexpr (one_warp_per_event<KK>()) {                                                                  \
       /* one warp per event (few helicities and colour flows) */                                              \
       constexpr int WPB = MF_REC_NT / 32;                                                                      \
       const void* fm = (const void*)me_rec_warp_kernel<KK, T>;                                                 \
