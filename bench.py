@@ -323,21 +323,21 @@ def run_gpu(args):
     pipe = "fp32" if prec_name == "mixed" else "fp64"
     peak, peak_how = measure_gemm_peak(pipe)
 
-    # end to end: the integrand contract f(x) with host buffers, copies timed
+    # end to end: the integrand contract f(x) on host buffers: the points in
+    # page-locked host memory, read by the kernels over the host link, and f
+    # written back to page-locked host memory (mf_integrand_rows, zero-copy);
+    # the transfers run inside the timed call
     e2e_n = min(N, args.e2e_events)
     rng = np.random.default_rng(args.seed)
     x_host = torch.from_numpy(rng.uniform(size=(e2e_n, integ.n_dim))).pin_memory()
     f_host = torch.empty(e2e_n, dtype=torch.float64).pin_memory()
-    x_dev = torch.empty((e2e_n, integ.n_dim), dtype=torch.float64, device="cuda")
-    x_dev.copy_(x_host, non_blocking=True)  # warm-up
-    f_host.copy_(integ(x_dev), non_blocking=True)
+    integ(x_host, out=f_host)  # warm-up
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     reps = max(1, args.e2e_reps)
     for _ in range(reps):
-        x_dev.copy_(x_host, non_blocking=True)
-        f_host.copy_(integ(x_dev), non_blocking=True)
+        integ(x_host, out=f_host)
     e1.record()
     torch.cuda.synchronize()
     e2e_rate = int((f_host != 0).sum()) * reps / (e0.elapsed_time(e1) / 1000.0)
@@ -374,7 +374,9 @@ def run_gpu(args):
         "nonfinite_weights": r["nonfinite"],
         "autotune": dict(tune, variants="index colour*4 + log2(waves); colour 0 SIMT, 1 tensor cores (tcgen05 TF32)"),
         "e2e": {"value": e2e_rate, "unit": "|M|^2 evals/s", "h2d_bytes_per_step": int(x_host.numel() * 8),
-                "d2h_bytes_per_step": int(f_host.numel() * 8), "api": "FusedIntegrand(x) -> f, host buffers",
+                "d2h_bytes_per_step": int(f_host.numel() * 8),
+                "api": "FusedIntegrand(x_host, out=f_host): x (N, ndim) float64 and f in page-locked host memory, "
+                       "read and written by the kernels over the host link (mf_integrand_rows, zero-copy)",
                 "events_per_step": e2e_n},
         "roofline": {"bound": pipe, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,

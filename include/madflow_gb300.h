@@ -162,6 +162,15 @@ int mf_integrand_ndim(const mf_process* proc, const mf_integrand_config* cfg, in
 int mf_integrand(const mf_process* proc, const mf_integrand_config* cfg, const double* x, int64_t n_events,
                  double* f, void* stream);
 
+/* f(x) with x in rows, [N][ndim], madflow's xrand[N, ndim] layout
+ * (madflow_exec.py:422), otherwise as mf_integrand.  x and f may each be
+ * device memory or page-locked host memory (cudaHostAlloc /
+ * cudaHostRegister): the kernels then read the points from, and write f to,
+ * host memory directly (zero-copy over the host link, inside the call's
+ * kernels, so no separate copy runs).  Other host memory: MF_ERR_ARG. */
+int mf_integrand_rows(const mf_process* proc, const mf_integrand_config* cfg, const double* x, int64_t n_events,
+                      double* f, void* stream);
+
 /* One VEGAS iteration (Lepage, J. Comput. Phys. 27 (1978) 192), fused:
  * Philox4x32-10 uniforms (seed, stream id, iteration) -> grid map -> integrand
  * -> per-iteration sums.  grid [ndim][nbins+1] (device, the bin edges).

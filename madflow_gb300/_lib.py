@@ -83,6 +83,7 @@ _SIGS = {
     "mf_VVV1P0_1": (c_int, [c_dp, c_dp, ctypes.POINTER(c_double), c_double, c_double, c_int64, c_dp, c_void_p]),
     "mf_integrand_ndim": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), ctypes.POINTER(c_int)]),
     "mf_integrand": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int64, c_dp, c_void_p]),
+    "mf_integrand_rows": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int64, c_dp, c_void_p]),
     "mf_vegas_iteration": (c_int, [c_void_p, ctypes.POINTER(IntegrandConfig), c_dp, c_int, c_uint64, c_uint32, c_dp,
                                    c_int64, c_dp, c_dp, c_dp, c_void_p]),
     "mf_smatrix_multi": (c_int, [ctypes.POINTER(c_void_p), c_int, ctypes.POINTER(c_void_p),

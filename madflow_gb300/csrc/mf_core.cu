@@ -1210,6 +1210,61 @@ int mf_integrand(const mf_process* pc, const mf_integrand_config* c, const doubl
   return run_fused(p, A, c, nullptr, f, stream);
 }
 
+// The device address of a caller's buffer: device or managed memory as it
+// is, page-locked host memory through its mapping (the kernels then read or
+// write it over the host link, zero-copy); other host memory: MF_ERR_ARG.
+static int device_view(const void* ptr, void** out) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return MF_ERR_ARG;
+  }
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+    *out = const_cast<void*>(ptr);
+    return MF_OK;
+  }
+  if (at.type == cudaMemoryTypeHost) {
+    if (at.devicePointer) {
+      *out = at.devicePointer;
+      return MF_OK;
+    }
+    return cuda_status(cudaHostGetDevicePointer(out, const_cast<void*>(ptr), 0));
+  }
+  return MF_ERR_ARG;
+}
+
+int mf_integrand_rows(const mf_process* pc, const mf_integrand_config* c, const double* x, int64_t N, double* f,
+                      void* stream) {
+  mf_process* p = const_cast<mf_process*>(pc);
+  int ndim = 0;
+  if (!p || !c || N < 0 || (N > 0 && (!x || !f))) return MF_ERR_ARG;
+  int st = mf_integrand_ndim(p, c, &ndim);
+  if (st) return st;
+  if (N == 0) return MF_OK;
+  void *xd = nullptr, *fd = nullptr;
+  st = device_view(x, &xd);
+  if (!st) st = device_view(f, &fd);
+  if (st) return st;
+  IterArgs A;
+  st = fill_iter_args(p, c, A);
+  if (st) return st;
+  if (!p->d_zero_iter) {
+    st = cuda_status(cudaMalloc(&p->d_zero_iter, sizeof(int)));
+    if (st) return st;
+    st = cuda_status(cudaMemset(p->d_zero_iter, 0, sizeof(int)));
+    if (st) return st;
+  }
+  A.div = nullptr;
+  A.ndim = ndim;
+  A.nb = 1;
+  A.iteration = p->d_zero_iter;
+  A.N = N;
+  A.inv_n = 1.0;
+  A.x_in = static_cast<const double*>(xd);
+  A.x_rows = 1;
+  return run_fused(p, A, c, nullptr, static_cast<double*>(fd), stream);
+}
+
 int mf_vegas_iteration(const mf_process* pc, const mf_integrand_config* c, const double* grid, int nb, uint64_t seed,
                        uint32_t stream_id, const int* iteration, int64_t N, double* results, double* f_out,
                        float* u_out, void* stream) {

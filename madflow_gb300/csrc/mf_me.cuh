@@ -41,7 +41,9 @@ struct IterArgs {
   double q2;
   const int* newton_iters;  // device: iterations of the batch Newton rule (<= 0: per event)
   int f32q;
-  const double* x_in;  // optional [ndim][ld] points (integrand API): no Philox / VEGAS map, jac = 1
+  const double* x_in;  // optional points (integrand API): no Philox / VEGAS map, jac = 1;
+                       // [ndim][ld], or [ld][ndim] (rows, madflow's xrand) with x_rows
+  int x_rows;
   float* u_out;        // optional [ndim][ld] uniforms
   int64_t e0, ld;      // the slice's first event in the call (Philox event index, x_in / u_out column)
                        // and the call's event count (x_in / u_out row length)
@@ -110,7 +112,10 @@ template <class P>
 MF_DO void event_point(const IterArgs& A, int64_t e, int it, const P* sdiv, P* x, P& jac, bool store) {
   const int64_t g = A.e0 + e;  // the event's index in the call
   if (A.x_in) {
-    for (int d = 0; d < A.ndim; ++d) x[d] = (P)A.x_in[(int64_t)d * A.ld + g];
+    if (A.x_rows)
+      for (int d = 0; d < A.ndim; ++d) x[d] = (P)A.x_in[g * A.ndim + d];
+    else
+      for (int d = 0; d < A.ndim; ++d) x[d] = (P)A.x_in[(int64_t)d * A.ld + g];
     jac = P(1);
     return;
   }

@@ -83,13 +83,31 @@ class FusedIntegrand:
         _lib.call("mf_integrand_ndim", self.matrix.handle, ctypes.byref(self._cs), ctypes.byref(nd))
         self.n_dim = nd.value
 
-    def __call__(self, xrand, n_dim=None, weight=None):
-        """f(x) for x (N, ndim); events failing the cuts give 0."""
-        x = to_device(xrand)
+    def __call__(self, xrand, n_dim=None, weight=None, out=None):
+        """f(x) for x (N, ndim); events failing the cuts give 0.
+
+        x in page-locked host memory (a pinned float64 CPU tensor) is read
+        by the kernels directly (mf_integrand_rows, zero-copy over the host
+        link), as is `out` (optional, float64 (N,), pinned CPU or CUDA),
+        which then receives f; other inputs are copied to the device first.
+        Returns f (out if given)."""
+        if isinstance(xrand, torch.Tensor) and xrand.device.type == "cpu" and xrand.is_pinned() \
+                and xrand.dtype == DTYPE and xrand.dim() == 2 and xrand.is_contiguous():
+            x = xrand
+        else:
+            x = to_device(xrand)
+        if x.dim() != 2 or x.shape[1] != self.n_dim:
+            raise ValueError(f"x must have shape (N, {self.n_dim}), got {tuple(x.shape)}")
         N = x.shape[0]
-        xs = x.T.contiguous()
-        f = torch.empty(N, dtype=DTYPE, device=device())
-        _lib.call("mf_integrand", self.matrix.handle, ctypes.byref(self._cs), xs.data_ptr(), N, f.data_ptr(),
+        if out is None:
+            f = torch.empty(N, dtype=DTYPE, device=device())
+        else:
+            ok = out.dtype == DTYPE and out.dim() == 1 and out.shape[0] == N and out.is_contiguous() and (
+                out.device.type == "cuda" or out.is_pinned())
+            if not ok:
+                raise ValueError("out must be a contiguous float64 (N,) CUDA or pinned CPU tensor")
+            f = out
+        _lib.call("mf_integrand_rows", self.matrix.handle, ctypes.byref(self._cs), x.data_ptr(), N, f.data_ptr(),
                   stream_ptr())
         return f
 
