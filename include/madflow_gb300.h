@@ -144,11 +144,13 @@ typedef struct {
    * events in consecutive slices of at most events_limit events, as
    * vegasflow's VegasFlow(events_limit=...) hands the integrand one slice per
    * call (scripts/madflow_exec.py:474-487, config.py:121-176).  The handle's
-   * scratch then holds one slice instead of the call (1.8 KB per event for
-   * four gluons, mixed; mf_process_scratch_bytes), the batch Newton rule of
+   * scratch then holds two slices instead of the call (1.8 KB per event for
+   * four gluons, mixed; mf_process_scratch_bytes): the phase space of the
+   * next slice runs on a stream of the handle while the current slice's
+   * matrix element runs on the caller's stream.  The batch Newton rule of
    * the massive phase space runs per slice, and the slices' sums add up in
-   * results.  Uniforms and the per-event outputs do not depend on the
-   * slicing.  0: one slice.  < 0: MF_ERR_ARG.  Stage timing
+   * results in slice order.  Uniforms and the per-event outputs do not
+   * depend on the slicing.  0: one slice.  < 0: MF_ERR_ARG.  Stage timing
    * (mf_process_set_timing) records one-slice calls only. */
   int64_t events_limit;
 } mf_integrand_config;

@@ -509,6 +509,25 @@ __global__ void __launch_bounds__(128) qq3_smatrix_kernel(int channel, const dou
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// per-event pipeline buffers of one slice of a call
+struct SliceBuf {
+  int4* prep = nullptr;
+  double* state = nullptr;
+  double* pref = nullptr;
+  double* me = nullptr;
+  unsigned char* bins = nullptr;
+  double* extra = nullptr;
+  double* qqin = nullptr;
+  int* kmin = nullptr;
+  int64_t cap = 0, extra_cap = 0, qqin_cap = 0;
+  void release() {
+    for (void* q : {(void*)prep, (void*)state, (void*)pref, (void*)me, (void*)bins, (void*)extra, (void*)qqin,
+                    (void*)kmin})
+      if (q) cudaFree(q);
+    *this = SliceBuf();
+  }
+};
+
 struct mf_process {
   int k, prec;
   int ncomb, nperm, ndiags;
@@ -534,6 +553,12 @@ struct mf_process {
   int64_t qqin_cap = 0;
   unsigned char* d_bins = nullptr;  // [MF_MAX_DIM][cap]
   int64_t event_cap = 0;
+  // the second buffer set of a call in slices (the odd slices), the side
+  // stream their phase-space passes run on and the events that order the
+  // two streams
+  SliceBuf alt;
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_ps[2] = {nullptr, nullptr}, ev_acc[2] = {nullptr, nullptr};
   int* d_err = nullptr;     // device error flags of the kernels (bit 0: a tensor-core wait ran out,
                             // bit 1: non-finite weights were zeroed)
   unsigned long long* d_nonfinite = nullptr;  // count of the zeroed non-finite weights
@@ -611,6 +636,10 @@ int mf_process_destroy(mf_process* p) {
   if (p->d_nonfinite) cudaFree(p->d_nonfinite);
   if (p->d_extra) cudaFree(p->d_extra);
   if (p->d_qqin) cudaFree(p->d_qqin);
+  p->alt.release();
+  if (p->side) cudaStreamDestroy(p->side);
+  for (cudaEvent_t e : {p->ev_start, p->ev_ps[0], p->ev_ps[1], p->ev_acc[0], p->ev_acc[1]})
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : p->tev)
     if (e) cudaEventDestroy(e);
   delete p;
@@ -987,20 +1016,100 @@ static int ensure_events(mf_process* p, int64_t N) {
   return MF_OK;
 }
 
-// One pass of the pipeline over n events, the slice [A.e0, A.e0 + n) of the
-// call: phase-space first pass (with the batch Newton minimum of the slice),
-// phase space, |M|^2, accumulation.  results (optional) [2 + ndim*nb]
-// (add_results: added to, for the later slices); f_out (optional) [n].
-static int run_slice(mf_process* p, IterArgs A, int64_t n, const mf_integrand_config* c, double* results,
-                     int add_results, double* f_out, bool timed, void* stream) {
+// The buffers of one slice (grown to n events, as ensure_events does for
+// the handle's own set)
+static int ensure_slicebuf(const mf_process* p, SliceBuf& b, int64_t n, bool qq) {
+  if (b.cap < n) {
+    for (void** q : {(void**)&b.prep, (void**)&b.state, (void**)&b.pref, (void**)&b.me, (void**)&b.bins}) {
+      cudaFree(*q);
+      *q = nullptr;
+    }
+    b.cap = 0;
+    int st = cuda_status(cudaMalloc(&b.prep, (size_t)mf_prep_bytes(p->k, p->prec) * n));
+    if (!st) st = cuda_status(cudaMalloc(&b.state, sizeof(double) * (size_t)mf_state_words(p->k) * n));
+    if (!st) st = cuda_status(cudaMalloc(&b.pref, sizeof(double) * (size_t)n));
+    if (!st) st = cuda_status(cudaMalloc(&b.me, sizeof(double) * (size_t)n));
+    if (!st) st = cuda_status(cudaMalloc(&b.bins, (size_t)MF_MAX_DIM * n));
+    if (st) return st;
+    b.cap = n;
+  }
+  if (qq && b.extra_cap < n) {
+    cudaFree(b.extra);
+    b.extra = nullptr;
+    b.extra_cap = 0;
+    int st = cuda_status(cudaMalloc(&b.extra, sizeof(double) * (size_t)n));
+    if (st) return st;
+    b.extra_cap = n;
+  }
+  if (qq && p->k == 3 && b.qqin_cap < n) {
+    cudaFree(b.qqin);
+    b.qqin = nullptr;
+    b.qqin_cap = 0;
+    int st = cuda_status(cudaMalloc(&b.qqin, sizeof(double) * 26 * (size_t)n));
+    if (st) return st;
+    b.qqin_cap = n;
+  }
+  if (!b.kmin) {
+    int st = cuda_status(cudaMalloc(&b.kmin, sizeof(int)));
+    if (st) return st;
+  }
+  return MF_OK;
+}
+
+// the handle's own buffer set as a SliceBuf view
+static SliceBuf main_buffers(mf_process* p) {
+  SliceBuf b;
+  b.prep = p->d_prep;
+  b.state = p->d_state;
+  b.pref = p->d_pref;
+  b.me = p->d_me;
+  b.bins = p->d_bins;
+  b.extra = p->d_extra;
+  b.qqin = p->d_qqin;
+  b.kmin = p->d_kmin;
+  return b;
+}
+
+static void bind_slice(IterArgs& A, const mf_process* p, const SliceBuf& b, int64_t n) {
   A.N = n;
-  A.prep = p->d_prep;
-  A.state = p->d_state;
-  A.pref = p->d_pref;
-  A.me = p->d_me;
-  A.extra = A.qq ? p->d_extra : nullptr;
-  A.qqin = A.qq && p->k == 3 ? p->d_qqin : nullptr;
-  A.bins = A.x_in ? nullptr : p->d_bins;
+  A.prep = b.prep;
+  A.state = b.state;
+  A.pref = b.pref;
+  A.me = b.me;
+  A.extra = A.qq ? b.extra : nullptr;
+  A.qqin = A.qq && p->k == 3 ? b.qqin : nullptr;
+  A.bins = A.x_in ? nullptr : b.bins;
+  A.newton_iters = b.kmin;
+}
+
+// The phase-space half of a slice (A bound to its buffers): the first pass
+// with the batch Newton minimum of the slice, the second pass with the
+// records, and the light-quark channels of p p > t t~ j.
+static int slice_phase_space(mf_process* p, IterArgs& A, const mf_integrand_config* c, const SliceBuf& b,
+                             bool timed, cudaStream_t st_) {
+  const bool per_event = c->newton_rule == MF_NEWTON_PER_EVENT;
+  if (timed) cudaEventRecord(p->tev[0], st_);
+  set_int_kernel<<<1, 1, 0, st_>>>(b.kmin, per_event ? 0 : 11);
+  if (mf_launch_seed(p->k, p->prec, A, b.kmin, per_event ? 0 : 1, st_)) return last_launch();
+  if (timed) cudaEventRecord(p->tev[1], st_);
+  if (mf_launch_ps(p->k, p->prec, A, st_)) return last_launch();
+  if (A.qqin) {
+    const int grid = blocks_for(4 * A.N, 128);  // four lanes per event
+    if (p->prec == MF_PREC_FP64)
+      qq3_channels_kernel<double><<<grid, 128, 0, st_>>>(A);
+    else
+      qq3_channels_kernel<float><<<grid, 128, 0, st_>>>(A);
+  }
+  if (timed) cudaEventRecord(p->tev[2], st_);
+  return last_launch();
+}
+
+// The matrix-element half of a slice: |M|^2 and the accumulation.  results
+// (optional) [2 + ndim*nb] (add_results: added to, for the later slices);
+// f_out (optional) [n].
+static int slice_matrix_element(mf_process* p, IterArgs& A, double* results, int add_results, double* f_out,
+                                bool timed, void* stream) {
+  const int64_t n = A.N;
   int accum_grid = 8 * 152;
   {
     int dev = 0, sms = 0;
@@ -1012,33 +1121,13 @@ static int run_slice(mf_process* p, IterArgs A, int64_t n, const mf_integrand_co
   const int width = 2 + A.ndim * A.nb;
   int st = ensure_partials(p, (size_t)accum_grid * width);
   if (st) return st;
-  A.newton_iters = p->d_kmin;
-  const bool per_event = c->newton_rule == MF_NEWTON_PER_EVENT;
-  auto mark = [&](int i) {
-    if (timed) cudaEventRecord(p->tev[i], S(stream));
-  };
-  mark(0);
-  set_int_kernel<<<1, 1, 0, S(stream)>>>(p->d_kmin, per_event ? 0 : 11);
-  if (mf_launch_seed(p->k, p->prec, A, p->d_kmin, per_event ? 0 : 1, S(stream))) return last_launch();
-  mark(1);
-  if (mf_launch_ps(p->k, p->prec, A, S(stream))) return last_launch();
-  if (A.qqin) {
-    const int grid = blocks_for(4 * n, 128);  // four lanes per event
-    if (p->prec == MF_PREC_FP64)
-      qq3_channels_kernel<double><<<grid, 128, 0, S(stream)>>>(A);
-    else
-      qq3_channels_kernel<float><<<grid, 128, 0, S(stream)>>>(A);
-    st = last_launch();
-    if (st) return st;
-  }
-  mark(2);
   if (autotune_wanted(p, n, stream)) {
     st = autotune_me(p, A.prep, n, A.pref, A.me, stream);
     if (st) return st;
   }
   if (mf_launch_me(p->k, p->prec, A.prep, n, A.pref, A.me, nullptr, p->d_err, p->tune, p->d_ws, S(stream)))
     return last_launch();
-  mark(3);
+  if (timed) cudaEventRecord(p->tev[3], S(stream));
   size_t shm = (size_t)(A.ndim * A.nb + 3 * 256) * sizeof(double);
   static bool attr_done[64] = {false};
   st = smem_attr_once((const void*)accum_kernel, attr_done);
@@ -1049,21 +1138,40 @@ static int run_slice(mf_process* p, IterArgs A, int64_t n, const mf_integrand_co
   if (results)
     reduce_partials_kernel<<<(width + 127) / 128, 128, 0, S(stream)>>>(p->d_partials, accum_grid, width, results,
                                                                        add_results);
-  mark(4);
+  if (timed) cudaEventRecord(p->tev[4], S(stream));
   return last_launch();
+}
+
+static int ensure_pipeline(mf_process* p) {
+  if (!p->side) {
+    int st = cuda_status(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+    if (st) return st;
+  }
+  for (cudaEvent_t* e : {&p->ev_start, &p->ev_ps[0], &p->ev_ps[1], &p->ev_acc[0], &p->ev_acc[1]})
+    if (!*e) {
+      int st = cuda_status(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+      if (st) return st;
+    }
+  return MF_OK;
 }
 
 // The pipeline over the A.N events of a call, in consecutive slices of at
 // most c->events_limit events (0: one slice), as the reference's integrator
 // hands its integrand one slice of events_limit events per call
-// (scripts/madflow_exec.py:474-487): the scratch holds one slice, the batch
-// Newton rule runs per slice, the slices' sums add up in results.  The
-// Philox event index, x_in, u_out, f_out and ps_out run over the whole call.
+// (scripts/madflow_exec.py:474-487): the batch Newton rule runs per slice,
+// the slices' sums add up in results (in slice order).  The Philox event
+// index, x_in, u_out, f_out and ps_out run over the whole call.
+// With several slices, two buffer sets alternate: the phase-space passes of
+// slice i + 1 run on the handle's side stream while slice i's matrix element
+// runs on the caller's stream (events order the two: a slice's matrix
+// element waits for its phase space, a buffer's next phase space for the
+// accumulation of the slice before).  The scratch then holds two slices.
 static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, double* results, double* f_out,
                      void* stream) {
   if (c->events_limit < 0) return MF_ERR_ARG;
   const int64_t total = A.N;
   const int64_t slice = (c->events_limit > 0 && c->events_limit < total) ? c->events_limit : total;
+  const bool piped = slice < total;
   int st = ensure_events(p, slice);
   if (st) return st;
   if (A.qq && p->extra_cap < slice) {
@@ -1086,9 +1194,14 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
     st = cuda_status(cudaMalloc(&p->d_kmin, sizeof(int)));
     if (st) return st;
   }
+  if (piped) {
+    st = ensure_slicebuf(p, p->alt, slice, A.qq != 0);
+    if (!st) st = ensure_pipeline(p);
+    if (st) return st;
+  }
   // stage timing: one slice, and not while the stream is being captured into a graph
   bool timed = false;
-  if (p->timing && slice == total) {
+  if (p->timing && !piped) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(S(stream), &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
       timed = true;
@@ -1100,14 +1213,36 @@ static int run_fused(mf_process* p, IterArgs& A, const mf_integrand_config* c, d
   A.ld = total;
   const int npart = p->k + 2;
   double* ps_out = A.ps_out;
-  for (int64_t off = 0; off < total; off += slice) {
-    const int64_t n = total - off < slice ? total - off : slice;
-    A.e0 = off;
-    A.ps_out = ps_out ? ps_out + off * npart * 4 : nullptr;
-    st = run_slice(p, A, n, c, results, off > 0, f_out ? f_out + off : nullptr, timed, stream);
-    if (st) return st;
+  const SliceBuf bufs[2] = {main_buffers(p), p->alt};
+  if (piped) {
+    // the side stream starts after the caller's earlier work
+    cudaEventRecord(p->ev_start, S(stream));
+    cudaStreamWaitEvent(p->side, p->ev_start, 0);
   }
-  return MF_OK;
+  int i = 0;
+  for (int64_t off = 0; off < total; off += slice, ++i) {
+    const int64_t n = total - off < slice ? total - off : slice;
+    const int b = piped ? (i & 1) : 0;
+    IterArgs As = A;
+    As.e0 = off;
+    As.ps_out = ps_out ? ps_out + off * npart * 4 : nullptr;
+    bind_slice(As, p, bufs[b], n);
+    if (piped) {
+      if (i >= 2) cudaStreamWaitEvent(p->side, p->ev_acc[b], 0);
+      st = slice_phase_space(p, As, c, bufs[b], false, p->side);
+      if (st) return st;
+      cudaEventRecord(p->ev_ps[b], p->side);
+      cudaStreamWaitEvent(S(stream), p->ev_ps[b], 0);
+      st = slice_matrix_element(p, As, results, off > 0, f_out ? f_out + off : nullptr, false, stream);
+      if (st) return st;
+      cudaEventRecord(p->ev_acc[b], S(stream));
+    } else {
+      st = slice_phase_space(p, As, c, bufs[b], timed, S(stream));
+      if (!st) st = slice_matrix_element(p, As, results, off > 0, f_out ? f_out + off : nullptr, timed, stream);
+      if (st) return st;
+    }
+  }
+  return last_launch();
 }
 
 int mf_process_tuning(const mf_process* p, int* colour, int* waves, int* tuned, float* ms) {
@@ -1179,6 +1314,8 @@ int mf_process_scratch_bytes(const mf_process* p, int64_t* bytes) {
               p->qqin_cap * 26 * (int64_t)sizeof(double) +
               (int64_t)p->partial_cap * (int64_t)sizeof(double);
   if (p->d_ws) b += mf_ws_bytes(p->k, p->prec);
+  b += p->alt.cap * per_event + p->alt.extra_cap * (int64_t)sizeof(double) +
+       p->alt.qqin_cap * 26 * (int64_t)sizeof(double);
   *bytes = b;
   return MF_OK;
 }
