@@ -658,7 +658,7 @@ MF_DO void mark_rest_nan(int64_t e, int64_t N, int64_t stride, const double* __r
 // the amplitude matrix (Re, then Im) at a time, K in chunks of 40 flows
 // (5 MMA K-steps each, A_hi and A_lo), C^T resident in shared memory, the
 // accumulator (128 columns) in tensor memory; else the row-loop SIMT sum.
-constexpr int MF_GWS_NT = 512;  // threads per block of the global-workspace kernel
+constexpr int MF_GWS_NT = 640;  // threads per block of the global-workspace kernel
 template <class T, int K> struct RecSmemG {
   PrepRec<T, K> pr;
   T red[MF_GWS_NT / 32];
