@@ -211,3 +211,29 @@ def test_negative_limit_rejected(cuda):
     assert st == _lib.MF_ERR_ARG
     with pytest.raises(ValueError):
         FusedIntegrand(2, kind=0, sqrts=1000.0, precision=0, events_limit=0)
+
+
+@pytest.mark.parametrize("k", [2, 3])
+def test_sliced_pp_channels_equal_one_slice(cuda, k):
+    """p p > t t~ (j) in slices (the quark channels' buffers alternate with
+    the slices too), per-event Newton rule: f_out equals one slice bit for
+    bit."""
+    torch = cuda
+    from madflow_gb300 import _lib
+    from madflow_gb300.vegas import FusedIntegrand
+
+    N, nb, limit = 30000, 50, 7000
+    cuts = dict(ptmin=30.0, etamax=4.0) if k == 3 else {}
+    integ = FusedIntegrand(k, kind=1, sqrts=13000.0, precision=1, initial_states="pp",
+                           newton_rule=_lib.MF_NEWTON_PER_EVENT, **cuts)
+    grid = _grid(torch, integ.n_dim, nb, 6)
+    it = torch.tensor([1], dtype=torch.int32, device="cuda")
+    outs = []
+    for lim in (None, limit):
+        res = torch.empty(2 + integ.n_dim * nb, dtype=torch.float64, device="cuda")
+        f = torch.empty(N, dtype=torch.float64, device="cuda")
+        integ.iteration(grid, 3, 0, it, N, res, f_out=f, events_limit=lim)
+        outs.append((_np(res).copy(), _np(f).copy()))
+    np.testing.assert_array_equal(outs[1][1], outs[0][1])
+    assert rel_err(outs[1][0][:2], outs[0][0][:2]) < 1e-13
+    assert np.count_nonzero(outs[0][1]) > N // 2
