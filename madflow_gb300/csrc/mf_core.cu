@@ -485,6 +485,20 @@ __global__ void qq_ttx_kernel(int prec, const double* __restrict__ ps, int64_t N
   }
 }
 template <class T>
+__global__ void __launch_bounds__(128) gg2_smatrix_kernel(const double* __restrict__ ps, int64_t N, double mt,
+                                                          double wt, const double* __restrict__ coup, int64_t cstride,
+                                                          double* __restrict__ out, double* __restrict__ hel_out) {
+  const T sqh = (T)mf_consts(true).sqh;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    double p[4][4];
+    for (int i = 0; i < 4; ++i)
+      for (int c = 0; c < 4; ++c) p[i][c] = ps[((int64_t)i * 4 + c) * N + e];
+    const double* cp = coup + 6 * cstride * e;
+    out[e] = gg2_me<T>(p, mt, wt, {cp[0], cp[1]}, {cp[2], cp[3]}, sqh, hel_out ? hel_out + e : nullptr, N);
+  }
+}
+
+template <class T>
 __global__ void __launch_bounds__(128) qq3_smatrix_kernel(int channel, const double* __restrict__ ps, int64_t N,
                                                           double mt, double wt, const double* __restrict__ coup,
                                                           int64_t cstride, double* __restrict__ out) {
@@ -673,6 +687,16 @@ int mf_smatrix(const mf_process* p, const double* ps, int64_t N, double mt, doub
   if (!p || (N > 0 && (!ps || !coup || !out)) || N < 0 || (cstride != 0 && cstride != 1)) return MF_ERR_ARG;
   if (N == 0) return MF_OK;
   mf_process* pm = const_cast<mf_process*>(p);
+  if (p->k == 2) {
+    // g g > t t~: one thread per event straight from the momenta
+    if (p->prec == MF_PREC_FP64)
+      gg2_smatrix_kernel<double><<<blocks_for(N, 128), 128, 0, S(stream)>>>(ps, N, mt, wt, coup, cstride, out,
+                                                                             hel_out);
+    else
+      gg2_smatrix_kernel<float><<<blocks_for(N, 128), 128, 0, S(stream)>>>(ps, N, mt, wt, coup, cstride, out,
+                                                                            hel_out);
+    return last_launch();
+  }
   int st = ensure_events(pm, N);
   if (st) return st;
   if (mf_launch_prep(p->k, p->prec, ps, N, mt, wt, coup, cstride, pm->d_prep, S(stream))) return last_launch();
@@ -1121,12 +1145,15 @@ static int slice_matrix_element(mf_process* p, IterArgs& A, double* results, int
   const int width = 2 + A.ndim * A.nb;
   int st = ensure_partials(p, (size_t)accum_grid * width);
   if (st) return st;
-  if (autotune_wanted(p, n, stream)) {
-    st = autotune_me(p, A.prep, n, A.pref, A.me, stream);
-    if (st) return st;
+  // g g > t t~: |M|^2 came with the phase space (ps_iter_kernel)
+  if (p->k != 2) {
+    if (autotune_wanted(p, n, stream)) {
+      st = autotune_me(p, A.prep, n, A.pref, A.me, stream);
+      if (st) return st;
+    }
+    if (mf_launch_me(p->k, p->prec, A.prep, n, A.pref, A.me, nullptr, p->d_err, p->tune, p->d_ws, S(stream)))
+      return last_launch();
   }
-  if (mf_launch_me(p->k, p->prec, A.prep, n, A.pref, A.me, nullptr, p->d_err, p->tune, p->d_ws, S(stream)))
-    return last_launch();
   if (timed) cudaEventRecord(p->tev[3], S(stream));
   size_t shm = (size_t)(A.ndim * A.nb + 3 * 256) * sizeof(double);
   static bool attr_done[64] = {false};

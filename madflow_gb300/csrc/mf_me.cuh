@@ -22,6 +22,7 @@
 #include "mf_me_rec.cuh"
 #include "mf_qq.cuh"
 #include "mf_qq3.cuh"
+#include "mf_gg2.cuh"
 
 struct IterArgs {
   const double* div;  // VEGAS grid [ndim][nb+1]
@@ -331,7 +332,11 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
         for (int c = 0; c < 4; ++c) q[4 * i + c] = ok ? t[c] : 0.0;
       }
     }
-    if (ok) {
+    if constexpr (K == 2) {
+      // g g > t t~: |M|^2 here, one thread per event, instead of a record
+      // for a matrix-element kernel
+      A.me[e] = ok ? gg2_me<T>(p, A.mt, A.wt, A.gc10, A.gc11, (T)KC.sqh) : 0.0;
+    } else if (ok) {
       PrepRec<T, K> r;
       prep_event<T, K>(r, p, A.mt, A.wt, A.gc10, A.gc11, A.gc12);
       const int4* src = reinterpret_cast<const int4*>(&r);

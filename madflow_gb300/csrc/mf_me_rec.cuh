@@ -1040,7 +1040,7 @@ __global__ void __launch_bounds__(MF_REC_NT, sizeof(T) == 4 ? 4 : 2)
                        double* __restrict__ out, double* __restrict__ hel_out) {
   using R = RecTraits<K>;
   constexpr int WPB = MF_REC_NT / 32, NW = prep_words<T, K>();
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
   RecSmem<T, K>& S = reinterpret_cast<RecSmem<T, K>*>(smem_raw)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   const int64_t G = (int64_t)gridDim.x * WPB;
