@@ -193,6 +193,11 @@ def iteration_estimate(s1, s2, n_per_rank, world=1):
     w^2 over world ranks of n events each: the mean of f jac over all
     M = world*n events and the error of that mean."""
     n, m = float(n_per_rank), float(n_per_rank) * world
+    if world == 1:
+        # the unsharded expression (VegasFlow.run_event), so one rank gives
+        # the same bits
+        var = (n * s2 - s1 * s1) / (n - 1.0)
+        return s1, math.sqrt(max(var, 0.0))
     res = s1 / world
     var = n * n * (s2 - s1 * s1 / m) / (m * (m - 1.0))
     return res, math.sqrt(max(var, 0.0))
