@@ -438,8 +438,9 @@ def test_autotuner(cuda):
 def test_smatrix_multi_process_launch(cuda, oracle, prec):
     """g g > t t~, t t~ g and t t~ g g batches of uneven sizes in one
     persistent launch give the single-process results (FP64: to rounding,
-    1e-13, and 1e-12 for g g > t t~, whose single-process launch evaluates
-    its three diagrams in one thread per event in another operation order;
+    1e-13, and 1e-11 for g g > t t~, whose single-process launch evaluates
+    its three diagrams in one thread per event (as the reference's module
+    does) while the persistent launch runs the colour-ordered recursion;
     mixed: within 1e-5, the single-process g g > t t~ g g colour sum runs on
     the tensor cores)."""
     from madflow_gb300.matrix import PROCESSES, smatrix_multi
@@ -454,7 +455,7 @@ def test_smatrix_multi_process_launch(cuda, oracle, prec):
     outs = [_np(o) for o in smatrix_multi(batches, MT, WT, GC10, GC11, GC12)]
     for k, o, s in zip((2, 3, 4), outs, singles):
         if prec == 0:
-            assert rel_err(o, s) < (1e-12 if k == 2 else 1e-13)
+            assert rel_err(o, s) < (1e-11 if k == 2 else 1e-13)
         else:
             assert rel_err(o, s) < 1e-5
 
