@@ -153,6 +153,51 @@ __global__ void __launch_bounds__(128) flow_layer_kernel(const float* z_in, floa
   }
 }
 
+// C(m, n) = sum_k A(m, k) B(k, n) over shared-memory operands with strides
+// (A(m, k) at A[m sam + k sak], B(k, n) at B[k sbk + n sbn]), each thread
+// one TM x TN block held in registers: rows m0 .. m0 + TM - 1, columns n,
+// n + NB, .. (NB = ceil(N / TN) column groups, so the threads of a warp read
+// neighbouring columns of B and the same rows of A).  Out-of-range rows and
+// columns read a valid element and their results are dropped; epi(m, n, c)
+// receives every result in range.
+template <int TM, int TN, class Epi>
+__device__ __forceinline__ void tile_gemm(int M, int N, int K, const float* __restrict__ A, int sam, int sak,
+                                          const float* __restrict__ B, int sbk, int sbn, int tid, int nt, Epi epi) {
+  const int nbk = (N + TN - 1) / TN, nblk = (M + TM - 1) / TM * nbk;
+  for (int blk = tid; blk < nblk; blk += nt) {
+    const int m0 = (blk / nbk) * TM, n0 = blk % nbk;
+    int am[TM], bn[TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i) am[i] = min(m0 + i, M - 1) * sam;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) bn[j] = min(n0 + j * nbk, N - 1) * sbn;
+    float acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
+#pragma unroll 4
+    for (int k = 0; k < K; ++k) {
+      float a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = A[am[i] + k * sak];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = B[k * sbk + bn[j]];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        const int m = m0 + i, n = n0 + j * nbk;
+        if (m < M && n < N) epi(m, n, acc[i][j]);
+      }
+  }
+}
+
 // Gradient of one coupling layer in the density direction.  z_in [N][dim]
 // the layer's input, g_out [N][dim] = dL/d(layer output), gl [N] = dL/d(log
 // pdf sum) -> g_in [N][dim] = dL/d(layer input); part [gridDim][grad_floats]
@@ -195,28 +240,15 @@ __global__ void __launch_bounds__(FNT, 1) flow_grad_kernel(const float* __restri
     }
     for (int i = tid; i < np * dim; i += FNT) g_in[t0 * dim + i] = g_out[t0 * dim + i];
     __syncthreads();
-    for (int i = tid; i < FT * FH; i += FNT) {
-      const int p = i / FH, j = i % FH;
-      float t = s.b1[j];
-      for (int c = 0; c < na; ++c) t = fmaf(s.W1[j * s.w1s + c], A[p * FA_MAX + c], t);
-      H1[i] = fmaxf(t, 0.f);
-    }
+    // H1 = relu(A W1^T + b1), H2 = relu(H1 W2^T + b2), P = H2 W3^T + b3
+    tile_gemm<4, 2>(FT, FH, na, A, FA_MAX, 1, s.W1, 1, s.w1s, tid, FNT,
+                    [&](int p, int j, float c) { H1[p * FH + j] = fmaxf(c + s.b1[j], 0.f); });
     __syncthreads();
-    for (int i = tid; i < FT * FH; i += FNT) {
-      const int p = i / FH, j = i % FH;
-      float t = s.b2[j];
-#pragma unroll 16
-      for (int k = 0; k < FH; ++k) t = fmaf(s.W2[j * FH_P + k], H1[p * FH + k], t);
-      H2[i] = fmaxf(t, 0.f);
-    }
+    tile_gemm<4, 2>(FT, FH, FH, H1, FH, 1, s.W2, 1, FH_P, tid, FNT,
+                    [&](int p, int j, float c) { H2[p * FH + j] = fmaxf(c + s.b2[j], 0.f); });
     __syncthreads();
-    for (int i = tid; i < FT * no; i += FNT) {
-      const int p = i / no, o = i % no;
-      float t = s.b3[o];
-#pragma unroll 16
-      for (int j = 0; j < FH; ++j) t = fmaf(s.W3[o * FH_P + j], H2[p * FH + j], t);
-      P[i] = t;
-    }
+    tile_gemm<4, 4>(FT, no, FH, H2, FH, 1, s.W3, 1, FH_P, tid, FNT,
+                    [&](int p, int o, float c) { P[p * no + o] = c + s.b3[o]; });
     __syncthreads();
     // the transform's backward per (point, dimension): dL/dx to g_in, the
     // parameters' gradient over the parameters (0 for points past the end)
@@ -232,19 +264,10 @@ __global__ void __launch_bounds__(FNT, 1) flow_grad_kernel(const float* __restri
     }
     __syncthreads();
     // G2 = (GP W3) * [H2 > 0]; dW3 += GP^T H2, db3 += sum GP
-    for (int i = tid; i < FT * FH; i += FNT) {
-      const int p = i / FH, j = i % FH;
-      float t = 0.f;
-      for (int o = 0; o < no; ++o) t = fmaf(P[p * no + o], s.W3[o * FH_P + j], t);
-      G2[i] = H2[i] > 0.f ? t : 0.f;
-    }
-    for (int i = tid; i < no * FH; i += FNT) {
-      const int o = i / FH, j = i % FH;
-      float t = 0.f;
-#pragma unroll 8
-      for (int p = 0; p < FT; ++p) t = fmaf(P[p * no + o], H2[p * FH + j], t);
-      pW3[i] += t;
-    }
+    tile_gemm<4, 2>(FT, FH, no, P, no, 1, s.W3, FH_P, 1, tid, FNT,
+                    [&](int p, int j, float c) { G2[p * FH + j] = H2[p * FH + j] > 0.f ? c : 0.f; });
+    tile_gemm<4, 4>(no, FH, FT, P, 1, no, H2, FH, 1, tid, FNT,
+                    [&](int o, int j, float c) { pW3[o * FH + j] += c; });
     for (int o = tid; o < no; o += FNT) {
       float t = 0.f;
       for (int p = 0; p < FT; ++p) t += P[p * no + o];
@@ -252,20 +275,10 @@ __global__ void __launch_bounds__(FNT, 1) flow_grad_kernel(const float* __restri
     }
     __syncthreads();
     // G1 = (G2 W2) * [H1 > 0]; dW2 += G2^T H1, db2 += sum G2
-    for (int i = tid; i < FT * FH; i += FNT) {
-      const int p = i / FH, k = i % FH;
-      float t = 0.f;
-#pragma unroll 16
-      for (int j = 0; j < FH; ++j) t = fmaf(G2[p * FH + j], s.W2[j * FH_P + k], t);
-      G1[i] = H1[i] > 0.f ? t : 0.f;
-    }
-    for (int i = tid; i < FH * FH; i += FNT) {
-      const int j = i / FH, k = i % FH;
-      float t = 0.f;
-#pragma unroll 8
-      for (int p = 0; p < FT; ++p) t = fmaf(G2[p * FH + j], H1[p * FH + k], t);
-      pW2[i] += t;
-    }
+    tile_gemm<4, 2>(FT, FH, FH, G2, FH, 1, s.W2, FH_P, 1, tid, FNT,
+                    [&](int p, int k, float c) { G1[p * FH + k] = H1[p * FH + k] > 0.f ? c : 0.f; });
+    tile_gemm<4, 4>(FH, FH, FT, G2, 1, FH, H1, FH, 1, tid, FNT,
+                    [&](int j, int k, float c) { pW2[j * FH + k] += c; });
     for (int j = tid; j < FH; j += FNT) {
       float t = 0.f;
       for (int p = 0; p < FT; ++p) t += G2[p * FH + j];
