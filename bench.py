@@ -578,8 +578,14 @@ def _public(d):
 
 
 def _flow(args, integ, layers, bins, bf16):
+    """bf16: False (TF32 tensor-core sampling), "tc" (BF16 tensor-core
+    sampling, both hand-written; training in the FP32 layer kernels) or True
+    (BF16 GEMMs through torch autocast / cuBLAS)."""
     from madflow_gb300.flow import NormalizingFlow
 
+    if bf16 == "tc":
+        return NormalizingFlow(integ.n_dim, n_layers=layers, bins=bins, hidden=args.flow_hidden, n_hidden=2, seed=0,
+                               tc_bf16=True)
     return NormalizingFlow(integ.n_dim, n_layers=layers, bins=bins, hidden=args.flow_hidden, n_hidden=2, seed=0,
                            bf16=bf16, tf32=not bf16)
 
@@ -588,7 +594,7 @@ def _flow_kernels(flow):
     if flow.bf16:
         return "BF16 GEMMs with FP32 accumulation (torch autocast, cuBLAS) and the hand-written transform kernels"
     train = "training in the hand-written FP32 layer kernels" if flow.native else "training through torch/cuBLAS"
-    sample = ("sampling in one tcgen05 TF32 kernel per layer" if flow.fused else
+    sample = (f"sampling in one tcgen05 {'BF16' if flow.tc_bf16 else 'TF32'} kernel per layer" if flow.fused else
               "sampling in the hand-written FP32 layer kernels" if flow.native else "sampling through torch/cuBLAS")
     return f"{sample}, {train}"
 
@@ -710,9 +716,9 @@ def flow_vs_vegas(args, cfg, target=1e-3):
     vg = _vegas_to_target(cfg, _lib.MF_PREC_MIXED, n, args.seed + 1, args.max_iter * 4, target)
     out = {"target_rel_error": target, "vegas": _public(vg)}
     out["vegas"]["unweighting_efficiency"] = _unweighting_efficiency(_sample_vegas(integ, vg["vegas"].grid, n, 77))
-    # the configuration's flow in the hand-written FP32 kernels, and with its
-    # BF16 GEMMs through cuBLAS
-    for key, bf16 in (("flow", False), ("flow_bf16_cublas", True)):
+    # the configuration's flow: hand-written FP32 training with TF32 or BF16
+    # tensor-core sampling, and with its BF16 GEMMs through cuBLAS
+    for key, bf16 in (("flow", False), ("flow_bf16", "tc"), ("flow_bf16_cublas", True)):
         fl, flow, grid = _flow_leg(args, integ, target, 6, 16, bf16, args.flow_vegas_iters, args.flow_vegas_events,
                                    n, 20, args.max_iter * 4)
         fl["unweighting_efficiency"] = _unweighting_efficiency(_sample_flow(integ, flow, grid, n, 78))

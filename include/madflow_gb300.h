@@ -392,6 +392,14 @@ int mf_flow_grad(const float* x, const float* params, const float* gy, const flo
 int mf_flow_inv_layer_tc(float* z, int64_t n, int dim, const int* ia, int na, const int* ib, int nb, int K,
                          const float* W1, const float* b1, const float* W2, const float* b2, const float* W3,
                          const float* b3, float* logq, int* err, void* stream);
+/* mf_flow_inv_layer_tc with BF16 GEMM operands (tcgen05 kind::f16, FP32
+ * accumulation): the MLP inputs, weights and hidden activations rounded to
+ * BF16 (to nearest even) where they enter a GEMM; biases, activations and the
+ * transform in FP32.  Same arguments, limits and error flags.  The sampled
+ * log density is that of the map as evaluated, so estimates stay unbiased. */
+int mf_flow_inv_layer_tc_bf16(float* z, int64_t n, int dim, const int* ia, int na, const int* ib, int nb, int K,
+                              const float* W1, const float* b1, const float* W2, const float* b2, const float* W3,
+                              const float* b3, float* logq, int* err, void* stream);
 
 /* Whole coupling layers in hand-written FP32 kernels (no counterpart in the
  * reference): the conditioner MLP na -> 64 -> 64 -> nb (2K+1) with ReLU (the

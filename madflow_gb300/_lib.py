@@ -121,6 +121,8 @@ _SIGS = {
                            + [c_dp, c_int64, c_void_p]),
     "mf_flow_inv_layer_tc": (c_int, [c_dp, c_int64, c_int, c_dp, c_int, c_dp, c_int, c_int, c_dp, c_dp, c_dp, c_dp,
                                      c_dp, c_dp, c_dp, c_dp, c_void_p]),
+    "mf_flow_inv_layer_tc_bf16": (c_int, [c_dp, c_int64, c_int, c_dp, c_int, c_dp, c_int, c_int, c_dp, c_dp, c_dp,
+                                          c_dp, c_dp, c_dp, c_dp, c_dp, c_void_p]),
 }
 
 

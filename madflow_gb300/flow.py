@@ -14,9 +14,10 @@ dimensions per half):
     transform's backward per point and dimension, weight gradients summed in
     a fixed order); Adam updates the weights;
   * sampling runs one tcgen05 kernel per coupling layer (``mf_flow_tc.cu``:
-    the MLP as three TF32 GEMMs with tensor-memory accumulators, the inverse
-    transform in the epilogue) when the layer fits it (its MLP outputs in at
-    most two chunks of whole dimensions, 256 columns each) and TF32 is
+    the MLP as three GEMMs on TF32 or BF16 operands with FP32 tensor-memory
+    accumulators, the inverse transform in the epilogue) when the layer fits
+    it (its MLP outputs in at most two chunks of whole dimensions, 256
+    columns each) and TF32 (``tf32=True``) or BF16 (``tc_bf16=True``) is
     chosen, else the hand-written FP32 layer kernel.
 Other shapes, and ``bf16=True``, run the conditioner through torch (cuBLAS,
 BF16 under autocast) with the hand-written transform kernels of
@@ -104,7 +105,7 @@ def _tc_chunks_fit(nb, np_):
 
 class NormalizingFlow(torch.nn.Module):
     def __init__(self, dim, n_layers=6, bins=16, hidden=64, n_hidden=2, seed=0, bf16=False, tf32=False, fused=None,
-                 native=None):
+                 native=None, tc_bf16=False):
         """native: train (and sample, where the tensor-core layer does not
         apply) with the hand-written FP32 layer kernels; by default whenever
         the shapes fit them (64 hidden units, two hidden layers, 4, 8 or 16
@@ -114,11 +115,16 @@ class NormalizingFlow(torch.nn.Module):
         coupling layer (mf_flow_inv_layer_tc: the MLP in TF32 and the inverse
         transform); by default whenever tf32 is set and the shapes fit it
         (also the MLP outputs in at most two chunks of whole dimensions, 256
-        columns each).  Reduced-precision GEMMs leave the estimates
+        columns each).  tc_bf16: the fused sampling kernel with BF16 GEMM
+        operands (mf_flow_inv_layer_tc_bf16) instead of TF32; it implies
+        fused sampling, and training stays in the FP32 layer kernels.
+        Reduced-precision GEMMs leave the estimates
         unbiased (the sampled log-density is the exact density of the map as
         evaluated); they perturb the training gradients."""
         super().__init__()
-        self.dim, self.K, self.bf16, self.tf32 = dim, bins, bf16, tf32
+        if tc_bf16 and bf16:
+            raise ValueError("tc_bf16 (hand-written BF16 sampling) and bf16 (torch autocast) exclude each other")
+        self.dim, self.K, self.bf16, self.tf32, self.tc_bf16 = dim, bins, bf16, tf32, bool(tc_bf16)
         self.masks = _masks(dim, n_layers, seed)
         self.nets = torch.nn.ModuleList()
         torch.manual_seed(seed)
@@ -139,10 +145,12 @@ class NormalizingFlow(torch.nn.Module):
         fits = (hidden == 64 and n_hidden == 2 and bins in (4, 8, 16)
                 and all(0 < len(ia) <= 16 and 0 < len(ib) <= 16 and _tc_chunks_fit(len(ib), 2 * bins + 1)
                         for ib, ia in self._idx))
-        if fused and not fits:
+        if (fused or tc_bf16) and not fits:
             raise ValueError("the fused sampling kernel needs 64 hidden units, 2 hidden layers, 4/8/16 bins, "
                              "at most 16 dimensions per half and two chunks of at most 256 MLP outputs")
-        self.fused = bool(fits and (tf32 and not bf16) if fused is None else fused)
+        self.fused = bool(fits and ((tf32 or tc_bf16) and not bf16) if fused is None else fused)
+        if self.tc_bf16 and not self.fused:
+            raise ValueError("tc_bf16 samples with the fused kernel")
         nfits = (hidden == 64 and n_hidden == 2 and bins in (4, 8, 16)
                  and all(0 < len(ia) <= 16 and 0 < len(ib) <= 16 and len(ib) * (2 * bins + 1) <= 320
                          for ib, ia in self._idx))
@@ -241,15 +249,16 @@ class NormalizingFlow(torch.nn.Module):
         z = u.T.float().contiguous()
         logq = torch.zeros(n, dtype=torch.float32, device=device())
         if self.fused:
+            fn = "mf_flow_inv_layer_tc_bf16" if self.tc_bf16 else "mf_flow_inv_layer_tc"
             err = torch.zeros(1, dtype=torch.int32, device=device())
             for l, net in enumerate(self.nets):
                 ib, ia = self._idx32[l]
                 w = [t.detach().float().contiguous() for t in (net[0].weight, net[0].bias, net[2].weight,
                                                                net[2].bias, net[4].weight, net[4].bias)]
-                _lib.call("mf_flow_inv_layer_tc", z.data_ptr(), n, self.dim, ia.data_ptr(), len(ia), ib.data_ptr(),
-                          len(ib), self.K, *[t.data_ptr() for t in w], logq.data_ptr(), err.data_ptr(), stream_ptr())
+                _lib.call(fn, z.data_ptr(), n, self.dim, ia.data_ptr(), len(ia), ib.data_ptr(), len(ib), self.K,
+                          *[t.data_ptr() for t in w], logq.data_ptr(), err.data_ptr(), stream_ptr())
             if int(err.item()) != 0:
-                raise RuntimeError(f"mf_flow_inv_layer_tc: device error flag {int(err.item())}")
+                raise RuntimeError(f"{fn}: device error flag {int(err.item())}")
             return z.double(), logq.double()
         if self.native:
             for l in range(len(self.masks)):

@@ -200,6 +200,61 @@ def test_fused_tensor_core_sampling(cuda, dim, bins):
     assert float((lp.double() - lf).abs().max()) < 2e-2
 
 
+@pytest.mark.parametrize("dim,bins", [(18, 16), (18, 8), (7, 4), (32, 8)])
+def test_fused_bf16_sampling(cuda, dim, bins):
+    """mf_flow_inv_layer_tc_bf16 (the three MLP GEMMs on BF16 operands with
+    FP32 accumulation, tcgen05 kind::f16) against a PyTorch restatement that
+    rounds the same operands to BF16 (inputs 2z - 1, weights, hidden
+    activations after bias and ReLU) and multiplies in FP32, followed by the
+    inverse transform kernel: points within 2e-3, log-densities within 2e-2
+    (the two differ only in the FP32 summation order and, rarely, a hidden
+    activation that rounds to the other BF16 neighbour).  And the sampler's
+    log density is its own map's: E_q[1/q] = 1 over the unit hypercube."""
+    import torch
+
+    from madflow_gb300.flow import NormalizingFlow, pq_inverse
+
+    torch.manual_seed(4)
+    f = NormalizingFlow(dim, n_layers=4, bins=bins, hidden=64, n_hidden=2, seed=2, tc_bf16=True)
+    with torch.no_grad():
+        for p in f.parameters():
+            p.copy_(torch.randn_like(p) * (0.5 / max(1, p.shape[-1]) ** 0.5))
+    assert f.fused and f.tc_bf16
+    n = 100_003  # not a multiple of the 128-point tile
+    zf, lf = f.sample(n, seed=13, iteration=1)
+    assert zf.shape == (n, dim) and torch.isfinite(zf).all() and torch.isfinite(lf).all()
+
+    def bf(t):
+        return t.bfloat16().float()
+
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        with torch.no_grad():
+            u = torch.empty((dim, n), dtype=torch.float64, device="cuda")
+            from madflow_gb300 import _lib
+            from madflow_gb300.config import stream_ptr
+
+            _lib.call("mf_philox_uniforms", 13, 7, 1, 0, n, dim, u.data_ptr(), stream_ptr())
+            z = u.T.float().contiguous()
+            lq = torch.zeros(n, dtype=torch.float64, device="cuda")
+            for l, net in enumerate(f.nets):
+                ib, ia = f._idx[l]
+                h1 = torch.relu(bf(2.0 * z[:, ia] - 1.0) @ bf(net[0].weight).T + net[0].bias)
+                h2 = torch.relu(bf(h1) @ bf(net[2].weight).T + net[2].bias)
+                par = (bf(h2) @ bf(net[4].weight).T + net[4].bias).reshape(n, len(ib), 2 * bins + 1)
+                xb, ld = pq_inverse(z[:, ib].contiguous(), par.contiguous(), bins)
+                z[:, ib] = xb
+                lq += ld.double()
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    assert float((zf - z.double()).abs().max()) < 2e-3
+    assert float((lf - lq).abs().max()) < 2e-2
+    w = torch.exp(-lf)
+    v, se = w.mean().item(), (w.std() / n**0.5).item()
+    assert abs(v - 1.0) < 5 * se + 1e-3, (v, se)
+
+
 def test_graphed_training_step_matches_eager(cuda):
     """The training step captured as a CUDA graph (log-density, backward,
     Adam) moves the weights as the eager step does, and leaves them untouched
