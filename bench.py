@@ -103,7 +103,7 @@ CONFIGS["ppj"] = dict(k=3, kind=1, sqrts=13000.0, cuts=dict(ptmin=30.0, etamax=4
                                "pT(j)>30, |eta(j)|<4, 14-dim ramboflow, VEGAS 50 bins/dim",
                       process="gg_ttxg (16 diagrams) + uux_ttxg, ug_ttxu, uxg_ttxux (5 diagrams each, one thread "
                               "per event, in the phase-space stage)")
-KERNELS = {2: "ps_iter_kernel<2,{T}> (phase space and |M|^2 in one pass)", 3: "me_rec_warp_kernel<3,{T}>", 4: "me_rec_kernel<4,{T},{C}>",
+KERNELS = {2: "ps_iter_kernel<2,{T},false> (phase space and |M|^2 in one pass)", 3: "me_rec_warp_kernel<3,{T}>", 4: "me_rec_kernel<4,{T},{C}>",
            5: "me_gws_kernel<5,{T},{C}>"}
 
 

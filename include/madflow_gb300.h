@@ -126,6 +126,15 @@ typedef struct {
   double mt, wt;
   double alpha_s;      /* couplings GC_10 = -g, GC_11 = i g, GC_12 = i g^2, g = 2 sqrt(pi alpha_s) */
   double ptmin, etamax, drmin;
+  /* q2 > 0: fixed factorisation and renormalisation scale Q^2 = q2 (madflow's
+   * --fixed_scale, scripts/madflow_exec.py:432-434), alpha_s fixed.
+   * q2 < 0 (kind 1): madflow's default dynamical scale
+   * (scripts/madflow_exec.py:428-431): per event mu^2 = (sum over the
+   * outgoing particles of m_T / 2)^2, m_T^2 = p.p + p_T^2; the densities at
+   * mu^2; alpha_s(mu^2) from one-loop running with five flavours from
+   * alpha_s = alpha_s(M_Z^2), M_Z = 91.1876 GeV (the synthetic densities
+   * carry no alpha_s of their own), entering |M|^2 per event as madflow's
+   * per-event couplings do.  Otherwise (kind 1): MF_ERR_ARG. */
   double q2;
   int newton_rule;
   /* MF_INITIAL_GG: the g g process alone.  MF_INITIAL_PP (kind 1), as

@@ -929,6 +929,14 @@ static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, Ite
   A.etamax = c->etamax;
   A.drmin = c->drmin;
   A.q2 = c->q2;
+  if (c->q2 < 0.0) {
+    // dynamical scale: hadronic collisions only, alpha_s is alpha_s(M_Z^2)
+    if (c->kind != 1 || !(c->alpha_s > 0.0)) return MF_ERR_ARG;
+    A.dyn = 1;
+    A.alpha0 = c->alpha_s;
+  } else if (c->kind == 1 && !(c->q2 > 0.0)) {
+    return MF_ERR_ARG;  // log Q^2 of the densities
+  }
   A.f32q = 1;
   return pdf_device_table(A.pdf);
 }

@@ -40,6 +40,8 @@ struct IterArgs {
   double ptmin, etamax, drmin;
   PdfTable pdf;
   double q2;
+  int dyn;        // dynamical scale: mu_F = mu_R = sum of the outgoing m_T / 2 per event
+  double alpha0;  // with dyn: alpha_s(M_Z^2), the start of the running
   const int* newton_iters;  // device: iterations of the batch Newton rule (<= 0: per event)
   int f32q;
   const double* x_in;  // optional points (integrand API): no Philox / VEGAS map, jac = 1;
@@ -154,15 +156,16 @@ MF_DO void event_massless(const IterArgs& A, int npart, const P* x, double w0, d
 
 // Rest of the phase space of one event: massive correction with
 // newton_iters iterations (<= 0: per event), incoming momenta, flux, lab
-// boost, cuts and luminosity.  v: the PDF table coordinate of Q^2; pw:
-// (2 pi)^(3 nout - 4).  Returns false when the event fails the cuts.
+// boost, cuts and luminosity.  v: the PDF table coordinate of Q^2 (DYN: set
+// to the event's own); pw: (2 pi)^(3 nout - 4).  Returns false when the
+// event fails the cuts.
 // The event weight (the exponentiated log-weight, flux, luminosity) is FP64
 // for either precision P: exp of an FP32 log-weight of 30 to 50 alone erred
 // by 2e-6; the cuts are decided in P.
-template <class P>
+template <class P, bool DYN = false>
 MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (*p)[4], double logw, double shat,
-                        double wgt, double x1, double x2, double v, double pw, double& wgt_lum,
-                        double x_start = -1.0, double* wgt_ps = nullptr) {
+                        double wgt, double x1, double x2, double& v, double pw, double& wgt_lum,
+                        double x_start = -1.0, double* wgt_ps = nullptr, double* as_ratio = nullptr) {
   MfConsts KC = mf_consts(A.f32q != 0);
   int nout = npart - 2;
   double roots = (A.kind == 0) ? A.sqrts : sqrt(shat);
@@ -187,6 +190,22 @@ MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (
       boost_lab<P>(plab[i], (P)x1, (P)x2);
     }
     ok = pass_gluon_cuts<P>(plab, npart, (P)A.ptmin, (P)A.etamax, (P)A.drmin);
+  }
+  if constexpr (DYN) {
+    // madflow's default scale (scripts/madflow_exec.py:428-431): mu^2 =
+    // (sum over the outgoing particles of m_T / 2)^2, m_T^2 = p.p + p_T^2
+    // (phasespace.py:406-415; invariant under the boost to the lab frame);
+    // the densities at mu^2 and alpha_s(mu^2) / alpha_s(M_Z^2) from one-loop
+    // running with five flavours
+    double smt = 0.0;
+    for (int i = 2; i < npart; ++i) {
+      const double m2 = p[i][0] * p[i][0] - p[i][1] * p[i][1] - p[i][2] * p[i][2] - p[i][3] * p[i][3];
+      const double pt = sqrt(p[i][1] * p[i][1] + p[i][2] * p[i][2]);
+      smt += sqrt(m2 + pt * pt);
+    }
+    const double q2e = (smt / 2.0) * (smt / 2.0);
+    v = pdf_qcoord(A.pdf, q2e);
+    if (as_ratio) *as_ratio = alphas_running_ratio(A.alpha0, q2e);
   }
   const double lum = pdf_xfx_v(A.pdf, x1, v) * pdf_xfx_v(A.pdf, x2, v) / x1 / x2;
   wgt_lum = wgt * lum;
@@ -248,14 +267,14 @@ template <int K, class P> __global__ void __launch_bounds__(256) ps_seed_kernel(
 // Second pass: the rest of the phase space of every event (phase-space
 // precision = the matrix-element precision T), and the per-event record of
 // the matrix element for the events that pass.
-template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(IterArgs A) {
+template <int K, class T, bool DYN> __global__ void __launch_bounds__(128) ps_iter_kernel(IterArgs A) {
   constexpr int NPART = K + 2;
   constexpr int NW = prep_words<T, K>();
   const int64_t N = A.N;
   // the batch rule runs at most 10 iterations (11 = no event converged)
   const int niter = min(*A.newton_iters, 10);
   const MfConsts KC = mf_consts(A.f32q != 0);
-  const double v = pdf_qcoord(A.pdf, A.q2);
+  const double v = DYN ? 0.0 : pdf_qcoord(A.pdf, A.q2);
   const double pw = pow(2.0 * KC.pi, (double)(3 * K - 4));
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
     double p[NPART][4], wl;
@@ -270,9 +289,18 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
     // batch rule: one step from the first pass's x_(niter-1) (the steps
     // before it are the ones the first pass took)
     const double xs = niter > 0 ? st[(int64_t)(4 * K + 6 + niter - 1) * N] : -1.0;
-    double wps = 0.0;
-    bool ok = event_finish<T>(A, NPART, niter > 0 ? 1 : niter, p, logw, shat, wgt, x1, x2, v, pw, wl, xs, &wps);
-    A.pref[e] = ok ? jac * wl : 0.0;
+    double wps = 0.0, ve = v, asr = 1.0;
+    bool ok = event_finish<T, DYN>(A, NPART, niter > 0 ? 1 : niter, p, logw, shat, wgt, x1, x2, ve, pw, wl, xs, &wps,
+                                   &asr);
+    // the event's coupling: every tree diagram of these processes (g g > t t~
+    // + (K-2) g, and the light-quark channels of p p > t t~ (j)) has K strong
+    // vertices, so |M|^2 at alpha_s(mu^2) is |M|^2 at alpha_s(M_Z^2) times
+    // (alpha_s(mu^2) / alpha_s(M_Z^2))^K: the per-event couplings of madflow's
+    // model.evaluate(alpha_s) (scripts/madflow_exec.py:431, 446) as one factor
+    double cs = 1.0;
+    if constexpr (DYN)
+      for (int j = 0; j < K; ++j) cs *= asr;
+    A.pref[e] = ok ? jac * wl * cs : 0.0;
     if constexpr (K == 2) {
       // the light-quark channels of p p > t t~, one thread per event (two
       // orders of magnitude cheaper than the block-per-event gluon channel)
@@ -280,7 +308,7 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
         double ex = 0.0;
         if (ok) {
           const double g11sq = A.gc11.re * A.gc11.re + A.gc11.im * A.gc11.im;
-          ex = jac * wps * pdf_qq_luminosity(A.pdf, x1, x2, v) * uux_ttx_me<T>(p, A.mt, g11sq);
+          ex = jac * wps * pdf_qq_luminosity(A.pdf, x1, x2, ve) * uux_ttx_me<T>(p, A.mt, g11sq) * cs;
         }
         A.extra[e] = ex;
       }
@@ -297,7 +325,7 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
         double lw[6] = {0, 0, 0, 0, 0, 0};
         if (ok) {
           // the densities at x1 and x2 from one interpolation stencil each
-          const PdfStencil s1 = pdf_stencil(A.pdf, x1, v), s2 = pdf_stencil(A.pdf, x2, v);
+          const PdfStencil s1 = pdf_stencil(A.pdf, x1, ve), s2 = pdf_stencil(A.pdf, x2, ve);
           double qq = 0.0, qbq = 0.0, Q1 = 0.0, Qb1 = 0.0, Q2 = 0.0, Qb2 = 0.0;
           for (int f = 1; f <= 4; ++f) {
             const double a = pdf_xfx_st(A.pdf, f, s1), ab = pdf_xfx_st(A.pdf, f + 4, s1);
@@ -310,7 +338,7 @@ template <int K, class T> __global__ void __launch_bounds__(128) ps_iter_kernel(
             Qb2 += bb;
           }
           const double g1 = pdf_xfx_st(A.pdf, 0, s1), g2 = pdf_xfx_st(A.pdf, 0, s2);
-          const double c = jac * wps / x1 / x2;
+          const double c = jac * wps / x1 / x2 * cs;
           // qq3_weighted_sum's order: q q~, q~ q, q g, q~ g, g q, g q~
           lw[0] = c * qq;
           lw[1] = c * qbq;

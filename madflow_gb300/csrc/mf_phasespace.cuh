@@ -296,6 +296,14 @@ MF_HD int pdf_flavour_index(int pdg) {
 }
 // table coordinate of log Q^2 (the same for every event of a batch)
 MF_HD double pdf_qcoord(const PdfTable& T, double q2) { return (log(q2) - T.lq0) / T.dlq; }
+// alpha_s(Q^2) / alpha_s(M_Z^2) at one loop with five flavours,
+// 1 / (1 + alpha_s(M_Z^2) b0 ln(Q^2 / M_Z^2)), b0 = (33 - 2 nf) / (12 pi):
+// the running coupling of the dynamical scale, standing in for the PDF set's
+// alpha_s(Q^2) (pdfflow's alphasQ2), which the synthetic densities lack
+MF_HD double alphas_running_ratio(double alpha_mz, double q2) {
+  const double mz = 91.1876, b0 = 23.0 / (12.0 * 3.141592653589793);
+  return 1.0 / (1.0 + alpha_mz * b0 * log(q2 / (mz * mz)));
+}
 // x f(x, Q^2) of table flavour f (0 = gluon) with v = pdf_qcoord(T, q2),
 // FP64 (the indices are clamped to the table, so any x, NaN included, reads
 // inside it)

@@ -129,8 +129,12 @@ static int sm_count() {
     int64_t cap = (int64_t)sm_count() * MF_PS_BLOCKS_PER_SM;                                                   \
     if (b > cap) b = cap;                                                                                      \
     if (b < 1) b = 1;                                                                                          \
-    if (prec == 0) ps_iter_kernel<KK, double><<<(int)b, 128, 0, st>>>(A);                                      \
-    else ps_iter_kernel<KK, float><<<(int)b, 128, 0, st>>>(A);                                                 \
+    /* the dynamical scale is a separate instantiation: the fixed-scale kernel */ \
+    /* keeps its registers */                                                      \
+    if (prec == 0 && A.dyn) ps_iter_kernel<KK, double, true><<<(int)b, 128, 0, st>>>(A);                      \
+    else if (prec == 0) ps_iter_kernel<KK, double, false><<<(int)b, 128, 0, st>>>(A);                         \
+    else if (A.dyn) ps_iter_kernel<KK, float, true><<<(int)b, 128, 0, st>>>(A);                               \
+    else ps_iter_kernel<KK, float, false><<<(int)b, 128, 0, st>>>(A);                                         \
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;                                                       \
   }                                                                                                            \
   int64_t mf_state_words_k##KK() { return ps_state_words<KK>(); }                                               \

@@ -59,6 +59,9 @@ class FusedIntegrand:
             p p > t t~ at leading order, the g g channel plus the light-quark
             channels q q~ and q~ q (q = d u s c) with the synthetic quark
             densities, summed per event as madflow sums its processes.
+    q2: the fixed scale Q^2 (default mt^2), or "dynamic": madflow's default
+            scale, per event mu = sum of the outgoing m_T / 2, with alpha_s
+            (then alpha_s(M_Z^2)) run to mu at one loop (mf_integrand_config).
     events_limit: run calls in slices of at most this many events (the
             handle's scratch holds one slice; the batch Newton rule runs per
             slice, as madflow's integrand sees one vegasflow slice per call);
@@ -75,7 +78,8 @@ class FusedIntegrand:
         self.initial_states = initial_states
         self.cfg = dict(kind=kind, sqrts=float(sqrts), mt=float(mt), wt=float(wt), alpha_s=float(alpha_s),
                         ptmin=float(ptmin), etamax=float(etamax), drmin=float(drmin),
-                        q2=float(mt * mt if q2 is None else q2), newton_rule=int(newton_rule),
+                        q2=float(mt * mt if q2 is None else (-1.0 if q2 == "dynamic" else q2)),
+                        newton_rule=int(newton_rule),
                         initial_states=_lib.MF_INITIAL_PP if initial_states == "pp" else _lib.MF_INITIAL_GG,
                         events_limit=_limit(events_limit))
         self._cs = _cfg_struct(self.cfg)

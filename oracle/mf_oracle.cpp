@@ -1082,6 +1082,14 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
   cfg.kind = (int)cfgv[0]; cfg.k = (int)cfgv[1]; cfg.sqrts = cfgv[2]; cfg.mt = cfgv[3]; cfg.wt = cfgv[4];
   cfg.alphas = cfgv[5]; cfg.ptmin = cfgv[6]; cfg.etamax = cfgv[7]; cfg.drmin = cfgv[8]; cfg.newton_rule = (int)cfgv[9];
   const int initial_states = (int)cfgv[10];  // 0: g g; 1: p p (g g + q q~ + q~ q, q = d u s c), k = 2 only
+  // 1: madflow's dynamical scale (scripts/madflow_exec.py:428-431): per event
+  // mu^2 = (sum over the outgoing particles of m_T / 2)^2 from the lab-frame
+  // momenta, m_T^2 = p.p + p_T^2 (phasespace.py:406-415), the densities at
+  // mu^2 and alpha_s(mu^2) from alpha_s(M_Z^2) = cfg.alphas at one loop with
+  // five flavours (the stand-in for pdfflow's alphasQ2); every tree diagram
+  // has k strong vertices, so the per-event couplings multiply |M|^2 by
+  // (alpha_s(mu^2) / alpha_s(M_Z^2))^k
+  const bool dyn = cfgv[11] != 0.0;
   double gs = 2.0 * std::sqrt(M_PI * cfg.alphas);
   // MT, WT, GC_10 = -g, GC_11 = i g, GC_12 = i g^2, c3 = -i, c4 = -1
   double prm[12] = {cfg.mt, cfg.wt, -gs, 0.0, 0.0, gs, 0.0, gs * gs, 0.0, -1.0, -1.0, 0.0};
@@ -1109,11 +1117,32 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
   orc_ramboflow(x, N, npart, cfg.sqrts, masses.data(), 1, cfg.newton_rule, p.data(), w.data(), x1.data(), x2.data());
   std::vector<char> pass(N, 1);
   std::vector<double> plab(4 * npart);
+  std::vector<double> q2v((size_t)N, cfg.mt * cfg.mt), csv((size_t)N, 1.0);
   for (int64_t e = 0; e < N; ++e) {
     std::memcpy(plab.data(), &p[(size_t)4 * npart * e], sizeof(double) * 4 * npart);
     boost_to_lab<double>(plab.data(), npart, x1[e], x2[e]);
     pass[e] = (char)orc_pass_cuts(plab.data(), npart, cfg.ptmin, cfg.etamax, cfg.drmin);
+    if (dyn) {
+      double smt = 0.0;
+      for (int i = 2; i < npart; ++i) {
+        const double* q = &plab[4 * i];
+        const double m2 = q[0] * q[0] - q[1] * q[1] - q[2] * q[2] - q[3] * q[3];
+        const double pt = std::sqrt(q[1] * q[1] + q[2] * q[2]);
+        smt += std::sqrt(m2 + pt * pt);
+      }
+      q2v[e] = (smt / 2.0) * (smt / 2.0);
+      const double mz = 91.1876, b0 = 23.0 / (12.0 * M_PI);
+      const double r = 1.0 / (1.0 + cfg.alphas * b0 * std::log(q2v[e] / (mz * mz)));
+      csv[e] = std::pow(r, cfg.k);
+    }
   }
+  // x f(x) at the event's scale
+  auto xf = [&](int pdg, const double* xs, int64_t e) {
+    double o;
+    if (pdg == 21) orc_pdf_xfx(xs + e, 1, q2v[e], &o);
+    else orc_pdf_xfx_flavour(pdg, xs + e, 1, q2v[e], &o);
+    return o;
+  };
   // evaluate the matrix element on the passing events only
   std::vector<int64_t> idx;
   for (int64_t e = 0; e < N; ++e) if (pass[e]) idx.push_back(e);
@@ -1123,13 +1152,20 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
   if (plan && !idx.empty()) orc_ttng_smatrix(plan, pp.data(), (int64_t)idx.size(), prm, 1, mep.data(), nullptr);
   std::vector<double> g1(N), g2(N);
   double q2 = cfg.mt * cfg.mt;
-  orc_pdf_xfx(x1.data(), N, q2, g1.data());
-  orc_pdf_xfx(x2.data(), N, q2, g2.data());
+  if (dyn) {
+    for (int64_t e = 0; e < N; ++e) {
+      g1[e] = xf(21, x1.data(), e);
+      g2[e] = xf(21, x2.data(), e);
+    }
+  } else {
+    orc_pdf_xfx(x1.data(), N, q2, g1.data());
+    orc_pdf_xfx(x2.data(), N, q2, g2.data());
+  }
   for (int64_t e = 0; e < N; ++e) f[e] = 0.0;
   for (size_t i = 0; i < idx.size(); ++i) {
     int64_t e = idx[i];
     double lum = g1[e] * g2[e] / x1[e] / x2[e];
-    f[e] = mep[i] * lum * w[e];
+    f[e] = mep[i] * lum * w[e] * csv[e];
   }
   if (initial_states == 1 && cfg.k == 2 && !idx.empty()) {
     // madflow's integrand: sum over the processes of luminosity x |M|^2, the
@@ -1140,6 +1176,11 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
     orc_smatrix_uux_ttx(pp.data(), (int64_t)idx.size(), prmq, meq.data());
     std::vector<double> lumq((size_t)N, 0.0);
     for (int q = 1; q <= 4; ++q) {
+      if (dyn) {
+        for (int64_t e = 0; e < N; ++e)
+          lumq[e] += xf(q, x1.data(), e) * xf(-q, x2.data(), e) + xf(-q, x1.data(), e) * xf(q, x2.data(), e);
+        continue;
+      }
       orc_pdf_xfx_flavour(q, x1.data(), N, q2, qa.data());
       orc_pdf_xfx_flavour(-q, x2.data(), N, q2, qb.data());
       orc_pdf_xfx_flavour(-q, x1.data(), N, q2, qc.data());
@@ -1148,7 +1189,7 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
     }
     for (size_t i = 0; i < idx.size(); ++i) {
       int64_t e = idx[i];
-      f[e] += meq[i] * (lumq[e] / x1[e] / x2[e]) * w[e];
+      f[e] += meq[i] * (lumq[e] / x1[e] / x2[e]) * w[e] * csv[e];
     }
   }
   if (initial_states == 1 && cfg.k == 3 && !idx.empty()) {
@@ -1168,6 +1209,13 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
     }
     std::vector<double> q1((size_t)N, 0.0), qb1((size_t)N, 0.0), t((size_t)N);
     for (int q = 1; q <= 4; ++q) {
+      if (dyn) {
+        for (int64_t e = 0; e < N; ++e) {
+          q1[e] += xf(q, x1.data(), e);
+          qb1[e] += xf(-q, x1.data(), e);
+        }
+        continue;
+      }
       orc_pdf_xfx_flavour(q, x1.data(), N, q2, t.data());
       for (int64_t e = 0; e < N; ++e) q1[e] += t[e];
       orc_pdf_xfx_flavour(-q, x1.data(), N, q2, t.data());
@@ -1179,10 +1227,10 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
       double s_qq = 0.0, s_qbq = 0.0, q_2 = 0.0, qb_2 = 0.0;
       for (int q = 1; q <= 4; ++q) {
         double a, b, c, d;
-        orc_pdf_xfx_flavour(q, &x1[e], 1, q2, &a);
-        orc_pdf_xfx_flavour(-q, &x2[e], 1, q2, &b);
-        orc_pdf_xfx_flavour(-q, &x1[e], 1, q2, &c);
-        orc_pdf_xfx_flavour(q, &x2[e], 1, q2, &d);
+        orc_pdf_xfx_flavour(q, &x1[e], 1, q2v[e], &a);
+        orc_pdf_xfx_flavour(-q, &x2[e], 1, q2v[e], &b);
+        orc_pdf_xfx_flavour(-q, &x1[e], 1, q2v[e], &c);
+        orc_pdf_xfx_flavour(q, &x2[e], 1, q2v[e], &d);
         s_qq += a * b;
         s_qbq += c * d;
         q_2 += d;
@@ -1196,7 +1244,7 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
       lq[5] = g1[e] * qb_2;       // g(x1) q~(x2)
       double sum = 0.0;
       for (int c = 0; c < 6; ++c) sum += me[c][i] * lq[c];
-      f[e] += sum / x1[e] / x2[e] * w[e];
+      f[e] += sum / x1[e] / x2[e] * w[e] * csv[e];
     }
   }
 }
