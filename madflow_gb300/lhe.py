@@ -84,16 +84,18 @@ class LheWriter:
 
     def write_events(self, momenta, weights, pids, scale, aqcd, aqed=-1.0):
         """momenta (M, n, 4) as (E, px, py, pz); weights (M,); pids (n,),
-        the first two incoming."""
+        the first two incoming; scale and aqcd one value or one per event."""
         p = np.asarray(momenta, dtype=np.float64)
         w = np.asarray(weights, dtype=np.float64)
         m, n, _ = p.shape
+        scales = np.broadcast_to(np.asarray(scale, dtype=np.float64), (m,))
+        aqcds = np.broadcast_to(np.asarray(aqcd, dtype=np.float64), (m,))
         m2 = p[..., 0] ** 2 - (p[..., 1] ** 2 + p[..., 2] ** 2 + p[..., 3] ** 2)
         mass = np.sqrt(np.maximum(m2, 0.0))
         lines = []
         for e in range(m):
             lines.append("<event>\n")
-            lines.append(f" {n} {self.process_id} {w[e]:+.10e} {scale:.10e} {aqed:.10e} {aqcd:.10e}\n")
+            lines.append(f" {n} {self.process_id} {w[e]:+.10e} {scales[e]:.10e} {aqed:.10e} {aqcds[e]:.10e}\n")
             for i in range(n):
                 st, m1, m2_ = (-1, 0, 0) if i < 2 else (1, 1, 2)
                 pe = p[e, i]
@@ -115,6 +117,19 @@ class LheWriter:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def dynamic_scale(momenta, alpha_mz, mz=91.1876):
+    """(mu, alpha_s(mu^2)) per event of the dynamical scale for momenta
+    (M, n, 4): mu = sum over the outgoing particles of m_T / 2, m_T^2 = p.p +
+    p_T^2 (scripts/madflow_exec.py:428-431), alpha_s at one loop with five
+    flavours from alpha_s(M_Z^2) = alpha_mz."""
+    q = np.asarray(momenta, dtype=np.float64)[:, 2:, :]
+    m2 = q[..., 0] ** 2 - q[..., 1] ** 2 - q[..., 2] ** 2 - q[..., 3] ** 2
+    pt = np.sqrt(q[..., 1] ** 2 + q[..., 2] ** 2)
+    mu = np.sqrt(m2 + pt**2).sum(-1) / 2.0
+    b0 = 23.0 / (12.0 * math.pi)
+    return mu, alpha_mz / (1.0 + alpha_mz * b0 * np.log(mu * mu / (mz * mz)))
 
 
 def generate_events(integrand, vegas, n_events, path, batch=1_000_000, trunc=1e-3, seed=11, max_batches=1000):
@@ -159,9 +174,14 @@ def generate_events(integrand, vegas, n_events, path, batch=1_000_000, trunc=1e-
     cfg = integrand.cfg
     pids = [21, 21, 6, -6] + [21] * (npart - 4)
     half = cfg["sqrts"] / 2.0
-    aqcd = cfg["alpha_s"]
+    if cfg["q2"] < 0:
+        # the dynamical scale of the integrand: mu = sum of the outgoing m_T / 2,
+        # alpha_s(mu^2) at one loop from alpha_s(M_Z^2) (mf_integrand_config)
+        scale, aqcd = dynamic_scale(p, cfg["alpha_s"])
+    else:
+        scale, aqcd = math.sqrt(cfg["q2"]), cfg["alpha_s"]
     with LheWriter(path, ebeam=(half, half), comment=f"madflow_gb300 {integrand.matrix}") as lhe:
         lhe.write_init(xsec, xerr, float(weights.max()) if n_keep else 0.0)
-        lhe.write_events(p, weights, pids, math.sqrt(cfg["q2"]), aqcd)
+        lhe.write_events(p, weights, pids, scale, aqcd)
     return {"xsec_pb": xsec, "xerr_pb": xerr, "kept": n_keep, "generated": n_gen,
             "efficiency": n_keep / n_gen if n_gen else 0.0, "w_max": w_max, "batches": nb_batches}

@@ -46,6 +46,29 @@ def test_lhe_writer_roundtrip(tmp_path):
         np.testing.assert_allclose(parts[:, 9], p[e, :, 0], rtol=1e-9)
 
 
+def test_lhe_dynamic_scale_per_event(tmp_path):
+    """Events of a dynamic-scale run carry their own scale and alpha_s:
+    mu = sum of the outgoing m_T / 2 and alpha_s(mu^2) at one loop from
+    alpha_s(M_Z^2) (scripts/madflow_exec.py:428-431)."""
+    rng = np.random.default_rng(3)
+    p = np.zeros((4, 4, 4))
+    p[:, 2:, 1:] = rng.normal(scale=100.0, size=(4, 2, 3))
+    p[:, 2:, 0] = np.sqrt(173.0**2 + (p[:, 2:, 1:] ** 2).sum(-1))
+    mu, a = lhe.dynamic_scale(p, 0.118)
+    mt = np.sqrt(173.0**2 + p[:, 2:, 1] ** 2 + p[:, 2:, 2] ** 2)
+    np.testing.assert_allclose(mu, mt.sum(-1) / 2.0, rtol=1e-14)
+    b0 = 23.0 / (12.0 * math.pi)
+    np.testing.assert_allclose(a, 0.118 / (1.0 + 0.118 * b0 * np.log(mu**2 / 91.1876**2)), rtol=1e-14)
+    assert np.all(a < 0.118)  # mu >= mt > M_Z
+    path = tmp_path / "dyn.lhe"
+    with lhe.LheWriter(path, ebeam=(6500.0, 6500.0)) as wr:
+        wr.write_init(1.0, 0.1, 1.0)
+        wr.write_events(p, np.ones(4), [21, 21, 6, -6], mu, a)
+    heads = [line.split() for line in open(path).read().split("<event>\n")[1:]]
+    np.testing.assert_allclose([float(h[3]) for h in heads], mu, rtol=1e-9)
+    np.testing.assert_allclose([float(h[5]) for h in heads], a, rtol=1e-9)
+
+
 def test_truncated_wmax():
     w = torch.tensor(np.random.default_rng(2).pareto(1.5, size=5000))
     assert lhe.truncated_wmax(w, 0.0) == float(w.max())
@@ -108,4 +131,30 @@ def test_event_generation_ggttx(cuda, tmp_path):
     init, events = _parse(tmp_path / "gg_ttx.lhe.gz")
     assert len(events) == 2000
     assert sum(e[0] for e in events) == pytest.approx(stats["xsec_pb"], rel=1e-6)
+    assert abs(stats["xsec_pb"] - v.history[-1][0]) < 5 * math.hypot(stats["xerr_pb"], v.history[-1][1])
+
+
+@pytest.mark.gpu
+def test_event_generation_dynamic_scale(cuda, tmp_path):
+    """Hadronic g g > t t~ at madflow's dynamical scale: the unweighted
+    events carry their own mu (sum of the outgoing m_T / 2 of the written
+    momenta) and alpha_s(mu^2), and the file's cross section agrees with the
+    VEGAS integral of the same integrand."""
+    from madflow_gb300.vegas import FusedIntegrand, VegasFlow
+
+    integ = FusedIntegrand(2, kind=1, sqrts=13000.0, q2="dynamic", precision=0)
+    v = VegasFlow(integ.n_dim, 100_000, use_graph=False)
+    v.compile(integ)
+    v.run_integration(4)
+    path = tmp_path / "gg_ttx_dyn.lhe"
+    stats = lhe.generate_events(integ, v, 500, path, batch=100_000, trunc=1e-3)
+    assert stats["kept"] == 500
+    text = open(path).read()
+    heads = [blk.split("\n")[0].split() for blk in text.split("<event>\n")[1:]]
+    _, events = _parse(path)
+    p = np.stack([parts[:, [9, 6, 7, 8]] for _, parts in events])  # (E, px, py, pz)
+    mu, a = lhe.dynamic_scale(p, 0.118)
+    np.testing.assert_allclose([float(h[3]) for h in heads], mu, rtol=1e-8)
+    np.testing.assert_allclose([float(h[5]) for h in heads], a, rtol=1e-8)
+    assert np.all(mu >= 173.0 * (1 - 1e-9)) and np.all(a < 0.118)
     assert abs(stats["xsec_pb"] - v.history[-1][0]) < 5 * math.hypot(stats["xerr_pb"], v.history[-1][1])
