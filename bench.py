@@ -334,6 +334,8 @@ def run_gpu(args):
     f_host = torch.empty(e2e_n, dtype=torch.float64).pin_memory()
     integ(x_host, out=f_host)  # warm-up
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     reps = max(1, args.e2e_reps)
@@ -341,7 +343,13 @@ def run_gpu(args):
         integ(x_host, out=f_host)
     e1.record()
     torch.cuda.synchronize()
-    e2e_rate = int((f_host != 0).sum()) * reps / (e0.elapsed_time(e1) / 1000.0)
+    # whole job: the passing events of all ranks over the slowest rank's time
+    e2e_t = torch.tensor([e0.elapsed_time(e1) / 1000.0], dtype=torch.float64, device="cuda")
+    e2e_pass = torch.tensor([int((f_host != 0).sum()) * reps], dtype=torch.int64, device="cuda")
+    if dist:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(e2e_pass)
+    e2e_rate = int(e2e_pass.item()) / float(e2e_t.item())
 
     T = "float" if prec_name == "mixed" else "double"
     kern = KERNELS[k].format(T=T, C=tune["colour"] if prec_name == "mixed" else 0)
@@ -374,11 +382,11 @@ def run_gpu(args):
         "stage_ms": stages,
         "nonfinite_weights": r["nonfinite"],
         "autotune": dict(tune, variants="index colour*4 + log2(waves); colour 0 SIMT, 1 tensor cores (tcgen05 TF32)"),
-        "e2e": {"value": e2e_rate, "unit": "|M|^2 evals/s", "h2d_bytes_per_step": int(x_host.numel() * 8),
-                "d2h_bytes_per_step": int(f_host.numel() * 8),
+        "e2e": {"value": e2e_rate, "unit": "|M|^2 evals/s", "h2d_bytes_per_step": int(x_host.numel() * 8) * world,
+                "d2h_bytes_per_step": int(f_host.numel() * 8) * world,
                 "api": "FusedIntegrand(x_host, out=f_host): x (N, ndim) float64 and f in page-locked host memory, "
                        "read and written by the kernels over the host link (mf_integrand_rows, zero-copy)",
-                "events_per_step": e2e_n},
+                "events_per_step": e2e_n * world},
         "roofline": {"bound": pipe, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "traffic_unit": "bytes per launch (ncu, 10^6-point capture scaled by the events per launch)",
