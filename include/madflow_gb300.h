@@ -391,8 +391,8 @@ int mf_flow_grad(const float* x, const float* params, const float* gy, const flo
  * tensor cores (tcgen05, TF32 operands, FP32 accumulation): the conditioner
  * MLP na -> 64 -> 64 -> nb (2K+1) with ReLU, then the inverse transform of
  * the nb transformed dimensions.  z [N][dim] float32 points, updated in place
- * on the dimensions ib [nb] (int32); the MLP reads the dimensions ia [na] as
- * 2 z - 1.  W1 [64][na], b1 [64], W2 [64][64], b2 [64], W3 [nb (2K+1)][64],
+ * on the dimensions ib [nb] (device int32, clamped to [0, dim)); the MLP
+ * reads the dimensions ia [na] (likewise) as 2 z - 1.  W1 [64][na], b1 [64], W2 [64][64], b2 [64], W3 [nb (2K+1)][64],
  * b3 [nb (2K+1)] in torch.nn.Linear layout (out x in); logq [N] += the sum of
  * log pdf.  1 <= na, nb <= 16, na + nb <= dim, K in {4, 8, 16},
  * nb (2K+1) <= 256.  err: device int set to 1 if a bounded tensor-core wait

@@ -238,8 +238,9 @@ __global__ void __launch_bounds__(FTILE) flow_inv_layer_tc_kernel(float* __restr
   }
   for (int i = tid; i < n3ap + n3bp; i += FTILE) S.bias[2 * FH + i] = i < n3 ? b3[i] : 0.f;
   if (tid < 16) {
-    S.idx[tid] = tid < na ? ia[tid] : 0;
-    S.idx[16 + tid] = tid < nb ? ib[tid] : 0;
+    // caller indices, clamped to the point's dim columns
+    S.idx[tid] = tid < na ? min(max(ia[tid], 0), dim - 1) : 0;
+    S.idx[16 + tid] = tid < nb ? min(max(ib[tid], 0), dim - 1) : 0;
   }
   if (warp == 0) tc_tmem_alloc(S.tmem, FTMEM);
   if (tid == 0) {
