@@ -162,6 +162,12 @@ typedef struct {
    * depend on the slicing.  0: one slice.  < 0: MF_ERR_ARG.  Stage timing
    * (mf_process_set_timing) records one-slice calls only. */
   int64_t events_limit;
+  /* > 0 (kind 1): madflow's --pt_cut (scripts/madflow_exec.py:396-401,
+   * phasespace.py:417-422, 458-466): p_T > ptmin_all, held through float32
+   * as madflow's float_me holds it, for every outgoing particle, the tops
+   * included; events failing it give 0.  It adds to the gluon cuts above.
+   * <= 0: off.  With kind 0: MF_ERR_ARG. */
+  double ptmin_all;
 } mf_integrand_config;
 
 /* Number of integration dimensions of a configuration (8 for kind 0,

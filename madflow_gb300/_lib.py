@@ -56,6 +56,7 @@ class IntegrandConfig(ctypes.Structure):
         ("newton_rule", c_int),
         ("initial_states", c_int),
         ("events_limit", c_int64),
+        ("ptmin_all", c_double),
     ]
 
 

@@ -928,6 +928,8 @@ static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, Ite
   A.ptmin = c->ptmin;
   A.etamax = c->etamax;
   A.drmin = c->drmin;
+  if (c->ptmin_all > 0.0 && c->kind != 1) return MF_ERR_ARG;
+  A.ptmin_all = c->ptmin_all > 0.0 ? (double)(float)c->ptmin_all : 0.0;
   A.q2 = c->q2;
   if (c->q2 < 0.0) {
     // dynamical scale: hadronic collisions only, alpha_s is alpha_s(M_Z^2)

@@ -38,6 +38,7 @@ struct IterArgs {
   double masses[MF_MAX_OUT];
   double shat_min;
   double ptmin, etamax, drmin;
+  double ptmin_all;  // > 0: p_T > ptmin_all for every outgoing particle (madflow's --pt_cut)
   PdfTable pdf;
   double q2;
   int dyn;        // dynamical scale: mu_F = mu_R = sum of the outgoing m_T / 2 per event
@@ -183,7 +184,13 @@ MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (
   wgt = wgt / (2.0 * shat);
   if (wgt_ps) *wgt_ps = wgt;  // the weight before the luminosity
   bool ok = true;
-  if (A.ptmin > 0.0 || A.etamax > 0.0 || A.drmin > 0.0) {
+  if (A.ptmin_all > 0.0) {
+    // madflow's --pt_cut on every outgoing particle, decided in FP64 on the
+    // partonic-frame momenta, as PhaseSpaceGenerator cuts before its boost
+    // (p_x, p_y are the lab frame's)
+    for (int i = 2; i < npart; ++i) ok = ok && sqrt(p[i][1] * p[i][1] + p[i][2] * p[i][2]) > A.ptmin_all;
+  }
+  if (ok && (A.ptmin > 0.0 || A.etamax > 0.0 || A.drmin > 0.0)) {
     P plab[MF_MAX_OUT + 2][4];
     for (int i = 0; i < npart; ++i) {
       for (int c = 0; c < 4; ++c) plab[i][c] = (P)p[i][c];

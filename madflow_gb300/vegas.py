@@ -62,6 +62,9 @@ class FusedIntegrand:
     q2: the fixed scale Q^2 (default mt^2), or "dynamic": madflow's default
             scale, per event mu = sum of the outgoing m_T / 2, with alpha_s
             (then alpha_s(M_Z^2)) run to mu at one loop (mf_integrand_config).
+    pt_cut: madflow's --pt_cut, p_T > pt_cut for every outgoing particle
+            (tops included; kind 1), beside the gluon cuts ptmin, etamax,
+            drmin.
     events_limit: run calls in slices of at most this many events (the
             handle's scratch holds one slice; the batch Newton rule runs per
             slice, as madflow's integrand sees one vegasflow slice per call);
@@ -71,7 +74,7 @@ class FusedIntegrand:
 
     def __init__(self, n_gluons, kind=1, sqrts=13000.0, mt=173.0, wt=1.4915000200271606, alpha_s=0.118, ptmin=0.0,
                  etamax=0.0, drmin=0.0, q2=None, newton_rule=_lib.MF_NEWTON_BATCH, precision=None,
-                 initial_states="gg", events_limit=None):
+                 initial_states="gg", events_limit=None, pt_cut=None):
         if initial_states not in ("gg", "pp"):
             raise ValueError(f"initial_states must be 'gg' or 'pp', not {initial_states!r}")
         self.matrix = PROCESSES[n_gluons](precision=precision)
@@ -81,7 +84,7 @@ class FusedIntegrand:
                         q2=float(mt * mt if q2 is None else (-1.0 if q2 == "dynamic" else q2)),
                         newton_rule=int(newton_rule),
                         initial_states=_lib.MF_INITIAL_PP if initial_states == "pp" else _lib.MF_INITIAL_GG,
-                        events_limit=_limit(events_limit))
+                        events_limit=_limit(events_limit), ptmin_all=float(pt_cut or 0.0))
         self._cs = _cfg_struct(self.cfg)
         nd = ctypes.c_int()
         _lib.call("mf_integrand_ndim", self.matrix.handle, ctypes.byref(self._cs), ctypes.byref(nd))

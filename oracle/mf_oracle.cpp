@@ -1090,6 +1090,10 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
   // has k strong vertices, so the per-event couplings multiply |M|^2 by
   // (alpha_s(mu^2) / alpha_s(M_Z^2))^k
   const bool dyn = cfgv[11] != 0.0;
+  // > 0: madflow's --pt_cut (scripts/madflow_exec.py:396-401): p_T >
+  // float32(cut) for every outgoing particle, on the momenta before the boost
+  // to the lab frame (phasespace.py:417-422, 458-466)
+  const double pt_all = cfgv[12] > 0.0 ? (double)(float)cfgv[12] : 0.0;
   double gs = 2.0 * std::sqrt(M_PI * cfg.alphas);
   // MT, WT, GC_10 = -g, GC_11 = i g, GC_12 = i g^2, c3 = -i, c4 = -1
   double prm[12] = {cfg.mt, cfg.wt, -gs, 0.0, 0.0, gs, 0.0, gs * gs, 0.0, -1.0, -1.0, 0.0};
@@ -1122,6 +1126,11 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
     std::memcpy(plab.data(), &p[(size_t)4 * npart * e], sizeof(double) * 4 * npart);
     boost_to_lab<double>(plab.data(), npart, x1[e], x2[e]);
     pass[e] = (char)orc_pass_cuts(plab.data(), npart, cfg.ptmin, cfg.etamax, cfg.drmin);
+    if (pt_all > 0.0)
+      for (int i = 2; i < npart; ++i) {
+        const double* q = &p[(size_t)4 * npart * e + 4 * i];
+        if (!(std::sqrt(q[1] * q[1] + q[2] * q[2]) > pt_all)) pass[e] = 0;
+      }
     if (dyn) {
       double smt = 0.0;
       for (int i = 2; i < npart; ++i) {

@@ -372,11 +372,12 @@ def pass_cuts(plab, ptmin, etamax, drmin):
 def integrand(cfg, x, plan=None, fast=False):
     """cfg: [kind, k, sqrts, mt, wt, alphas, ptmin, etamax, drmin, newton_rule
     (, initial_states: 0 g g, 1 p p (, dynamic scale: 0 fixed Q = mt, 1
-    madflow's sum of m_T / 2 with alphas = alpha_s(M_Z^2)))].  fast: the
-    timing build (plan, if given, must come from the same build)."""
+    madflow's sum of m_T / 2 with alphas = alpha_s(M_Z^2) (, pt_all: > 0
+    madflow's --pt_cut on every outgoing particle)))].  fast: the timing
+    build (plan, if given, must come from the same build)."""
     if plan is not None:
         fast = plan.fast
-    cfg = list(cfg) + [0] * (12 - len(cfg))
+    cfg = list(cfg) + [0] * (13 - len(cfg))
     x = _c64(x)
     f = np.empty(x.shape[0])
     lib(fast).orc_integrand(_p(_c64(cfg)), ctypes.c_void_p(plan.h if plan is not None else None), _p(x),
