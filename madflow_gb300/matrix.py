@@ -124,6 +124,13 @@ class MatrixTTNG:
         """|M|^2 averaged over initial and summed over final helicities and colours."""
         return self._run(all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12, False)[0]
 
+    def cusmatrix(self, *args):
+        """madflow's custom-operator variant of smatrix (the method its
+        custom_op/generation.py:259-283 adds to the module, called by
+        scripts/madflow_exec.py:404, 446 with --custom_op): here the same
+        CUDA evaluation as smatrix."""
+        return self.smatrix(*args)
+
     def smatrix_per_helicity(self, all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12=None):
         """(smatrix, per-helicity matrix values (ncomb, N))."""
         return self._run(all_ps, mdl_MT, mdl_WT, GC_10, GC_11, GC_12, True)
@@ -193,6 +200,10 @@ class Matrix_1_uux_ttx:
     def __str__(self):
         return self.process_string
 
+    def cusmatrix(self, *args):
+        """madflow's custom-operator variant of smatrix: the same evaluation."""
+        return self.smatrix(*args)
+
     def smatrix(self, all_ps, mdl_MT, mdl_WT, GC_11):
         """|M|^2 averaged over the initial spins (4) and colours (9)."""
         ps = to_device(all_ps)
@@ -227,6 +238,10 @@ class _MatrixQQ3:
 
     def __str__(self):
         return self.process_string
+
+    def cusmatrix(self, *args):
+        """madflow's custom-operator variant of smatrix: the same evaluation."""
+        return self.smatrix(*args)
 
     def smatrix(self, all_ps, mdl_MT, mdl_WT, GC_10, GC_11):
         """|M|^2 averaged over the initial spins and colours."""

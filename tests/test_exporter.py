@@ -145,3 +145,5 @@ def test_exported_smatrix_equals_library(cuda, tmp_path):
             want = lib.smatrix(ps, *params).cpu().numpy()
             assert np.all(np.isfinite(got)) and np.all(got > 0), str(mat)
             np.testing.assert_array_equal(got, want)
+            # madflow's --custom_op path calls cusmatrix with the same arguments
+            np.testing.assert_array_equal(mat.cusmatrix(ps, *params).cpu().numpy(), got)
