@@ -120,6 +120,21 @@ int mf_VVV1P0_1(const double* V2, const double* V3, const double* coup, double M
  *           cuts on the outgoing gluons (pT > ptmin, |eta| < etamax,
  *           Delta R > drmin in the lab frame; <= 0 disables). */
 typedef enum { MF_INITIAL_GG = 0, MF_INITIAL_PP = 1 } mf_initial_states;
+/* One cut of madflow's PhaseSpaceGenerator.register_cut(variable, particle,
+ * min_val, max_val) (phasespace.py:405-478): the variable of one particle
+ * (MadGraph order, 0 .. nexternal-1) on the momenta before the boost to the
+ * lab frame, kept when min_val < value (has_min) and value < max_val
+ * (has_max), the thresholds held through float32 as madflow's float_me holds
+ * them.  pt = sqrt(px^2 + py^2), mt2 = p.p + pt^2, mt = sqrt(mt2) (madflow's
+ * three), eta = artanh(pz / |p|) (an addition). */
+#define MF_MAX_CUTS 8
+typedef enum { MF_CUT_PT = 0, MF_CUT_MT = 1, MF_CUT_MT2 = 2, MF_CUT_ETA = 3 } mf_cut_variable;
+typedef struct {
+  int variable;
+  int particle;
+  int has_min, has_max;
+  double min_val, max_val;
+} mf_cut;
 typedef struct {
   int kind;
   double sqrts;
@@ -168,6 +183,11 @@ typedef struct {
    * included; events failing it give 0.  It adds to the gluon cuts above.
    * <= 0: off.  With kind 0: MF_ERR_ARG. */
   double ptmin_all;
+  /* cuts[0 .. ncuts-1] (kind 1), all of them applied beside the cuts above;
+   * 0 <= ncuts <= MF_MAX_CUTS, a variable or particle out of range, or cuts
+   * with kind 0: MF_ERR_ARG. */
+  int ncuts;
+  mf_cut cuts[MF_MAX_CUTS];
 } mf_integrand_config;
 
 /* Number of integration dimensions of a configuration (8 for kind 0,

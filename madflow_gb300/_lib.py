@@ -42,6 +42,15 @@ class DeviceError(RuntimeError):
     (a bounded wait on the tensor cores ran out; the affected events got NaN)."""
 
 
+MF_MAX_CUTS = 8
+CUT_VARIABLES = {"pt": 0, "mt": 1, "mt2": 2, "eta": 3}
+
+
+class Cut(ctypes.Structure):
+    _fields_ = [("variable", c_int), ("particle", c_int), ("has_min", c_int), ("has_max", c_int),
+                ("min_val", c_double), ("max_val", c_double)]
+
+
 class IntegrandConfig(ctypes.Structure):
     _fields_ = [
         ("kind", c_int),
@@ -57,6 +66,8 @@ class IntegrandConfig(ctypes.Structure):
         ("initial_states", c_int),
         ("events_limit", c_int64),
         ("ptmin_all", c_double),
+        ("ncuts", c_int),
+        ("cuts", Cut * MF_MAX_CUTS),
     ]
 
 

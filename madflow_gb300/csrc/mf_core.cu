@@ -930,6 +930,18 @@ static int fill_iter_args(const mf_process* p, const mf_integrand_config* c, Ite
   A.drmin = c->drmin;
   if (c->ptmin_all > 0.0 && c->kind != 1) return MF_ERR_ARG;
   A.ptmin_all = c->ptmin_all > 0.0 ? (double)(float)c->ptmin_all : 0.0;
+  if (c->ncuts < 0 || c->ncuts > MF_MAX_CUTS || (c->ncuts > 0 && c->kind != 1)) return MF_ERR_ARG;
+  A.ncuts = c->ncuts;
+  for (int i = 0; i < c->ncuts; ++i) {
+    mf_cut C = c->cuts[i];
+    if (C.variable < MF_CUT_PT || C.variable > MF_CUT_ETA || C.particle < 0 || C.particle >= p->k + 2) return MF_ERR_ARG;
+    C.has_min = C.has_min != 0;
+    C.has_max = C.has_max != 0;
+    // float_me(min_val), float_me(max_val): the reference's float32 thresholds
+    C.min_val = C.has_min ? (double)(float)C.min_val : 0.0;
+    C.max_val = C.has_max ? (double)(float)C.max_val : 0.0;
+    A.cuts[i] = C;
+  }
   A.q2 = c->q2;
   if (c->q2 < 0.0) {
     // dynamical scale: hadronic collisions only, alpha_s is alpha_s(M_Z^2)

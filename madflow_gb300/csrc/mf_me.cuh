@@ -19,6 +19,7 @@
 //
 // so that an iteration is bit-reproducible.
 #pragma once
+#include "../../include/madflow_gb300.h"
 #include "mf_me_rec.cuh"
 #include "mf_qq.cuh"
 #include "mf_qq3.cuh"
@@ -39,6 +40,8 @@ struct IterArgs {
   double shat_min;
   double ptmin, etamax, drmin;
   double ptmin_all;  // > 0: p_T > ptmin_all for every outgoing particle (madflow's --pt_cut)
+  int ncuts;         // registered cuts (mf_cut), thresholds already held through float32
+  mf_cut cuts[MF_MAX_CUTS];
   PdfTable pdf;
   double q2;
   int dyn;        // dynamical scale: mu_F = mu_R = sum of the outgoing m_T / 2 per event
@@ -219,6 +222,38 @@ MF_DO bool event_finish(const IterArgs& A, int npart, int newton_iters, double (
   return ok;
 }
 
+// The registered cuts (mf_cut), in FP64 on the partonic-frame momenta
+// p [NPART][4] (madflow's PhaseSpaceGenerator cuts before its boost,
+// phasespace.py:458-466), in the reference's operation order (_fourdot; mt2 =
+// p.p + pt^2 with pt a square root).  Compile-time indices throughout, so
+// the cut table and the momenta stay out of local memory.
+template <int NPART> MF_DO bool pass_cut_table(const IterArgs& A, const double (*p)[4]) {
+#pragma unroll
+  for (int c = 0; c < MF_MAX_CUTS; ++c) {
+    if (c >= A.ncuts) break;
+    const mf_cut C = A.cuts[c];
+    double q[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int i = 0; i < NPART; ++i)
+      if (i == C.particle) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) q[j] = p[i][j];
+      }
+    const double pt = sqrt(q[1] * q[1] + q[2] * q[2]);
+    double val = pt;
+    if (C.variable == MF_CUT_MT || C.variable == MF_CUT_MT2) {
+      const double mt2 = (q[0] * q[0] - ((q[1] * q[1] + q[2] * q[2]) + q[3] * q[3])) + pt * pt;
+      val = C.variable == MF_CUT_MT ? sqrt(mt2) : mt2;
+    } else if (C.variable == MF_CUT_ETA) {
+      const double pabs = sqrt((q[1] * q[1] + q[2] * q[2]) + q[3] * q[3]);
+      val = 0.5 * log((pabs + q[3]) / (pabs - q[3]));
+    }
+    if (C.has_min && !(val > C.min_val)) return false;
+    if (C.has_max && !(val < C.max_val)) return false;
+  }
+  return true;
+}
+
 // First pass: the phase-space state of every event and, when batch_rule is
 // set, the batch minimum of the Newton convergence iteration (atomicMin into
 // *kmin, which starts at 11).  An event only needs to be followed up to the
@@ -299,6 +334,7 @@ template <int K, class T, bool DYN> __global__ void __launch_bounds__(128) ps_it
     double wps = 0.0, ve = v, asr = 1.0;
     bool ok = event_finish<T, DYN>(A, NPART, niter > 0 ? 1 : niter, p, logw, shat, wgt, x1, x2, ve, pw, wl, xs, &wps,
                                    &asr);
+    ok = ok && pass_cut_table<NPART>(A, p);
     // the event's coupling: every tree diagram of these processes (g g > t t~
     // + (K-2) g, and the light-quark channels of p p > t t~ (j)) has K strong
     // vertices, so |M|^2 at alpha_s(mu^2) is |M|^2 at alpha_s(M_Z^2) times

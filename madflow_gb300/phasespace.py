@@ -113,11 +113,18 @@ class PhaseSpaceGenerator:
         self._nparticles = nparticles
         self._cuts = []
         self._cuts_info = []
+        self._cut_specs = []
         self._com_output = com_output
 
     def clear_cuts(self):
         self._cuts = []
         self._cuts_info = []
+        self._cut_specs = []
+
+    def cut_table(self):
+        """The registered cuts as (variable, particle, min_val, max_val), the
+        form FusedIntegrand(cuts=...) takes."""
+        return list(self._cut_specs)
 
     @staticmethod
     def mt2(ps_point):
@@ -159,6 +166,7 @@ class PhaseSpaceGenerator:
 
         self._cuts.append(cut_function)
         self._cuts_info.append(f"{min_val} < {variable}({particle}) < {max_val}")
+        self._cut_specs.append((variable, particle, min_val, max_val))
 
     def __call__(self, xrand):
         ps, wgt, x1, x2 = ramboflow(xrand, self._nparticles, self._sqrts, self._masses)

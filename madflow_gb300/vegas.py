@@ -40,10 +40,36 @@ def _limit(events_limit):
     return int(events_limit)
 
 
+def _cut_table(cuts):
+    """(variable, particle, min_val, max_val) tuples, as
+    PhaseSpaceGenerator.register_cut takes them (None: no bound)."""
+    cuts = list(cuts or [])
+    if len(cuts) > _lib.MF_MAX_CUTS:
+        raise ValueError(f"at most {_lib.MF_MAX_CUTS} cuts")
+    out = []
+    for variable, particle, lo, hi in cuts:
+        if variable not in _lib.CUT_VARIABLES:
+            raise ValueError(f"{variable} is not implemented")
+        if particle is None:
+            raise ValueError("a cut of the fused integrand names its particle")
+        out.append((variable, int(particle), lo, hi))
+    return out
+
+
 def _cfg_struct(cfg):
     s = _lib.IntegrandConfig()
     for k, _ in _lib.IntegrandConfig._fields_:
-        setattr(s, k, cfg[k])
+        if k == "ncuts":
+            s.ncuts = len(cfg["cuts"])
+        elif k == "cuts":
+            for i, (variable, particle, lo, hi) in enumerate(cfg["cuts"]):
+                c = s.cuts[i]
+                c.variable, c.particle = _lib.CUT_VARIABLES[variable], particle
+                c.has_min, c.has_max = int(lo is not None), int(hi is not None)
+                c.min_val = 0.0 if lo is None else float(lo)
+                c.max_val = 0.0 if hi is None else float(hi)
+        else:
+            setattr(s, k, cfg[k])
     return s
 
 
@@ -65,6 +91,9 @@ class FusedIntegrand:
     pt_cut: madflow's --pt_cut, p_T > pt_cut for every outgoing particle
             (tops included; kind 1), beside the gluon cuts ptmin, etamax,
             drmin.
+    cuts:   up to 8 (variable, particle, min_val, max_val) as
+            PhaseSpaceGenerator.register_cut takes them (pt, mt, mt2, eta;
+            None for no bound), e.g. PhaseSpaceGenerator.cut_table(); kind 1.
     events_limit: run calls in slices of at most this many events (the
             handle's scratch holds one slice; the batch Newton rule runs per
             slice, as madflow's integrand sees one vegasflow slice per call);
@@ -74,7 +103,7 @@ class FusedIntegrand:
 
     def __init__(self, n_gluons, kind=1, sqrts=13000.0, mt=173.0, wt=1.4915000200271606, alpha_s=0.118, ptmin=0.0,
                  etamax=0.0, drmin=0.0, q2=None, newton_rule=_lib.MF_NEWTON_BATCH, precision=None,
-                 initial_states="gg", events_limit=None, pt_cut=None):
+                 initial_states="gg", events_limit=None, pt_cut=None, cuts=None):
         if initial_states not in ("gg", "pp"):
             raise ValueError(f"initial_states must be 'gg' or 'pp', not {initial_states!r}")
         self.matrix = PROCESSES[n_gluons](precision=precision)
@@ -84,7 +113,8 @@ class FusedIntegrand:
                         q2=float(mt * mt if q2 is None else (-1.0 if q2 == "dynamic" else q2)),
                         newton_rule=int(newton_rule),
                         initial_states=_lib.MF_INITIAL_PP if initial_states == "pp" else _lib.MF_INITIAL_GG,
-                        events_limit=_limit(events_limit), ptmin_all=float(pt_cut or 0.0))
+                        events_limit=_limit(events_limit), ptmin_all=float(pt_cut or 0.0),
+                        cuts=_cut_table(cuts))
         self._cs = _cfg_struct(self.cfg)
         nd = ctypes.c_int()
         _lib.call("mf_integrand_ndim", self.matrix.handle, ctypes.byref(self._cs), ctypes.byref(nd))

@@ -1094,6 +1094,30 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
   // float32(cut) for every outgoing particle, on the momenta before the boost
   // to the lab frame (phasespace.py:417-422, 458-466)
   const double pt_all = cfgv[12] > 0.0 ? (double)(float)cfgv[12] : 0.0;
+  // PhaseSpaceGenerator.register_cut (phasespace.py:424-478): cfgv[13] cuts,
+  // then per cut variable (0 pt, 1 mt, 2 mt2, 3 eta), particle, has_min,
+  // has_max, min_val, max_val; strict, thresholds through float32, on the
+  // momenta before the boost
+  const int ncuts = (int)cfgv[13];
+  auto pass_table = [&](const double* pe) {
+    for (int c = 0; c < ncuts; ++c) {
+      const double* cv = cfgv + 14 + 6 * c;
+      const double* q = pe + 4 * (int)cv[1];
+      const double pt = std::sqrt(q[1] * q[1] + q[2] * q[2]);
+      double val = pt;
+      const int var = (int)cv[0];
+      if (var == 1 || var == 2) {
+        const double mt2 = (q[0] * q[0] - ((q[1] * q[1] + q[2] * q[2]) + q[3] * q[3])) + pt * pt;
+        val = var == 1 ? std::sqrt(mt2) : mt2;
+      } else if (var == 3) {
+        const double pabs = std::sqrt((q[1] * q[1] + q[2] * q[2]) + q[3] * q[3]);
+        val = 0.5 * std::log((pabs + q[3]) / (pabs - q[3]));
+      }
+      if (cv[2] != 0.0 && !(val > (double)(float)cv[4])) return false;
+      if (cv[3] != 0.0 && !(val < (double)(float)cv[5])) return false;
+    }
+    return true;
+  };
   double gs = 2.0 * std::sqrt(M_PI * cfg.alphas);
   // MT, WT, GC_10 = -g, GC_11 = i g, GC_12 = i g^2, c3 = -i, c4 = -1
   double prm[12] = {cfg.mt, cfg.wt, -gs, 0.0, 0.0, gs, 0.0, gs * gs, 0.0, -1.0, -1.0, 0.0};
@@ -1131,6 +1155,7 @@ extern "C" void orc_integrand(const double* cfgv, void* plan, const double* x, i
         const double* q = &p[(size_t)4 * npart * e + 4 * i];
         if (!(std::sqrt(q[1] * q[1] + q[2] * q[2]) > pt_all)) pass[e] = 0;
       }
+    if (ncuts > 0 && !pass_table(&p[(size_t)4 * npart * e])) pass[e] = 0;
     if (dyn) {
       double smt = 0.0;
       for (int i = 2; i < npart; ++i) {

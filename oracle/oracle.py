@@ -373,16 +373,30 @@ def integrand(cfg, x, plan=None, fast=False):
     """cfg: [kind, k, sqrts, mt, wt, alphas, ptmin, etamax, drmin, newton_rule
     (, initial_states: 0 g g, 1 p p (, dynamic scale: 0 fixed Q = mt, 1
     madflow's sum of m_T / 2 with alphas = alpha_s(M_Z^2) (, pt_all: > 0
-    madflow's --pt_cut on every outgoing particle)))].  fast: the timing
-    build (plan, if given, must come from the same build)."""
+    madflow's --pt_cut on every outgoing particle (, the registered cuts as
+    cut_vector gives them))))].  fast: the timing build (plan, if given,
+    must come from the same build)."""
     if plan is not None:
         fast = plan.fast
-    cfg = list(cfg) + [0] * (13 - len(cfg))
+    cfg = list(cfg) + [0] * (14 - len(cfg))
     x = _c64(x)
     f = np.empty(x.shape[0])
     lib(fast).orc_integrand(_p(_c64(cfg)), ctypes.c_void_p(plan.h if plan is not None else None), _p(x),
                             ctypes.c_int64(x.shape[0]), _p(f))
     return f
+
+
+CUT_VARIABLES = {"pt": 0, "mt": 1, "mt2": 2, "eta": 3}
+
+
+def cut_vector(cuts):
+    """The integrand configuration's tail for registered cuts:
+    (variable, particle, min_val, max_val) tuples (None: no bound)."""
+    out = [len(cuts)]
+    for variable, particle, lo, hi in cuts:
+        out += [CUT_VARIABLES[variable], particle, int(lo is not None), int(hi is not None),
+                0.0 if lo is None else float(lo), 0.0 if hi is None else float(hi)]
+    return out
 
 
 def num_threads(fast=False):
