@@ -87,3 +87,29 @@ def test_integrand_config_layout_matches_header(tmp_path):
     got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     assert got[0] == ctypes.sizeof(_lib.IntegrandConfig)
     assert got[1:] == [getattr(_lib.IntegrandConfig, f).offset for f in fields]
+
+
+def test_config_struct_layout_matches_header(tmp_path):
+    """The ctypes mirror of mf_integrand_config and mf_cut has the size and
+    field offsets a C compiler gives the header's structs."""
+    import shutil
+    import subprocess
+
+    import pytest
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = [f for f, _ in _lib.IntegrandConfig._fields_]
+    src = tmp_path / "layout.c"
+    body = "".join(f'  printf("%zu\\n", offsetof(mf_integrand_config, {f}));\n' for f in fields)
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "madflow_gb300.h"\nint main(void) {\n'
+                   '  printf("%zu\\n%zu\\n", sizeof(mf_integrand_config), sizeof(mf_cut));\n' + body +
+                   '  return 0;\n}\n')
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(__import__("pathlib").Path(_lib.HEADER).parent), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    want = [ctypes.sizeof(_lib.IntegrandConfig), ctypes.sizeof(_lib.Cut)] + [
+        getattr(_lib.IntegrandConfig, f).offset for f in fields]
+    assert got == want
